@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the kpm_1d Chebyshev-moment path on GB300.
+
+Workload (default): kpm_1d DOS at scale on a 3D cubic Anderson model, L=128
+periodic (NH = 2,097,152, 7 nonzeros per row), t = 1, onsite uniform
+[-8.25, 8.25] (W = 16.5), ComplexF64, centred rescaling, NC = 4096 moments,
+NR = 64 random-phase probes.  Synthetic seeded inputs; the vectors (2.1 GB per
+slot) are far larger than L2, so no flush is needed between steps.
+
+A step is one full kpm_1d call (NC/2 = 2048 recurrence launches).  `value` is
+vector-steps/s (NR * NC/2 per call) with the probes resident in HBM, timed with
+CUDA events on the launching stream; `e2e` is the same metric through the
+public host API (pinned host probes copied in, moments copied out, every step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "kpm.jl_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+METRIC = "kpm_1d vector-steps/s"
+UNIT = "vector-steps/s"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--precision", default="ff", choices=["ff", "fp64"])
+    p.add_argument("--L", type=int, default=128)
+    p.add_argument("--W", type=float, default=16.5)
+    p.add_argument("--NC", type=int, default=4096)
+    p.add_argument("--NR", type=int, default=64)
+    p.add_argument("--cpu-steps", type=int, default=16,
+                   help="recurrence steps in the bounded CPU-baseline sample")
+    p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def workload(args, rank):
+    from kpm_gb300 import models, rescale, random_phase_vectors
+    rng = np.random.default_rng(42)
+    H = models.cubic_anderson(args.L, t=1.0, W=args.W, rng=rng)
+    h = rescale(H, center=True)
+    psi = random_phase_vectors(np.random.default_rng(1000 + rank), H.shape[0], args.NR)
+    return h, psi
+
+
+def config(args, scaling_note=None):
+    NH = args.L ** 3
+    return {
+        "workload": (f"kpm_1d DOS, 3D cubic Anderson L={args.L} periodic (NH={NH}, 7 nnz/row), "
+                     f"W={args.W}, centred rescaling, NC={args.NC}, NR={args.NR}"),
+        "NH": NH, "NC": args.NC, "NR": args.NR, "nnz_per_row": 7,
+        "precision": args.precision,
+        "l2": "inputs larger than L2 (2.1 GB per recurrence slot), no flush needed",
+        "step": "one kpm_1d call = NC/2 recurrence launches with fused moments",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = None
+
+    def __enter__(self):
+        try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.f:
+            return None
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return math.nan
+        sm = [num(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" == r[5 + i]})
+        return {"sm_mhz": statistics.median([s for s in sm if not math.isnan(s)] or [0]),
+                "sm_max_mhz": max(num(r[2]) for r in rows), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(num(r[3]) for r in rows)}
+
+
+def measured_hbm():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(precision):
+    """DRAM bytes per step launch from the committed ncu summary, if present."""
+    f = ROOT / "profiles" / f"kpm1d_step_{precision}_traffic.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_full_size:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def cpu_sample(h, psi, args, nthreads):
+    """The C port of the reference CPU algorithm on a bounded sample of the workload."""
+    from oracle import cpu_port
+    steps = max(2, min(args.cpu_steps, args.NC // 2))
+    t0 = time.perf_counter()
+    mu = cpu_port.kpm1d_cpu(h.H, args.NC, psi, nthreads=nthreads, last_n=steps)
+    dt = time.perf_counter() - t0
+    return {"value": args.NR * steps / dt, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": (f"first {steps} of {args.NC // 2} recurrence steps of the same workload "
+                       f"(NR={args.NR} columns each), C/OpenMP restatement of the reference "
+                       f"CPU path, {nthreads} threads"),
+            "seconds": dt}, mu, steps
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference CPU algorithm (C port) on this machine's host cores."""
+    if rank != 0:
+        return
+    from oracle import cpu_port
+    h, psi = workload(args, 0)
+    nthreads = cpu_port.max_threads()
+    for _ in range(args.warmup):
+        cpu_sample(h, psi, args, nthreads)
+    times, vals = [], []
+    for _ in range(args.steps):
+        res, _, steps = cpu_sample(h, psi, args, nthreads)
+        times.append(res["seconds"])
+        vals.append(res["value"])
+    value = args.NR * steps * args.steps / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config(args),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": res["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("KPM.jl is Julia and Julia is not installed; the reference arm runs the "
+                 "C/OpenMP restatement of its CPU algorithm (oracle/kpm_cpu.c)"),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    import torch
+    import torch.distributed as dist
+    import kpm_gb300 as kg
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    h, psi = workload(args, rank)
+    NH, NR, NC = h.H.shape[0], args.NR, args.NC
+    op = kg.GB300Operator(h.H)
+    stream = torch.cuda.current_stream()
+    psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
+
+    def call(prec):
+        kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec, stream=stream)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        call(args.precision)
+    kg.sync(op)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = kg.kernel_launch_count()
+    with ClockSampler(local) as clk:
+        barrier()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            call(args.precision)
+        ev1.record(stream)
+        barrier()
+    launches = kg.kernel_launch_count() - n0
+    kg.sync(op)
+    ms = ev0.elapsed_time(ev1) / args.steps
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    value = world * NR * (NC // 2) / (ms / 1e3)
+    mu_chosen = mu_t.cpu().numpy().T.copy()
+
+    # roofline of the dominant kernel (the fused recurrence step)
+    nnz = h.H.nnz
+    B_step = 48 * NH * NR + 20 * nnz + 4 * (NH + 1)
+    step_launches = (NC // 2) * math.ceil(NR / 128)
+    avg_launch_s = (ms / 1e3) / step_launches
+    peak, peak_kind = measured_hbm()
+    achieved = B_step / avg_launch_s / 1e9
+    traffic = profile_traffic(args.precision)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                else "fallback 6.8 TB/s",
+                "bytes_per_launch": B_step,
+                "avg_launch_ms": avg_launch_s * 1e3}
+
+    # end to end through the public host API: pinned host probes in, moments out
+    e2e = None
+    if not args.no_e2e:
+        pinned = torch.empty((NR, NH), dtype=torch.complex128, pin_memory=True)
+        pinned.numpy()[...] = psi.T
+        host_psi = pinned.numpy().T  # (NH, NR) column-major view of pinned memory
+        mu_host = np.zeros((NR, NC), dtype=np.complex128)
+        kg.kpm_1d_bang(op, NC, NR, NH, mu_host, host_psi, precision=args.precision)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            kg.kpm_1d_bang(op, NC, NR, NH, mu_host, host_psi, precision=args.precision)
+        barrier()
+        te = (time.perf_counter() - t0) / args.steps
+        tt = torch.tensor([te], device="cuda")
+        if world > 1:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        te = float(tt.item())
+        e2e = {"value": world * NR * (NC // 2) / te, "unit": UNIT,
+               "h2d_bytes_per_step": NH * NR * 16, "d2h_bytes_per_step": NR * NC * 16,
+               "ms_per_step": te * 1e3}
+
+    # chosen form vs the plain FP64 path on the same inputs
+    plain = None
+    if not args.no_plain and args.precision != "fp64":
+        mu64 = torch.zeros_like(mu_t)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        kg.kpm_1d_device(op, NC, psi_t, mu64, precision="fp64", stream=stream)
+        e1.record(stream)
+        barrier()
+        kg.sync(op)
+        m64 = mu64.cpu().numpy().T
+        avg_c, avg_p = mu_chosen.mean(0).real, m64.mean(0).real
+        plain = {"ms_per_step": e0.elapsed_time(e1),
+                 "value": NR * (NC // 2) / (e0.elapsed_time(e1) / 1e3),
+                 "speedup_chosen_vs_plain": e0.elapsed_time(e1) / ms,
+                 "moment_rel_err_normwise": float(np.linalg.norm(mu_chosen - m64)
+                                                  / np.linalg.norm(m64)),
+                 "moment_rel_err_max": float(np.max(np.abs(avg_c - avg_p)) / np.max(np.abs(avg_p)))}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle import cpu_port
+        cpu, mu_cpu, steps = cpu_sample(h, psi, args, cpu_port.max_threads())
+        k = 2 * steps
+        cpu["check_rel_err_first_moments"] = float(
+            np.linalg.norm(mu_cpu[:, :k] - mu_chosen[:, :k]) / np.linalg.norm(mu_cpu[:, :k]))
+        cpu.pop("seconds", None)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": ("f64 emulated as float-float on the FP32 pipe" if args.precision == "ff"
+                      else "f64"),
+            "data": "synthetic (seeded 3D Anderson model and random-phase probes)",
+            "config": config(args),
+            "roofline": roofline,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clk.summary(),
+            "plain_fp64": plain,
+            "cpu_baseline": cpu,
+            "version": kg.version(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,164 @@
+/*
+ * kpmgb.h - C ABI of the GB300 Chebyshev-moment library (libkpmgb.so).
+ *
+ * The library replaces the moment engine of KPM.jl (the Chebyshev recurrence,
+ * the fused moment reductions and the kpm_2d moment-matrix contraction).  A
+ * Julia host binds these entry points with `ccall`; the Python mirror binds
+ * them with ctypes.  Signatures use only plain integers, doubles and
+ * pointers.
+ *
+ * Data layouts (all complex values are interleaved re/im doubles, i.e. the
+ * memory layout of Julia's ComplexF64 and NumPy's complex128):
+ *   - operators arrive in compressed-sparse-column form exactly as Julia's
+ *     SparseMatrixCSC stores them (colptr[n+1], rowval[nnz], nzval[nnz]);
+ *     index_base is 1 for Julia arrays and 0 for SciPy arrays;
+ *   - probe blocks psi are NH x NR column-major (column i contiguous);
+ *   - kpm_1d moments mu_all are NR x NC column-major (entry (i, n) at
+ *     i + NR*n), the layout of the reference's `mu_all`;
+ *   - kpm_2d moments mu are NC x NC column-major (entry (n, m) at n + NC*m).
+ *
+ * Every call returns KPMGB_OK (0) or a status class; the message of the last
+ * failure on the calling thread is returned by kpmgb_last_error().  Calls on
+ * distinct operator handles may run concurrently from different threads;
+ * calls sharing a handle are serialised by the library.
+ */
+#ifndef KPMGB_H
+#define KPMGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status classes.  They map onto the reference's Julia exceptions:
+ * ARGUMENT  -> ArgumentError / AssertionError (odd NC in the doubling path
+ *              src/moment.jl:434, shape mismatch :438, bad parity :913-915,
+ *              arr_size < 2 :954, aliasing :519),
+ * NUMERICAL -> ErrorException of the stability guard
+ *              (src/utils/chebyshev_iteration.jl:100-133),
+ * CUDA/ALLOC/TIMEOUT -> ErrorException from the device layer. */
+#define KPMGB_OK 0
+#define KPMGB_ERR_ARGUMENT 1
+#define KPMGB_ERR_NUMERICAL 2
+#define KPMGB_ERR_CUDA 3
+#define KPMGB_ERR_ALLOC 4
+#define KPMGB_ERR_TIMEOUT 5
+
+/* Arithmetic of the recurrence and of the moment reductions.
+ * FP64: native double precision (moments within 1e-12 relative of the CPU
+ *       reference).
+ * FF:   emulated double precision on the FP32 pipe: every vector element is a
+ *       pair of floats (hi + lo, 48-bit significand) and every product and
+ *       sum is error-compensated; the vectors occupy the same 16 bytes per
+ *       complex element as FP64.  Moments agree with FP64 to about 1e-12
+ *       relative and are guaranteed by the tests to 1e-9. */
+#define KPMGB_PREC_FP64 0
+#define KPMGB_PREC_FF 1
+
+/* kpm_2d contraction arithmetic (mu = R L^H over K = NH*NR). */
+#define KPMGB_CONTRACT_FP64 0  /* double-precision SIMT GEMM              */
+#define KPMGB_CONTRACT_SPLIT 1 /* BF16 slices on tcgen05, FP32 accumulate */
+
+/* moment_parity of kpm_2d (src/moment.jl:913-915, :1067-1069). */
+#define KPMGB_PARITY_NONE 0
+#define KPMGB_PARITY_ODD 1
+#define KPMGB_PARITY_EVEN 2
+
+typedef struct kpmgb_operator_s* kpmgb_operator;
+
+typedef struct kpmgb_kpm1d_options {
+  int32_t precision;       /* KPMGB_PREC_*                                    */
+  int32_t stability_check; /* 0: off (reference kpm_1d! semantics); 1: fail
+                              with KPMGB_ERR_NUMERICAL when a moment is not
+                              finite or a column norm grows beyond 1.5x its
+                              seed norm (chebyshev_iteration.jl:110-133)       */
+  int32_t use_graph;       /* 1: replay the recurrence as a CUDA graph        */
+  int32_t reserved;
+} kpmgb_kpm1d_options;
+
+typedef struct kpmgb_kpm2d_options {
+  int64_t arr_size;        /* K_left; 0 = automatic (src/moment.jl:759-810)   */
+  int64_t right_block;     /* K_right; 0 = automatic                          */
+  int64_t workspace_bytes; /* device budget; < 0 = half of free memory        */
+  int32_t moment_parity;   /* KPMGB_PARITY_*                                  */
+  int32_t mn_sym;          /* 1: symmetrise as src/moment.jl:1078-1086        */
+  int32_t precision;       /* recurrence arithmetic, KPMGB_PREC_*             */
+  int32_t contraction;     /* KPMGB_CONTRACT_*                                */
+} kpmgb_kpm2d_options;
+
+/* Library version string, e.g. "kpmgb 0.1.0 (sm_103a)". */
+const char* kpmgb_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* kpmgb_last_error(void);
+
+/* Upload a square sparse operator given in CSC form and keep it resident on
+ * the current CUDA device until kpmgb_operator_destroy.  The library builds
+ * the row-major CSR (a true transpose, the operator need not be Hermitian).
+ * Replaces the per-call `maybe_to_device(H)` conversion of
+ * src/moment.jl:432,1002-1004 / ext/KPMCUDAExt.jl:26-27. */
+int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr,
+                          const int64_t* rowval, const double* nzval,
+                          int32_t index_base, kpmgb_operator* out);
+
+int kpmgb_operator_destroy(kpmgb_operator op);
+
+/* Dimensions of an operator; is_real = 1 when every imaginary part is 0. */
+int kpmgb_operator_info(kpmgb_operator op, int64_t* n, int64_t* nnz,
+                        int32_t* is_real);
+
+/* Equal-vector moments with the doubling identities: the entry point behind
+ * kpm_1d!(H, NC, NR, NH, mu_all, psi_in) (src/moment.jl:420-492).  NC must be
+ * even.  psi: host NH x NR column-major; mu_all: host NR x NC column-major.
+ * Blocking call. */
+int kpmgb_kpm1d(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,
+                const double* psi, double* mu_all,
+                const kpmgb_kpm1d_options* opts);
+
+/* Independent bra/ket moments mu_all[i, n] = <psil_i|T_n(H)|psir_i>: the
+ * entry point behind kpm_1d!(H, NC, NR, NH, mu_all, psi_in_l, psi_in_r)
+ * (src/moment.jl:498-556).  NC >= 2 (odd allowed).  Blocking call. */
+int kpmgb_kpm1d_lr(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,
+                   const double* psi_l, const double* psi_r, double* mu_all,
+                   const kpmgb_kpm1d_options* opts);
+
+/* Moment matrix mu[n, m] = (1/NR) sum_i <T_m psil_i | Jb T_n Ja psir_i>: the
+ * entry point behind kpm_2d!(H, Ja, Jb, NC, NR, NH, mu, psi_in_l, psi_in_r)
+ * (src/moment.jl:887-1088), including moment_parity and mn_sym.  mu is
+ * overwritten (the reference's fill!(mu, 0) at :916).  Blocking call. */
+int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
+                int64_t NC, int64_t NR, int64_t NH, const double* psi_l,
+                const double* psi_r, double* mu,
+                const kpmgb_kpm2d_options* opts);
+
+/* Device-resident forms of the three calls above: psi/psi_l/psi_r and
+ * mu_all/mu are device addresses with the same layouts.  Work is enqueued on
+ * `stream` (a cudaStream_t; NULL = the operator's own stream) and the call
+ * returns without waiting; kpmgb_operator_sync waits and reports a deferred
+ * numerical failure. */
+int kpmgb_kpm1d_device(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,
+                       const void* psi, void* mu_all,
+                       const kpmgb_kpm1d_options* opts, void* stream);
+int kpmgb_kpm1d_lr_device(kpmgb_operator H, int64_t NC, int64_t NR,
+                          int64_t NH, const void* psi_l, const void* psi_r,
+                          void* mu_all, const kpmgb_kpm1d_options* opts,
+                          void* stream);
+int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
+                       int64_t NC, int64_t NR, int64_t NH, const void* psi_l,
+                       const void* psi_r, void* mu,
+                       const kpmgb_kpm2d_options* opts, void* stream);
+
+/* Wait for the work enqueued on an operator and report any deferred failure
+ * flagged by the kernels (non-finite moments, stability guard). */
+int kpmgb_operator_sync(kpmgb_operator op, void* stream);
+
+/* Number of CUDA kernels the library launched since the process started
+ * (instrumentation for benchmarks). */
+int64_t kpmgb_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KPMGB_H */

@@ -1,0 +1,628 @@
+// C ABI of libkpmgb: operator handles and the kpm_1d / kpm_2d drivers.
+//
+// The drivers reproduce the control flow of the reference's moment engine
+// (src/moment.jl) on device-resident data:
+//   kpm_1d!  doubling  src/moment.jl:420-492   -> run_kpm1d(lr = false)
+//   kpm_1d!  bra/ket   src/moment.jl:498-556   -> run_kpm1d(lr = true)
+//   kpm_2d! / _kpm_2d_blocked!  src/moment.jl:887-1088 -> run_kpm2d
+// Differences by design: the operator is uploaded once per handle (the
+// reference converts and uploads it on every call, src/moment.jl:432), the
+// moment reductions are fused into the recurrence kernels, and kpm_2d keeps
+// the whole right chain resident when it fits instead of recomputing it for
+// every left block.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kpmgb_ffmath.cuh"
+#include "kpmgb_internal.h"
+
+namespace kpmgb {
+
+std::atomic<int64_t> g_launches{0};
+
+namespace {
+thread_local std::string t_last_error;
+}
+
+int fail(int code, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_last_error = buf;
+  return code;
+}
+
+void clear_error() { t_last_error.clear(); }
+
+int DevBuf::ensure(size_t need) {
+  if (need <= bytes && ptr) return KPMGB_OK;
+  release();
+  if (need == 0) return KPMGB_OK;
+  cudaError_t e = cudaMalloc(&ptr, need);
+  if (e != cudaSuccess) {
+    ptr = nullptr;
+    bytes = 0;
+    cudaGetLastError();
+    return fail(KPMGB_ERR_ALLOC, "cudaMalloc of %zu bytes failed: %s", need,
+                cudaGetErrorString(e));
+  }
+  bytes = need;
+  return KPMGB_OK;
+}
+
+void DevBuf::release() {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  bytes = 0;
+}
+
+Operator::~Operator() {
+  cudaSetDevice(device);
+  if (stream) cudaStreamSynchronize(stream);
+  DevBuf* bufs[] = {&ws.slots, &ws.bra,  &ws.partials, &ws.sync,  &ws.scales, &ws.mu,
+                    &ws.psi_in, &ws.left, &ws.right,   &ws.ring,  &ws.gemm,   &ws.split};
+  for (DevBuf* b : bufs) b->release();
+  cudaFree(csr.rowptr);
+  cudaFree(csr.col);
+  cudaFree(csr.val);
+  cudaFree(csr.val_real);
+  cudaFree(csr.val_ff);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+namespace {
+
+__global__ void k_split_values(const double2* __restrict__ v, int64_t nnz, int is_real,
+                               void* out, double* real_out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnz;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 h = v[i];
+    const float2 re = ff::split_double(h.x);
+    if (is_real) {
+      static_cast<float2*>(out)[i] = re;
+      real_out[i] = h.x;
+    } else {
+      const float2 im = ff::split_double(h.y);
+      static_cast<float4*>(out)[i] = make_float4(re.x, re.y, im.x, im.y);
+    }
+  }
+}
+
+__global__ void k_mul_scalar(const double* a, const double* b, double* out) { out[0] = a[0] * b[0]; }
+
+struct Guard {
+  Operator* op;
+  std::unique_lock<std::mutex> lk;
+  explicit Guard(Operator* o) : op(o), lk(o->mtx) { cudaSetDevice(o->device); }
+};
+
+int check_status(Operator* op, cudaStream_t s) {
+  unsigned st = 0;
+  KPMGB_CUDA(cudaMemcpyAsync(&st, op->ws.sync.as<unsigned>() + 1, sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, s));
+  KPMGB_CUDA(cudaStreamSynchronize(s));
+  if (st & STATUS_GROWTH)
+    return fail(KPMGB_ERR_NUMERICAL,
+                "Chebyshev recurrence is unstable (a column norm grew beyond 1.5x its seed "
+                "norm); use a larger eps (rescaling safety margin)");
+  if (st & STATUS_NONFINITE)
+    return fail(KPMGB_ERR_NUMERICAL, "non-finite moment produced by the recurrence");
+  return KPMGB_OK;
+}
+
+int ensure_sync(Operator* op, cudaStream_t s) {
+  const bool fresh = op->ws.sync.ptr == nullptr;
+  KPMGB_TRY(op->ws.sync.ensure(64));
+  if (fresh) KPMGB_CUDA(cudaMemsetAsync(op->ws.sync.ptr, 0, 64, s));
+  KPMGB_CUDA(cudaMemsetAsync(op->ws.sync.as<unsigned>() + 1, 0, sizeof(unsigned), s));
+  return KPMGB_OK;
+}
+
+cudaStream_t pick_stream(Operator* op, void* stream) {
+  return stream ? static_cast<cudaStream_t>(stream) : op->stream;
+}
+
+int check_precision(int precision) {
+  if (precision != KPMGB_PREC_FP64 && precision != KPMGB_PREC_FF)
+    return fail(KPMGB_ERR_ARGUMENT, "unknown precision %d", precision);
+  return KPMGB_OK;
+}
+
+// -------------------------------------------------------------- kpm_1d
+int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_l,
+              const void* psi_r, double2* mu, const kpmgb_kpm1d_options* o, cudaStream_t s,
+              bool lr) {
+  const int precision = o ? o->precision : KPMGB_PREC_FP64;
+  KPMGB_TRY(check_precision(precision));
+  if (NR < 1 || NR > (1 << 20)) return fail(KPMGB_ERR_ARGUMENT, "Invalid NR=%lld", (long long)NR);
+  if (NH != op->csr.n)
+    return fail(KPMGB_ERR_ARGUMENT, "Invalid `psi_in` with size (%lld, %lld). Expecting (%lld, %lld)",
+                (long long)NH, (long long)NR, (long long)op->csr.n, (long long)NR);
+  if (lr) {
+    if (NC < 2) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be at least 2.");
+    if (psi_l == psi_r && psi_l == nullptr)
+      return fail(KPMGB_ERR_ARGUMENT, "psi_in_l and psi_in_r must be set");
+  } else {
+    if (NC < 2 || NC % 2 != 0) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be even.");
+  }
+  if (!psi_r || !mu) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
+  Workspace& ws = op->ws;
+  const size_t slot = (size_t)NH * NR * 16;
+  KPMGB_TRY(ws.slots.ensure(2 * slot));
+  if (lr) KPMGB_TRY(ws.bra.ensure(slot));
+  KPMGB_TRY(ws.scales.ensure((size_t)(3 * NR + 2) * sizeof(double)));
+  KPMGB_TRY(ws.partials.ensure(step_partials_bytes(op->csr, NH, (int)NR, precision)));
+  KPMGB_TRY(ensure_sync(op, s));
+  char* slots = ws.slots.as<char>();
+  void* sl[2] = {slots, slots + slot};
+  double* sc = ws.scales.as<double>();
+  const bool ff = precision == KPMGB_PREC_FF;
+  KPMGB_TRY(launch_load_block(psi_r, sl[0], NH, (int)NR, precision, sc, false, s));
+  if (lr) KPMGB_TRY(launch_load_block(psi_l, ws.bra.ptr, NH, (int)NR, precision, sc + NR, false, s));
+  const double* mom_scale = nullptr;
+  if (ff) {
+    KPMGB_TRY(launch_scale_product(sc, lr ? sc + NR : sc, sc + 2 * NR, (int)NR, s));
+    mom_scale = sc + 2 * NR;
+  }
+  StepArgs a;
+  a.H = &op->csr;
+  a.NH = NH;
+  a.NR = (int)NR;
+  a.mu = mu;
+  a.mom_scale = mom_scale;
+  a.sync = ws.sync.as<unsigned>();
+  a.partials = ws.partials.ptr;
+  a.bra = lr ? ws.bra.ptr : nullptr;
+  // alpha_1 = H alpha_0 with mu_0, mu_1 (src/moment.jl:440-449, :521-527)
+  a.x = sl[0];
+  a.z = nullptr;
+  a.y = sl[1];
+  a.alpha = 1.0;
+  a.beta = 0.0;
+  a.dot = lr ? DOT_LR2 : DOT_DOUBLING;
+  a.mom = MOM_STORE;
+  a.i0 = 0;
+  KPMGB_TRY(launch_step(a, precision, s));
+  int ip = 1, ipp = 0;
+  a.alpha = 2.0;
+  a.beta = -1.0;
+  if (!lr) {
+    const bool check = o && o->stability_check;
+    for (int64_t n = 2; n <= NC / 2; ++n) {
+      // alpha_n = 2 H alpha_{n-1} - alpha_{n-2} in place; doubling moments
+      // mu_{2n-2}, mu_{2n-1} (src/moment.jl:460-487)
+      a.x = sl[ip];
+      a.z = sl[ipp];
+      a.y = sl[ipp];
+      a.dot = DOT_DOUBLING;
+      a.mom = MOM_DOUBLING;
+      a.i0 = 2 * n - 2;
+      a.growth_limit = check ? 2.25 : 0.0;
+      KPMGB_TRY(launch_step(a, precision, s));
+      std::swap(ip, ipp);
+    }
+  } else {
+    for (int64_t n = 2; n < NC; ++n) {
+      // full recurrence, mu_n = <psil|alpha_n> (src/moment.jl:540-549)
+      a.x = sl[ip];
+      a.z = sl[ipp];
+      a.y = sl[ipp];
+      a.dot = DOT_LR1;
+      a.mom = MOM_STORE;
+      a.i0 = n;
+      KPMGB_TRY(launch_step(a, precision, s));
+      std::swap(ip, ipp);
+    }
+  }
+  return KPMGB_OK;
+}
+
+// -------------------------------------------------------------- kpm_2d
+int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, int64_t NH,
+              const void* psi_l, const void* psi_r, double2* mu, const kpmgb_kpm2d_options* o,
+              cudaStream_t s) {
+  kpmgb_kpm2d_options d{};
+  d.workspace_bytes = -1;
+  const kpmgb_kpm2d_options& opt = o ? *o : d;
+  KPMGB_TRY(check_precision(opt.precision));
+  if (opt.moment_parity < 0 || opt.moment_parity > 2)
+    return fail(KPMGB_ERR_ARGUMENT, "moment_parity=%d not understood.", opt.moment_parity);
+  if (opt.contraction != KPMGB_CONTRACT_FP64 && opt.contraction != KPMGB_CONTRACT_SPLIT)
+    return fail(KPMGB_ERR_ARGUMENT, "unknown contraction %d", opt.contraction);
+  if (NC < 2) return fail(KPMGB_ERR_ARGUMENT, "NC must be at least 2 (got %lld)", (long long)NC);
+  if (NR < 1 || NR > (1 << 20)) return fail(KPMGB_ERR_ARGUMENT, "NR must be positive");
+  if (NH != H->csr.n || NH != Ja->csr.n || NH != Jb->csr.n)
+    return fail(KPMGB_ERR_ARGUMENT, "`psi_in_r` has %lld rows but the operators are %lld x %lld",
+                (long long)NH, (long long)H->csr.n, (long long)H->csr.n);
+  if (opt.arr_size != 0 && opt.arr_size < 2)
+    return fail(KPMGB_ERR_ARGUMENT, "arr_size must be :auto or an integer at least 2");
+  if (opt.right_block < 0)
+    return fail(KPMGB_ERR_ARGUMENT, "right_block must be :auto or a positive integer");
+  if (!psi_l || !psi_r || !mu) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
+  if (NC > (1 << 20)) return fail(KPMGB_ERR_ARGUMENT, "NC too large");
+  const int precision = opt.precision;
+  const bool ff = precision == KPMGB_PREC_FF;
+  Workspace& ws = H->ws;
+  const size_t block = (size_t)NH * NR * 16;
+  const int64_t K = NH * NR;
+
+  // Block sizes: explicit values are honoured (results are blocking
+  // invariant); otherwise keep both chains resident when the budget allows
+  // (src/moment.jl:759-810 for the reference's rule).
+  size_t budget;
+  if (opt.workspace_bytes >= 0) {
+    budget = (size_t)opt.workspace_bytes;
+  } else {
+    size_t fr = 0, tot = 0;
+    KPMGB_CUDA(cudaMemGetInfo(&fr, &tot));
+    budget = fr / 2;
+  }
+  int64_t KR = opt.right_block > 0 ? opt.right_block : 0;
+  int64_t KL = opt.arr_size > 0 ? opt.arr_size : 0;
+  if (KL == 0 || KR == 0) {
+    const int64_t kr_auto = KR ? KR : NC;
+    const size_t full = (size_t)(NC + kr_auto + 4) * block +
+                        contract_scratch_bytes(K, (int)std::min<int64_t>(kr_auto, NC), (int)NC,
+                                               precision, opt.contraction);
+    if (full <= budget) {
+      if (!KR) KR = NC;
+      if (!KL) KL = NC;
+    } else {
+      if (!KR) KR = std::min<int64_t>(NC, 16);
+      if (!KL) {
+        const int64_t base = (KR + 7) * (int64_t)block;
+        const int64_t per_left = (int64_t)block + KR * 16;
+        const int64_t kl = ((int64_t)budget - base) / per_left;
+        if (kl < 2)
+          return fail(KPMGB_ERR_ARGUMENT,
+                      "workspace_bytes=%zu cannot fit the minimum kpm_2d workspace", budget);
+        KL = std::min<int64_t>(kl, NC);
+      }
+    }
+  }
+  const int64_t KLa = std::min<int64_t>(KL, NC), KRa = std::min<int64_t>(KR, NC);
+  KPMGB_TRY(ws.left.ensure(KLa * block));
+  KPMGB_TRY(ws.right.ensure(KRa * block));
+  KPMGB_TRY(ws.ring.ensure(4 * block));
+  KPMGB_TRY(ws.scales.ensure((size_t)(2 * NR + 8) * sizeof(double)));
+  KPMGB_TRY(ws.partials.ensure(step_partials_bytes(H->csr, NH, (int)NR, precision)));
+  const size_t cs = contract_scratch_bytes(K, (int)KRa, (int)KLa, precision, opt.contraction);
+  KPMGB_TRY(ws.gemm.ensure(cs));
+  KPMGB_TRY(ensure_sync(H, s));
+  KPMGB_CUDA(cudaMemsetAsync(mu, 0, (size_t)NC * NC * sizeof(double2), s));
+
+  auto L = [&](int64_t i) { return (void*)(ws.left.as<char>() + i * block); };
+  auto R = [&](int64_t i) { return (void*)(ws.right.as<char>() + i * block); };
+  auto RING = [&](int64_t i) { return (void*)(ws.ring.as<char>() + i * block); };
+  double* sc = ws.scales.as<double>();
+  // ff: one power-of-two factor per probe block (the contraction sums over
+  // columns, so all columns of a block share it)
+  KPMGB_TRY(launch_load_block(psi_l, L(0), NH, (int)NR, precision, sc, true, s));
+  KPMGB_TRY(launch_load_block(psi_r, R(0), NH, (int)NR, precision, sc + NR + 1, true, s));
+  const double* dscale = nullptr;
+  if (ff) {
+    k_mul_scalar<<<1, 1, 0, s>>>(sc + NR, sc + 2 * NR + 1, sc + 2 * NR + 4);
+    KPMGB_LAUNCHED();
+    dscale = sc + 2 * NR + 4;
+  }
+  auto apply = [&](const DeviceCSR* op, const void* x, const void* z, void* y, double alpha,
+                   double beta) {
+    StepArgs a;
+    a.H = op;
+    a.NH = NH;
+    a.NR = (int)NR;
+    a.x = x;
+    a.z = z;
+    a.y = y;
+    a.alpha = alpha;
+    a.beta = beta;
+    a.sync = ws.sync.as<unsigned>();
+    a.partials = ws.partials.ptr;
+    return launch_step(a, precision, s);
+  };
+  // right seed Ja psi_r -> ring slot 3 (src/moment.jl:1021)
+  KPMGB_TRY(apply(&Ja->csr, R(0), nullptr, RING(3), 1.0, 0.0));
+  // left seed psi_l, H psi_l (src/moment.jl:1013-1018)
+  if (KLa >= 2) KPMGB_TRY(apply(&H->csr, L(0), nullptr, L(1), 1.0, 0.0));
+
+  // right chain v_n = T_n(H) Ja psi_r (v_0 in ring slot 3, v_n in slot n%3),
+  // right block entries Jb v_n (src/moment.jl:1034-1052)
+  int64_t chain_n = -1;
+  auto right_vec = [&](int64_t n) -> void* { return n == 0 ? RING(3) : RING(n % 3); };
+  auto advance_chain_to = [&](int64_t n) -> int {
+    if (n < chain_n) chain_n = -1;  // restart from v_0
+    while (chain_n < n) {
+      const int64_t m = chain_n + 1;
+      if (m == 0) {
+      } else if (m == 1) {
+        KPMGB_TRY(apply(&H->csr, RING(3), nullptr, RING(1), 1.0, 0.0));
+      } else {
+        KPMGB_TRY(apply(&H->csr, right_vec(m - 1), right_vec(m - 2), RING(m % 3), 2.0, -1.0));
+      }
+      chain_n = m;
+    }
+    return KPMGB_OK;
+  };
+  auto fill_right = [&](int64_t n1, int64_t n2) -> int {
+    for (int64_t n = n1; n <= n2; ++n) {
+      KPMGB_TRY(advance_chain_to(n));
+      KPMGB_TRY(apply(&Jb->csr, right_vec(n), nullptr, R(n - n1), 1.0, 0.0));
+    }
+    return KPMGB_OK;
+  };
+  const bool right_resident = KRa >= NC;
+  if (right_resident) {
+    chain_n = -1;
+    KPMGB_TRY(fill_right(0, NC - 1));
+  }
+  const int64_t reps = (NC + KL - 1) / KL;
+  for (int64_t rep = 0; rep < reps; ++rep) {
+    const int64_t m1 = rep * KL;
+    const int64_t m2 = std::min<int64_t>(m1 + KL, NC);  // exclusive
+    const int64_t rep_size = m2 - m1;
+    for (int64_t i = 2; i < rep_size; ++i)
+      KPMGB_TRY(apply(&H->csr, L(i - 1), L(i - 2), L(i), 2.0, -1.0));
+    const int64_t nmax = opt.mn_sym ? m2 : NC;  // exclusive
+    for (int64_t n1 = 0; n1 < nmax; n1 += KR) {
+      const int64_t n2 = std::min<int64_t>(n1 + KR, nmax);  // exclusive
+      if (!right_resident) {
+        chain_n = n1 == 0 ? -1 : chain_n;
+        KPMGB_TRY(fill_right(n1, n2 - 1));
+      }
+      ContractArgs c;
+      c.R = right_resident ? R(n1) : R(0);
+      c.L = L(0);
+      c.K = K;
+      c.nr = (int)(n2 - n1);
+      c.nl = (int)rep_size;
+      c.n0 = (int)n1;
+      c.m0 = (int)m1;
+      c.NC = (int)NC;
+      c.inv_nr = 1.0 / (double)NR;
+      c.dscale = dscale;
+      c.parity = opt.moment_parity;
+      c.nmax_row = (int)nmax;
+      c.mu = mu;
+      c.scratch = ws.gemm.ptr;
+      c.scratch_bytes = ws.gemm.bytes;
+      KPMGB_TRY(launch_contract(c, precision, opt.contraction, s));
+    }
+    if (rep < reps - 1) {
+      // continue the left chain past the ring (chebyshev_iter_wrap,
+      // src/utils/chebyshev_iteration.jl:31-34)
+      KPMGB_TRY(apply(&H->csr, L(KL - 1), L(KL - 2), L(0), 2.0, -1.0));
+      KPMGB_TRY(apply(&H->csr, L(0), L(KL - 1), L(1), 2.0, -1.0));
+    }
+  }
+  if (opt.mn_sym) KPMGB_TRY(launch_mn_sym(mu, (int)NC, s));
+  return KPMGB_OK;
+}
+
+Operator* as_op(kpmgb_operator h) { return reinterpret_cast<Operator*>(h); }
+
+}  // namespace
+}  // namespace kpmgb
+
+using namespace kpmgb;
+
+extern "C" {
+
+const char* kpmgb_version(void) { return "kpmgb 0.1.0 (sm_103a)"; }
+
+const char* kpmgb_last_error(void) { return t_last_error.c_str(); }
+
+int64_t kpmgb_kernel_launch_count(void) { return g_launches.load(); }
+
+int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const int64_t* rowval,
+                          const double* nzval, int32_t index_base, kpmgb_operator* out) {
+  clear_error();
+  if (!out) return fail(KPMGB_ERR_ARGUMENT, "out is null");
+  *out = nullptr;
+  if (n < 1 || n >= (int64_t(1) << 31)) return fail(KPMGB_ERR_ARGUMENT, "invalid dimension %lld", (long long)n);
+  if (nnz < 0 || nnz >= (int64_t(1) << 31)) return fail(KPMGB_ERR_ARGUMENT, "invalid nnz %lld", (long long)nnz);
+  if (index_base != 0 && index_base != 1) return fail(KPMGB_ERR_ARGUMENT, "index_base must be 0 or 1");
+  if (!colptr || (nnz > 0 && (!rowval || !nzval))) return fail(KPMGB_ERR_ARGUMENT, "null array");
+  if (colptr[0] != index_base || colptr[n] - index_base != nnz)
+    return fail(KPMGB_ERR_ARGUMENT, "colptr is inconsistent with nnz");
+  // CSC -> CSR (a true transpose; rows come out sorted by column)
+  std::vector<int> rowptr(n + 1, 0);
+  for (int64_t j = 0; j < n; ++j) {
+    const int64_t a = colptr[j] - index_base, b = colptr[j + 1] - index_base;
+    if (b < a || a < 0 || b > nnz) return fail(KPMGB_ERR_ARGUMENT, "colptr is not monotone");
+    for (int64_t k = a; k < b; ++k) {
+      const int64_t i = rowval[k] - index_base;
+      if (i < 0 || i >= n) return fail(KPMGB_ERR_ARGUMENT, "row index out of range");
+      rowptr[i + 1]++;
+    }
+  }
+  int max_nnz = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    max_nnz = std::max(max_nnz, rowptr[i + 1]);
+    rowptr[i + 1] += rowptr[i];
+  }
+  std::vector<int> col(nnz);
+  std::vector<double> val(2 * nnz);
+  std::vector<int> fillp(rowptr.begin(), rowptr.end() - 1);
+  int is_real = 1;
+  for (int64_t j = 0; j < n; ++j) {
+    for (int64_t k = colptr[j] - index_base; k < colptr[j + 1] - index_base; ++k) {
+      const int64_t i = rowval[k] - index_base;
+      const int dst = fillp[i]++;
+      col[dst] = (int)j;
+      val[2 * dst] = nzval[2 * k];
+      val[2 * dst + 1] = nzval[2 * k + 1];
+      if (nzval[2 * k + 1] != 0.0) is_real = 0;
+    }
+  }
+  Operator* op = new Operator();
+  cudaGetDevice(&op->device);
+  auto cleanup = [&](int rc) {
+    delete op;
+    return rc;
+  };
+  DeviceCSR& c = op->csr;
+  c.n = n;
+  c.nnz = nnz;
+  c.is_real = is_real;
+  c.max_row_nnz = max_nnz;
+  const size_t nz = (size_t)std::max<int64_t>(nnz, 1);
+#define CREATE_CUDA(call)                                                                   \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return cleanup(fail(e_ == cudaErrorMemoryAllocation ? KPMGB_ERR_ALLOC : KPMGB_ERR_CUDA, \
+                          "%s failed: %s", #call, cudaGetErrorString(e_)));                 \
+  } while (0)
+  CREATE_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
+  CREATE_CUDA(cudaMalloc(&c.rowptr, (n + 1) * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&c.col, nz * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&c.val, nz * sizeof(double2)));
+  if (is_real) CREATE_CUDA(cudaMalloc(&c.val_real, nz * sizeof(double)));
+  CREATE_CUDA(cudaMalloc(&c.val_ff, nz * (is_real ? sizeof(float2) : sizeof(float4))));
+  CREATE_CUDA(cudaMemcpy(c.rowptr, rowptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  if (nnz > 0) {
+    CREATE_CUDA(cudaMemcpy(c.col, col.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
+    CREATE_CUDA(cudaMemcpy(c.val, val.data(), nnz * sizeof(double2), cudaMemcpyHostToDevice));
+    const int blocks = (int)std::min<int64_t>((nnz + 255) / 256, 4096);
+    k_split_values<<<blocks, 256, 0, op->stream>>>(c.val, nnz, is_real, c.val_ff, c.val_real);
+    g_launches.fetch_add(1);
+    CREATE_CUDA(cudaGetLastError());
+    CREATE_CUDA(cudaStreamSynchronize(op->stream));
+  }
+#undef CREATE_CUDA
+  *out = reinterpret_cast<kpmgb_operator>(op);
+  return KPMGB_OK;
+}
+
+int kpmgb_operator_destroy(kpmgb_operator h) {
+  clear_error();
+  if (!h) return KPMGB_OK;
+  Operator* op = as_op(h);
+  { std::lock_guard<std::mutex> lk(op->mtx); }
+  delete op;
+  return KPMGB_OK;
+}
+
+int kpmgb_operator_info(kpmgb_operator h, int64_t* n, int64_t* nnz, int32_t* is_real) {
+  clear_error();
+  if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  Operator* op = as_op(h);
+  if (n) *n = op->csr.n;
+  if (nnz) *nnz = op->csr.nnz;
+  if (is_real) *is_real = op->csr.is_real;
+  return KPMGB_OK;
+}
+
+int kpmgb_operator_sync(kpmgb_operator h, void* stream) {
+  clear_error();
+  if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  Operator* op = as_op(h);
+  Guard g(op);
+  if (!op->ws.sync.ptr) {
+    KPMGB_CUDA(cudaStreamSynchronize(pick_stream(op, stream)));
+    return KPMGB_OK;
+  }
+  return check_status(op, pick_stream(op, stream));
+}
+
+int kpmgb_kpm1d_device(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const void* psi,
+                       void* mu_all, const kpmgb_kpm1d_options* opts, void* stream) {
+  clear_error();
+  if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  Operator* op = as_op(h);
+  Guard g(op);
+  return run_kpm1d(op, NC, NR, NH, nullptr, psi, static_cast<double2*>(mu_all), opts,
+                   pick_stream(op, stream), false);
+}
+
+int kpmgb_kpm1d_lr_device(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH,
+                          const void* psi_l, const void* psi_r, void* mu_all,
+                          const kpmgb_kpm1d_options* opts, void* stream) {
+  clear_error();
+  if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  if (!psi_l || !psi_r) return fail(KPMGB_ERR_ARGUMENT, "must set both `psi_in_l` and `psi_in_r`");
+  Operator* op = as_op(h);
+  Guard g(op);
+  return run_kpm1d(op, NC, NR, NH, psi_l, psi_r, static_cast<double2*>(mu_all), opts,
+                   pick_stream(op, stream), true);
+}
+
+static int host_kpm1d(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const double* psi_l,
+                      const double* psi_r, double* mu_all, const kpmgb_kpm1d_options* opts,
+                      bool lr) {
+  clear_error();
+  if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  if (!psi_r || !mu_all || (lr && !psi_l)) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
+  if (NR < 1 || NH < 1 || NC < 0) return fail(KPMGB_ERR_ARGUMENT, "invalid sizes");
+  Operator* op = as_op(h);
+  Guard g(op);
+  cudaStream_t s = op->stream;
+  const size_t slot = (size_t)NH * NR * 16;
+  KPMGB_TRY(op->ws.psi_in.ensure(lr ? 2 * slot : slot));
+  KPMGB_TRY(op->ws.mu.ensure((size_t)NR * std::max<int64_t>(NC, 1) * 16));
+  char* in = op->ws.psi_in.as<char>();
+  KPMGB_CUDA(cudaMemcpyAsync(in, psi_r, slot, cudaMemcpyHostToDevice, s));
+  if (lr) KPMGB_CUDA(cudaMemcpyAsync(in + slot, psi_l, slot, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(run_kpm1d(op, NC, NR, NH, lr ? in + slot : nullptr, in, op->ws.mu.as<double2>(), opts,
+                      s, lr));
+  KPMGB_CUDA(cudaMemcpyAsync(mu_all, op->ws.mu.ptr, (size_t)NR * NC * 16, cudaMemcpyDeviceToHost, s));
+  return check_status(op, s);
+}
+
+int kpmgb_kpm1d(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const double* psi,
+                double* mu_all, const kpmgb_kpm1d_options* opts) {
+  return host_kpm1d(h, NC, NR, NH, nullptr, psi, mu_all, opts, false);
+}
+
+int kpmgb_kpm1d_lr(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const double* psi_l,
+                   const double* psi_r, double* mu_all, const kpmgb_kpm1d_options* opts) {
+  if (!psi_l || !psi_r) {
+    clear_error();
+    return fail(KPMGB_ERR_ARGUMENT, "must set both `psi_in_l` and `psi_in_r` or neither.");
+  }
+  return host_kpm1d(h, NC, NR, NH, psi_l, psi_r, mu_all, opts, true);
+}
+
+int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t NC,
+                       int64_t NR, int64_t NH, const void* psi_l, const void* psi_r, void* mu,
+                       const kpmgb_kpm2d_options* opts, void* stream) {
+  clear_error();
+  if (!H || !Ja || !Jb) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  Operator* op = as_op(H);
+  Guard g(op);
+  return run_kpm2d(op, as_op(Ja), as_op(Jb), NC, NR, NH, psi_l, psi_r, static_cast<double2*>(mu),
+                   opts, pick_stream(op, stream));
+}
+
+int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t NC, int64_t NR,
+                int64_t NH, const double* psi_l, const double* psi_r, double* mu,
+                const kpmgb_kpm2d_options* opts) {
+  clear_error();
+  if (!H || !Ja || !Jb) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  if (!psi_l || !psi_r || !mu) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
+  if (NR < 1 || NH < 1 || NC < 2)
+    return fail(KPMGB_ERR_ARGUMENT, "NC must be at least 2 (got %lld)", (long long)NC);
+  Operator* op = as_op(H);
+  Guard g(op);
+  cudaStream_t s = op->stream;
+  const size_t slot = (size_t)NH * NR * 16;
+  KPMGB_TRY(op->ws.psi_in.ensure(2 * slot));
+  KPMGB_TRY(op->ws.mu.ensure((size_t)NC * NC * 16));
+  char* in = op->ws.psi_in.as<char>();
+  KPMGB_CUDA(cudaMemcpyAsync(in, psi_l, slot, cudaMemcpyHostToDevice, s));
+  KPMGB_CUDA(cudaMemcpyAsync(in + slot, psi_r, slot, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(run_kpm2d(op, as_op(Ja), as_op(Jb), NC, NR, NH, in, in + slot, op->ws.mu.as<double2>(),
+                      opts, s));
+  KPMGB_CUDA(cudaMemcpyAsync(mu, op->ws.mu.ptr, (size_t)NC * NC * 16, cudaMemcpyDeviceToHost, s));
+  return check_status(op, s);
+}
+
+}  // extern "C"

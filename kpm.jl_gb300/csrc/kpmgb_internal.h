@@ -1,0 +1,190 @@
+// Internal declarations shared by the translation units of libkpmgb.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstddef>
+#include <cstdint>
+#include <mutex>
+#include <string>
+
+#include "kpmgb.h"
+
+namespace kpmgb {
+
+// ---------------------------------------------------------------- errors
+int fail(int code, const char* fmt, ...);
+void clear_error();
+extern std::atomic<int64_t> g_launches;
+
+#define KPMGB_CUDA(call)                                                       \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return ::kpmgb::fail(e_ == cudaErrorMemoryAllocation ? KPMGB_ERR_ALLOC    \
+                                                           : KPMGB_ERR_CUDA,   \
+                           "%s failed: %s (%s:%d)", #call,                     \
+                           cudaGetErrorString(e_), __FILE__, __LINE__);        \
+  } while (0)
+
+#define KPMGB_TRY(expr)        \
+  do {                         \
+    int rc_ = (expr);          \
+    if (rc_ != KPMGB_OK)       \
+      return rc_;              \
+  } while (0)
+
+// Launch bookkeeping: every kernel launch goes through this macro so that
+// launch errors are caught at the call site and counted.
+#define KPMGB_LAUNCHED()                                                     \
+  do {                                                                       \
+    ::kpmgb::g_launches.fetch_add(1, std::memory_order_relaxed);             \
+    cudaError_t le_ = cudaGetLastError();                                    \
+    if (le_ != cudaSuccess)                                                  \
+      return ::kpmgb::fail(KPMGB_ERR_CUDA, "kernel launch failed: %s (%s:%d)", \
+                           cudaGetErrorString(le_), __FILE__, __LINE__);     \
+  } while (0)
+
+// ------------------------------------------------------------- resources
+// Grow-only device buffer owned by an operator handle.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need);
+  void release();
+  template <typename T>
+  T* as() const { return static_cast<T*>(ptr); }
+};
+
+// Row-major CSR of one operator, resident on the device.
+//   val    : complex FP64 values (double2)
+//   val_ff : float-float values; complex -> float4 (re.hi, re.lo, im.hi,
+//            im.lo); real operators -> float2 (hi, lo) packed in the same
+//            allocation.
+struct DeviceCSR {
+  int64_t n = 0;
+  int64_t nnz = 0;
+  int* rowptr = nullptr;
+  int* col = nullptr;
+  double2* val = nullptr;
+  double* val_real = nullptr;  // real parts only, when is_real
+  void* val_ff = nullptr;
+  int is_real = 0;
+  int max_row_nnz = 0;
+};
+
+// Device status words written by kernels (read back by the host at sync).
+enum StatusBits : unsigned {
+  STATUS_NONFINITE = 1u,
+  STATUS_GROWTH = 2u,
+};
+
+struct Workspace {
+  DevBuf slots;      // recurrence vectors, row-major NH x NR (16 B elements)
+  DevBuf bra;        // bra block for the l/r path
+  DevBuf partials;   // per-block moment partial sums
+  DevBuf sync;       // [0] ticket counter, [1] status bits, [2..] spare
+  DevBuf scales;     // per-column scale factors (float-float path)
+  DevBuf mu;         // moments on the device (host-variant staging)
+  DevBuf psi_in;     // staging for host probe blocks
+  DevBuf left;       // kpm_2d left Chebyshev block
+  DevBuf right;      // kpm_2d right block (Jb T_n Ja psi_r)
+  DevBuf ring;       // kpm_2d right recurrence ring (3 slots)
+  DevBuf gemm;       // kpm_2d contraction partials
+  DevBuf split;      // kpm_2d split-precision operand slices
+};
+
+struct Operator {
+  DeviceCSR csr;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mtx;
+  Workspace ws;
+  ~Operator();
+};
+
+// ------------------------------------------------------ recurrence kernels
+enum DotMode : int {
+  DOT_NONE = 0,      // no reductions
+  DOT_DOUBLING = 1,  // d0 = <x|x>, d1 = <x|y>
+  DOT_LR2 = 2,       // d0 = <b|x>, d1 = <b|y>
+  DOT_LR1 = 3,       // d0 = <b|y>
+};
+
+enum MomentMode : int {
+  MOM_NONE = 0,
+  MOM_STORE = 1,     // mu[i0 + d] = d_d                        (d = 0..ND-1)
+  MOM_DOUBLING = 2,  // mu[i0] = 2 d0 - mu[0], mu[i0+1] = 2 d1 - mu[1]
+};
+
+// One application of the recurrence y = alpha * H x + beta * z to a row-major
+// NH x NR block, with the moment reductions of `dot` fused in.
+struct StepArgs {
+  const DeviceCSR* H = nullptr;
+  int64_t NH = 0;
+  int NR = 0;
+  const void* x = nullptr;   // must not alias y
+  const void* z = nullptr;   // may alias y (in-place recurrence), unused if beta == 0
+  void* y = nullptr;
+  double alpha = 1.0;
+  double beta = 0.0;
+  const void* bra = nullptr;
+  int dot = DOT_NONE;
+  int mom = MOM_NONE;
+  int64_t i0 = 0;            // moment index written by this step
+  double2* mu = nullptr;     // device moments [NC][NR]
+  const double* mom_scale = nullptr;  // per-column factor applied to the dots
+  double growth_limit = 0.0; // >0: flag if <x|x> > growth_limit * mu[0] (doubling)
+  unsigned* sync = nullptr;  // ticket counter + status word
+  void* partials = nullptr;
+};
+
+// precision: KPMGB_PREC_FP64 or KPMGB_PREC_FF.  Returns KPMGB_OK or an error.
+int launch_step(const StepArgs& a, int precision, cudaStream_t s);
+// Bytes of partial-sum scratch that launch_step needs for this shape.
+size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision);
+
+// Column-major (NH x NR, complex double) -> row-major slot, converting to the
+// working precision.  For KPMGB_PREC_FF each column is also multiplied by a
+// power of two (written to col_scale, may be null for FP64) that brings its
+// norm near 1.
+// With `uniform`, all columns share the largest factor (written to
+// col_scale[0..NR] and col_scale[NR]).
+int launch_load_block(const void* psi_colmajor, void* slot, int64_t NH, int NR,
+                      int precision, double* col_scale, bool uniform,
+                      cudaStream_t s);
+
+// Moment-scale helpers for the float-float path.
+int launch_scale_product(const double* sa, const double* sb, double* out, int NR,
+                         cudaStream_t s);
+// mu (NC x NR rows of complex) -> caller layout, multiplying by nothing; used
+// when the caller wants the moments in a separate device buffer.
+int launch_copy_moments(const double2* src, double2* dst, int64_t count,
+                        cudaStream_t s);
+
+// ------------------------------------------------------ kpm_2d contraction
+// mu[n0 + a, m0 + b] += parity-masked (1/NR) sum_k R[a][k] conj(L[b][k]) for
+// a < nr, b < nl.  R and L are blocks of row-major vectors of K complex
+// elements in the working precision of the recurrence.
+struct ContractArgs {
+  const void* R = nullptr;
+  const void* L = nullptr;
+  int64_t K = 0;          // complex elements per vector (NH * NR)
+  int nr = 0, nl = 0;     // vectors in each block
+  int n0 = 0, m0 = 0;     // global moment offsets
+  int NC = 0;
+  double inv_nr = 1.0;
+  const double* dscale = nullptr;  // optional device scalar multiplying the block
+  int parity = KPMGB_PARITY_NONE;
+  int nmax_row = 0;       // only rows n < nmax_row are written (mn_sym)
+  double2* mu = nullptr;  // device NC x NC column-major, accumulated into
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+};
+int launch_contract(const ContractArgs& a, int precision, int contraction,
+                    cudaStream_t s);
+size_t contract_scratch_bytes(int64_t K, int nr, int nl, int precision, int contraction);
+int launch_mn_sym(double2* mu, int NC, cudaStream_t s);
+
+}  // namespace kpmgb

@@ -1,0 +1,269 @@
+// Chebyshev recurrence kernels with fused moment reductions.
+//
+// One launch applies y = alpha * H x + beta * z to a row-major NH x NR block
+// (row r holds the NR probe columns contiguously), which is the GPU form of
+// chebyshev_iter_single (src/utils/chebyshev_iteration.jl:59-75,
+// ext/KPMCUDAExt.jl:84-88), and in the same pass accumulates the column-wise
+// inner products that the reference computes with separate columnwise_dot!
+// passes (src/utils/vectors.jl:103-117, ext/KPMCUDAExt.jl:128-145).
+//
+// Thread mapping: a group of LPR consecutive lanes owns one row; lane g of the
+// group owns columns g, g + LPR, ..., g + (CPL-1) LPR.  For NR = 64 a full
+// warp owns a row and every neighbour's row of x is read as two coalesced
+// 512-byte warp loads (16 bytes per lane).  The operator row (column indices
+// and values) is read once per group and broadcast.
+//
+// Reductions are deterministic: warp shuffles, then a fixed-order sum over the
+// warps of a block, per-block partials in global memory, and a fixed-order
+// sum over blocks performed by the last block to finish (ticket counter).
+// The grid size is a pure function of the problem shape, so two identical
+// calls give bitwise-identical moments.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <unordered_map>
+
+#include "kpmgb_step.cuh"
+
+namespace kpmgb {
+namespace {
+
+using namespace step;
+
+// --------------------------------------------------------------- dispatch
+Shape pick_shape(int ncols) {
+  if (ncols <= 1) return {1, 1};
+  if (ncols <= 2) return {2, 1};
+  if (ncols <= 4) return {4, 1};
+  if (ncols <= 8) return {8, 1};
+  if (ncols <= 12) return {4, 3};
+  if (ncols <= 16) return {16, 1};
+  if (ncols <= 32) return {32, 1};
+  if (ncols <= 64) return {32, 2};
+  return {32, 4};
+}
+
+KernelFn select_kernel(Shape s, int precision, int dot, bool real) {
+  return precision == KPMGB_PREC_FF ? select_kernel_ff(s, dot, real)
+                                    : select_kernel_f64(s, dot, real);
+}
+
+int num_sms() {
+  static int sms = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 1;
+  }();
+  return sms;
+}
+
+// Grid size: resident blocks per SM times the SM count, capped by the number
+// of row tiles.  Depends only on the kernel and the shape (determinism).
+int blocks_per_sm(KernelFn fn) {
+  static std::mutex m;
+  static std::unordered_map<const void*, int> cache;
+  std::lock_guard<std::mutex> lk(m);
+  auto it = cache.find((const void*)fn);
+  if (it != cache.end()) return it->second;
+  int per_sm = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0) != cudaSuccess)
+    per_sm = 1;
+  per_sm = std::max(per_sm, 1);
+  cache.emplace((const void*)fn, per_sm);
+  return per_sm;
+}
+
+int grid_for(KernelFn fn, int64_t NH, int lpr) {
+  const int per_sm = blocks_per_sm(fn);
+  const int64_t groups = kThreads / lpr;
+  const int64_t tiles = (NH + groups - 1) / groups;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)per_sm * num_sms()));
+}
+
+}  // namespace
+
+size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision) {
+  size_t worst = 0;
+  for (int c0 = 0; c0 < NR; c0 += kMaxCols) {
+    const int ncols = std::min(kMaxCols, NR - c0);
+    const Shape s = pick_shape(ncols);
+    for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
+      KernelFn fn = select_kernel(s, precision, dot, H.is_real != 0);
+      const int G = grid_for(fn, NH, s.lpr);
+      worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
+    }
+  }
+  return worst;
+}
+
+int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
+  const DeviceCSR& H = *a.H;
+  if (precision == KPMGB_PREC_FF) {
+    const double al = std::fabs(a.alpha);
+    int e = 0;
+    const double m = std::frexp(al, &e);
+    if (!(m == 0.5) || !(a.beta == 0.0 || a.beta == 1.0 || a.beta == -1.0))
+      return fail(KPMGB_ERR_ARGUMENT,
+                  "float-float recurrence supports alpha = +-2^k and beta in {-1, 0, 1}");
+    if (!H.val_ff) return fail(KPMGB_ERR_ARGUMENT, "operator has no float-float values");
+  }
+  for (int c0 = 0; c0 < a.NR; c0 += kMaxCols) {
+    KParams p;
+    p.rowptr = H.rowptr;
+    p.col = H.col;
+    p.val = precision == KPMGB_PREC_FF ? H.val_ff
+                                       : (H.is_real ? (const void*)H.val_real : (const void*)H.val);
+    p.NH = a.NH;
+    p.ld = a.NR;
+    p.c0 = c0;
+    p.ncols = std::min(kMaxCols, a.NR - c0);
+    p.x = a.x;
+    p.z = a.z;
+    p.y = a.y;
+    p.bra = a.bra;
+    p.alpha = a.alpha;
+    p.beta = a.beta;
+    p.mom = a.mom;
+    p.i0 = a.i0;
+    p.mu = a.mu;
+    p.mom_scale = a.mom_scale;
+    p.growth_limit = a.growth_limit;
+    p.sync = a.sync;
+    p.partials = static_cast<double2*>(a.partials);
+    const Shape sh = pick_shape(p.ncols);
+    KernelFn fn = select_kernel(sh, precision, a.dot, H.is_real != 0);
+    const int G = grid_for(fn, a.NH, sh.lpr);
+    fn<<<G, kThreads, 0, s>>>(p);
+    KPMGB_LAUNCHED();
+  }
+  return KPMGB_OK;
+}
+
+// ------------------------------------------------------------ block loading
+namespace {
+
+// Per-column squared norms of a column-major block (one block per column,
+// fixed-order reduction).
+__global__ void __launch_bounds__(256) k_colnorm2(const double2* __restrict__ psi, int64_t NH,
+                                                  double* out) {
+  const int c = blockIdx.x;
+  const double2* col = psi + (int64_t)c * NH;
+  double s = 0.0;
+  for (int64_t i = threadIdx.x; i < NH; i += 256) {
+    const double2 v = col[i];
+    s = fma(v.x, v.x, s);
+    s = fma(v.y, v.y, s);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double nrm = sqrt(red[0]);
+    int e = 0;
+    if (nrm > 0.0 && isfinite(nrm)) frexp(nrm, &e);
+    // stored column = psi * 2^-e (norm in [0.5, 1)); moments carry 2^e
+    out[c] = ldexp(1.0, e);
+  }
+}
+
+// Column-major NH x NR -> row-major, FP64 (scale ignored) or float-float with
+// the column scale 1/col_scale applied (an exact power of two).
+template <bool FF>
+__global__ void __launch_bounds__(256) k_transpose_in(const double2* __restrict__ psi, void* out,
+                                                      int64_t NH, int NR,
+                                                      const double* __restrict__ col_scale) {
+  __shared__ double2 tile[32][33];
+  const int64_t r0 = (int64_t)blockIdx.x * 32;
+  const int c0 = blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8
+  for (int k = ty; k < 32; k += 8) {
+    const int c = c0 + k;
+    const int64_t r = r0 + tx;
+    double2 v = make_double2(0.0, 0.0);
+    if (c < NR && r < NH) v = psi[(int64_t)c * NH + r];
+    tile[k][tx] = v;
+  }
+  __syncthreads();
+  for (int k = ty; k < 32; k += 8) {
+    const int64_t r = r0 + k;
+    const int c = c0 + tx;
+    if (c < NR && r < NH) {
+      const double2 v = tile[tx][k];
+      if constexpr (FF) {
+        const double f = 1.0 / col_scale[c];
+        const float2 re = ff::split_double(v.x * f);
+        const float2 im = ff::split_double(v.y * f);
+        static_cast<float4*>(out)[r * NR + c] = make_float4(re.x, re.y, im.x, im.y);
+      } else {
+        static_cast<double2*>(out)[r * NR + c] = v;
+      }
+    }
+  }
+}
+
+// All columns take the largest factor; the block factor is also stored at s[n].
+__global__ void k_uniform_scale(double* s, int n) {
+  double m = s[0];
+  for (int i = 1; i < n; ++i) m = fmax(m, s[i]);
+  for (int i = 0; i < n; ++i) s[i] = m;
+  s[n] = m;
+}
+
+__global__ void k_scale_product(const double* a, const double* b, double* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] * b[i];
+}
+
+__global__ void k_copy2(const double2* src, double2* dst, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
+}  // namespace
+
+int launch_load_block(const void* psi, void* slot, int64_t NH, int NR, int precision,
+                      double* col_scale, bool uniform, cudaStream_t s) {
+  const bool ff = precision == KPMGB_PREC_FF;
+  if (ff) {
+    k_colnorm2<<<NR, 256, 0, s>>>(static_cast<const double2*>(psi), NH, col_scale);
+    KPMGB_LAUNCHED();
+    if (uniform) {
+      k_uniform_scale<<<1, 1, 0, s>>>(col_scale, NR);
+      KPMGB_LAUNCHED();
+    }
+  }
+  dim3 grid((unsigned)((NH + 31) / 32), (unsigned)((NR + 31) / 32));
+  if (ff)
+    k_transpose_in<true><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
+                                              col_scale);
+  else
+    k_transpose_in<false><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
+                                               nullptr);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+int launch_scale_product(const double* sa, const double* sb, double* out, int NR,
+                         cudaStream_t s) {
+  k_scale_product<<<(NR + 255) / 256, 256, 0, s>>>(sa, sb, out, NR);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+int launch_copy_moments(const double2* src, double2* dst, int64_t count, cudaStream_t s) {
+  const int blocks = (int)std::min<int64_t>((count + 255) / 256, 1024);
+  k_copy2<<<std::max(blocks, 1), 256, 0, s>>>(src, dst, count);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+}  // namespace kpmgb

@@ -1,0 +1,487 @@
+// Kernel templates of the Chebyshev recurrence step (see kpmgb_recurrence.cu
+// for the overview).  Instantiated per precision in kpmgb_step_f64.cu and
+// kpmgb_step_ff.cu so that the two families compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "kpmgb_ffmath.cuh"
+#include "kpmgb_internal.h"
+
+namespace kpmgb {
+namespace step {
+
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxCols = 128;  // columns per launch (larger NR runs in batches)
+
+struct KParams {
+  const int* rowptr;
+  const int* col;
+  const void* val;
+  int64_t NH;
+  int ld;      // row stride of the blocks (total NR)
+  int c0;      // first column handled by this launch
+  int ncols;   // columns handled by this launch
+  const void* x;
+  const void* z;
+  void* y;
+  const void* bra;
+  double alpha, beta;
+  int mom;
+  int64_t i0;
+  double2* mu;
+  const double* mom_scale;
+  double growth_limit;
+  unsigned* sync;
+  double2* partials;
+};
+
+template <int DOT>
+struct NDots {
+  static constexpr int value = DOT == DOT_NONE ? 0 : (DOT == DOT_LR1 ? 1 : 2);
+};
+
+// ------------------------------------------------------------------ reduction
+// Sum per-lane dot accumulators over the grid and write the moments.
+template <int ND, int LPR, int CPL>
+__device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CPL],
+                                                const KParams& p) {
+  if constexpr (ND == 0) {
+    return;
+  } else {
+    __shared__ double2 red[kWarps][ND][LPR * CPL];
+    __shared__ unsigned s_ticket;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = LPR; off < 32; off <<= 1) {
+#pragma unroll
+      for (int k = 0; k < ND; ++k)
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) {
+          d[k][c].x += __shfl_xor_sync(0xffffffffu, d[k][c].x, off);
+          d[k][c].y += __shfl_xor_sync(0xffffffffu, d[k][c].y, off);
+        }
+    }
+    if (lane < LPR) {
+#pragma unroll
+      for (int k = 0; k < ND; ++k)
+#pragma unroll
+        for (int c = 0; c < CPL; ++c) red[warp][k][lane + c * LPR] = d[k][c];
+    }
+    __syncthreads();
+    const int NE = ND * p.ncols;
+    for (int e = threadIdx.x; e < NE; e += kThreads) {
+      const int k = e / p.ncols, c = e - k * p.ncols;
+      double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+      for (int w = 0; w < kWarps; ++w) {
+        s.x += red[w][k][c].x;
+        s.y += red[w][k][c].y;
+      }
+      p.partials[(size_t)blockIdx.x * NE + e] = s;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_ticket = atomicAdd(&p.sync[0], 1u);
+    __syncthreads();
+    if (s_ticket != gridDim.x - 1) return;
+    __threadfence();
+    // Last block: fixed-order sum over blocks.  Threads split the blocks into
+    // P interleaved parts, then the parts are added in order.
+    double2* tmp = &red[0][0][0];  // reuse (capacity kWarps*ND*LPR*CPL >= 256? see below)
+    const int P = max(1, min(kThreads / NE, (int)(sizeof(red) / sizeof(double2)) / NE));
+    const int e = threadIdx.x % NE;
+    const int part = threadIdx.x / NE;
+    __syncthreads();
+    if (part < P) {
+      double2 s = make_double2(0.0, 0.0);
+      for (int b = part; b < (int)gridDim.x; b += P) {
+        const double2 v = __ldcg(p.partials + (size_t)b * NE + e);
+        s.x += v.x;
+        s.y += v.y;
+      }
+      tmp[part * NE + e] = s;
+    }
+    __syncthreads();
+    for (int ee = threadIdx.x; ee < NE; ee += kThreads) {
+      double2 s = make_double2(0.0, 0.0);
+      for (int q = 0; q < P; ++q) {
+        s.x += tmp[q * NE + ee].x;
+        s.y += tmp[q * NE + ee].y;
+      }
+      const int k = ee / p.ncols, c = ee - k * p.ncols;
+      const int cc = p.c0 + c;
+      if (p.mom_scale) {
+        const double f = p.mom_scale[cc];
+        s.x *= f;
+        s.y *= f;
+      }
+      double2 out = s;
+      if (p.mom == MOM_DOUBLING) {
+        const double2 base = p.mu[(size_t)k * p.ld + cc];
+        out.x = 2.0 * s.x - base.x;
+        out.y = 2.0 * s.y - base.y;
+        if (k == 0 && p.growth_limit > 0.0 && !(s.x <= p.growth_limit * base.x))
+          atomicOr(&p.sync[1], (unsigned)STATUS_GROWTH);
+      }
+      if (p.mom != MOM_NONE) p.mu[(size_t)(p.i0 + k) * p.ld + cc] = out;
+      if (!isfinite(out.x) || !isfinite(out.y)) atomicOr(&p.sync[1], (unsigned)STATUS_NONFINITE);
+    }
+    if (threadIdx.x == 0) p.sync[0] = 0u;
+  }
+}
+
+// ------------------------------------------------------------------ FP64 path
+template <bool REALH>
+struct F64Val;
+template <>
+struct F64Val<true> {
+  using T = double;
+};
+template <>
+struct F64Val<false> {
+  using T = double2;
+};
+
+__device__ __forceinline__ void cmac(double2& acc, double h, double2 v) {
+  acc.x = fma(h, v.x, acc.x);
+  acc.y = fma(h, v.y, acc.y);
+}
+__device__ __forceinline__ void cmac(double2& acc, double2 h, double2 v) {
+  acc.x = fma(h.x, v.x, acc.x);
+  acc.x = fma(-h.y, v.y, acc.x);
+  acc.y = fma(h.x, v.y, acc.y);
+  acc.y = fma(h.y, v.x, acc.y);
+}
+// acc += conj(a) * b
+__device__ __forceinline__ void cdot(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+}
+
+template <int LPR, int CPL, bool REALH, int DOT>
+__global__ void __launch_bounds__(kThreads) k_step_f64(KParams p) {
+  constexpr int ND = NDots<DOT>::value;
+  constexpr int GROUPS = kThreads / LPR;
+  using HV = typename F64Val<REALH>::T;
+  const int g = threadIdx.x / LPR;
+  const int lg = threadIdx.x - g * LPR;
+  const double2* __restrict__ x = static_cast<const double2*>(p.x);
+  const double2* z = static_cast<const double2*>(p.z);
+  double2* y = static_cast<double2*>(p.y);
+  const double2* __restrict__ bra = static_cast<const double2*>(p.bra);
+  const HV* __restrict__ val = static_cast<const HV*>(p.val);
+  double2 d[ND > 0 ? ND : 1][CPL];
+#pragma unroll
+  for (int k = 0; k < (ND > 0 ? ND : 1); ++k)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) d[k][c] = make_double2(0.0, 0.0);
+
+  const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t r = t * GROUPS + g;
+    if (r >= p.NH) continue;
+    const int k0 = __ldg(p.rowptr + r), k1 = __ldg(p.rowptr + r + 1);
+    double2 acc[CPL];
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) acc[c] = make_double2(0.0, 0.0);
+#pragma unroll 4
+    for (int k = k0; k < k1; ++k) {
+      const int j = __ldg(p.col + k);
+      const HV h = __ldg(val + k);
+      const double2* xr = x + (int64_t)j * p.ld + p.c0;
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const int cc = lg + c * LPR;
+        if (cc < p.ncols) cmac(acc[c], h, __ldg(xr + cc));
+      }
+    }
+    const int64_t base = r * p.ld + p.c0;
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int cc = lg + c * LPR;
+      if (cc >= p.ncols) continue;
+      double2 yv = make_double2(p.alpha * acc[c].x, p.alpha * acc[c].y);
+      if (p.beta != 0.0) {
+        const double2 zv = z[base + cc];
+        yv.x = fma(p.beta, zv.x, yv.x);
+        yv.y = fma(p.beta, zv.y, yv.y);
+      }
+      y[base + cc] = yv;
+      if constexpr (DOT == DOT_DOUBLING) {
+        const double2 xv = __ldg(x + base + cc);
+        d[0][c].x = fma(xv.x, xv.x, d[0][c].x);
+        d[0][c].x = fma(xv.y, xv.y, d[0][c].x);
+        cdot(d[1][c], xv, yv);
+      } else if constexpr (DOT == DOT_LR2) {
+        const double2 bv = __ldg(bra + base + cc);
+        cdot(d[0][c], bv, __ldg(x + base + cc));
+        cdot(d[1][c], bv, yv);
+      } else if constexpr (DOT == DOT_LR1) {
+        cdot(d[0][c], __ldg(bra + base + cc), yv);
+      }
+    }
+  }
+  reduce_finalize<ND, LPR, CPL>(d, p);
+}
+
+// ------------------------------------------------------------ float-float path
+template <bool REALH>
+struct FFVal;
+template <>
+struct FFVal<true> {
+  using T = float2;  // (hi, lo)
+};
+template <>
+struct FFVal<false> {
+  using T = float4;  // (re.hi, re.lo, im.hi, im.lo)
+};
+
+__device__ __forceinline__ float habs(float2 h) { return fabsf(h.x); }
+__device__ __forceinline__ float habs(float4 h) { return fabsf(h.x) + fabsf(h.z); }
+__device__ __forceinline__ void hzero(float2& h) { h = make_float2(0.f, 0.f); }
+__device__ __forceinline__ void hzero(float4& h) { h = make_float4(0.f, 0.f, 0.f, 0.f); }
+
+__device__ __forceinline__ void ffmac(float& Ar, float& Cr, float& Ai, float& Ci, float2 h,
+                                      float4 v) {
+  ff::amac(Ar, Cr, h.x, h.y, v.x, v.y);
+  ff::amac(Ai, Ci, h.x, h.y, v.z, v.w);
+}
+__device__ __forceinline__ void ffmac(float& Ar, float& Cr, float& Ai, float& Ci, float4 h,
+                                      float4 v) {
+  ff::amac(Ar, Cr, h.x, h.y, v.x, v.y);
+  ff::amac(Ar, Cr, -h.z, -h.w, v.z, v.w);
+  ff::amac(Ai, Ci, h.x, h.y, v.z, v.w);
+  ff::amac(Ai, Ci, h.z, h.w, v.x, v.y);
+}
+
+// y = alpha * (S + C) + beta * z for one real component, normalised.
+__device__ __forceinline__ float2 ff_epilogue(float S, float C, float alpha, int beta_mode,
+                                              float zh, float zl) {
+  const float u = __fmul_rn(alpha, S);  // alpha is a power of two: exact
+  const float c = __fmul_rn(alpha, C);
+  float h, l;
+  if (beta_mode == 0) {
+    ff::renorm(u, c, h, l);
+  } else {
+    const float zs = beta_mode > 0 ? zh : -zh;
+    const float zt = beta_mode > 0 ? zl : -zl;
+    float s, e;
+    ff::two_sum(u, zs, s, e);
+    ff::renorm(s, __fadd_rn(e, __fadd_rn(c, zt)), h, l);
+  }
+  return make_float2(h, l);
+}
+
+// conj(a) * b accumulated into compensated float accumulators (S, C) for the
+// real (index 0) and imaginary (index 1) parts.
+__device__ __forceinline__ void ffdot(float (&S)[2], float (&C)[2], float4 a, float4 b) {
+  ff::dacc(S[0], C[0], a.x, a.y, b.x, b.y);
+  ff::dacc(S[0], C[0], a.z, a.w, b.z, b.w);
+  ff::dacc(S[1], C[1], a.x, a.y, b.z, b.w);
+  ff::dacc(S[1], C[1], -a.z, -a.w, b.x, b.y);
+}
+__device__ __forceinline__ void ffnorm2(float (&S)[2], float (&C)[2], float4 a) {
+  ff::dacc(S[0], C[0], a.x, a.y, a.x, a.y);
+  ff::dacc(S[0], C[0], a.z, a.w, a.z, a.w);
+}
+
+constexpr int kFlushRows = 16;  // per-lane float accumulators fold into FP64 this often
+
+template <int LPR, int CPL, bool REALH, int DOT, int CH>
+__global__ void __launch_bounds__(kThreads) k_step_ff(KParams p) {
+  constexpr int ND = NDots<DOT>::value;
+  constexpr int NDA = ND > 0 ? ND : 1;
+  constexpr int GROUPS = kThreads / LPR;
+  using HV = typename FFVal<REALH>::T;
+  const int g = threadIdx.x / LPR;
+  const int lg = threadIdx.x - g * LPR;
+  const float4* __restrict__ x = static_cast<const float4*>(p.x);
+  const float4* z = static_cast<const float4*>(p.z);
+  float4* y = static_cast<float4*>(p.y);
+  const float4* __restrict__ bra = static_cast<const float4*>(p.bra);
+  const HV* __restrict__ val = static_cast<const HV*>(p.val);
+  const float alpha = (float)p.alpha;
+  const int beta_mode = p.beta == 0.0 ? 0 : (p.beta > 0.0 ? 1 : -1);
+
+  double2 d[NDA][CPL];
+  float dS[NDA][CPL][2], dC[NDA][CPL][2];
+#pragma unroll
+  for (int k = 0; k < NDA; ++k)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      d[k][c] = make_double2(0.0, 0.0);
+      dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
+    }
+  int rows_since_flush = 0;
+
+  const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t r = t * GROUPS + g;
+    if (r >= p.NH) continue;
+    const int k0 = __ldg(p.rowptr + r), k1 = __ldg(p.rowptr + r + 1);
+    float Sr[CPL], Cr[CPL], Si[CPL], Ci[CPL];
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) Sr[c] = Cr[c] = Si[c] = Ci[c] = 0.f;
+    for (int kc = k0; kc < k1; kc += CH) {
+      const int cnt = min(CH, k1 - kc);
+      int jj[CH];
+      HV hv[CH];
+      float R = 0.f;
+#pragma unroll
+      for (int u = 0; u < CH; ++u) {
+        if (u < cnt) {
+          jj[u] = __ldg(p.col + kc + u);
+          hv[u] = __ldg(val + kc + u);
+        } else {
+          jj[u] = 0;
+          hzero(hv[u]);
+        }
+        R = __fadd_rn(R, habs(hv[u]));
+      }
+      float4 xv[CPL][CH];
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        const int cc = lg + c * LPR;
+#pragma unroll
+        for (int u = 0; u < CH; ++u) {
+          if (u < cnt && cc < p.ncols)
+            xv[c][u] = __ldg(x + (int64_t)jj[u] * p.ld + p.c0 + cc);
+          else
+            xv[c][u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        float M = 0.f;
+#pragma unroll
+        for (int u = 0; u < CH; ++u) M = fmaxf(M, fmaxf(fabsf(xv[c][u].x), fabsf(xv[c][u].z)));
+        // |partial sums| <= R*M (1 + tiny); anchor at 1.5 * 2^E with 2^E = 4P,
+        // P <= bound < 2P, so every partial sum stays inside the binade.
+        const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+        const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+        float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+        for (int u = 0; u < CH; ++u)
+          if (u < cnt) ffmac(Ar, cr, Ai, ci, hv[u], xv[c][u]);
+        const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+        if (kc == k0) {
+          Sr[c] = sr;
+          Cr[c] = cr;
+          Si[c] = si;
+          Ci[c] = ci;
+        } else {
+          float s, e;
+          ff::two_sum(Sr[c], sr, s, e);
+          Sr[c] = s;
+          Cr[c] = __fadd_rn(Cr[c], __fadd_rn(cr, e));
+          ff::two_sum(Si[c], si, s, e);
+          Si[c] = s;
+          Ci[c] = __fadd_rn(Ci[c], __fadd_rn(ci, e));
+        }
+      }
+    }
+    const int64_t base = r * p.ld + p.c0;
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int cc = lg + c * LPR;
+      if (cc >= p.ncols) continue;
+      float4 zv = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (beta_mode != 0) zv = z[base + cc];
+      const float2 yr = ff_epilogue(Sr[c], Cr[c], alpha, beta_mode, zv.x, zv.y);
+      const float2 yi = ff_epilogue(Si[c], Ci[c], alpha, beta_mode, zv.z, zv.w);
+      const float4 yv = make_float4(yr.x, yr.y, yi.x, yi.y);
+      y[base + cc] = yv;
+      if constexpr (DOT == DOT_DOUBLING) {
+        const float4 xr = __ldg(x + base + cc);
+        ffnorm2(dS[0][c], dC[0][c], xr);
+        ffdot(dS[1][c], dC[1][c], xr, yv);
+      } else if constexpr (DOT == DOT_LR2) {
+        const float4 bv = __ldg(bra + base + cc);
+        ffdot(dS[0][c], dC[0][c], bv, __ldg(x + base + cc));
+        ffdot(dS[1][c], dC[1][c], bv, yv);
+      } else if constexpr (DOT == DOT_LR1) {
+        ffdot(dS[0][c], dC[0][c], __ldg(bra + base + cc), yv);
+      }
+    }
+    if constexpr (ND > 0) {
+      if (++rows_since_flush == kFlushRows) {
+        rows_since_flush = 0;
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+#pragma unroll
+          for (int c = 0; c < CPL; ++c) {
+            d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
+            d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
+            dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
+          }
+      }
+    }
+  }
+  if constexpr (ND > 0) {
+#pragma unroll
+    for (int k = 0; k < ND; ++k)
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
+        d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
+      }
+  }
+  reduce_finalize<ND, LPR, CPL>(d, p);
+}
+
+struct Shape {
+  int lpr, cpl;
+};
+
+using KernelFn = void (*)(KParams);
+
+template <int LPR, int CPL, bool REALH, int DOT, int PREC>
+KernelFn kernel_for_prec() {
+  if constexpr (PREC == KPMGB_PREC_FF) {
+    constexpr int CH = CPL >= 3 ? 4 : 8;
+    return k_step_ff<LPR, CPL, REALH, DOT, CH>;
+  } else {
+    return k_step_f64<LPR, CPL, REALH, DOT>;
+  }
+}
+
+template <int LPR, int CPL, bool REALH, int PREC>
+KernelFn kernel_dot(int dot) {
+  switch (dot) {
+    case DOT_DOUBLING: return kernel_for_prec<LPR, CPL, REALH, DOT_DOUBLING, PREC>();
+    case DOT_LR2: return kernel_for_prec<LPR, CPL, REALH, DOT_LR2, PREC>();
+    case DOT_LR1: return kernel_for_prec<LPR, CPL, REALH, DOT_LR1, PREC>();
+    default: return kernel_for_prec<LPR, CPL, REALH, DOT_NONE, PREC>();
+  }
+}
+
+template <int LPR, int CPL, int PREC>
+KernelFn kernel_real(int dot, bool real) {
+  return real ? kernel_dot<LPR, CPL, true, PREC>(dot) : kernel_dot<LPR, CPL, false, PREC>(dot);
+}
+
+template <int PREC>
+KernelFn select_kernel_impl(Shape s, int dot, bool real) {
+  switch (s.lpr * 10 + s.cpl) {
+    case 11: return kernel_real<1, 1, PREC>(dot, real);
+    case 21: return kernel_real<2, 1, PREC>(dot, real);
+    case 41: return kernel_real<4, 1, PREC>(dot, real);
+    case 81: return kernel_real<8, 1, PREC>(dot, real);
+    case 43: return kernel_real<4, 3, PREC>(dot, real);
+    case 161: return kernel_real<16, 1, PREC>(dot, real);
+    case 321: return kernel_real<32, 1, PREC>(dot, real);
+    case 322: return kernel_real<32, 2, PREC>(dot, real);
+    default: return kernel_real<32, 4, PREC>(dot, real);
+  }
+}
+
+KernelFn select_kernel_f64(Shape s, int dot, bool real);
+KernelFn select_kernel_ff(Shape s, int dot, bool real);
+
+}  // namespace step
+}  // namespace kpmgb

@@ -1,0 +1,22 @@
+"""GB300 Chebyshev-moment engine: a drop-in for KPM.jl's kpm_1d / kpm_2d path.
+
+Host-side mirror of the reference interface over the C ABI of libkpmgb
+(include/kpmgb.h).  All moment arithmetic runs in hand-written sm_103a CUDA;
+there is no CPU fallback.
+"""
+from ._native import (KPMArgumentError, KPMDeviceError, KPMLibraryError, KPMNumericalError,
+                      kernel_launch_count, version)
+from .frontend import (ConductivityMoments, DosMoments, RescaledHamiltonian, cond_moments,
+                       dos_moments, normalizeH, on_device, random_phase_vectors, rescale)
+from .moment import (kpm_1d, kpm_1d_bang, kpm_1d_device, kpm_2d, kpm_2d_bang, kpm_2d_blocking,
+                     kpm_2d_device, normalize_by_col, sync)
+from .operator import GB300Operator, as_operator
+
+__all__ = [
+    "KPMArgumentError", "KPMDeviceError", "KPMLibraryError", "KPMNumericalError",
+    "kernel_launch_count", "version", "ConductivityMoments", "DosMoments",
+    "RescaledHamiltonian", "cond_moments", "dos_moments", "normalizeH", "on_device",
+    "random_phase_vectors", "rescale", "kpm_1d", "kpm_1d_bang", "kpm_1d_device", "kpm_2d",
+    "kpm_2d_bang", "kpm_2d_blocking", "kpm_2d_device", "normalize_by_col", "sync",
+    "GB300Operator", "as_operator",
+]

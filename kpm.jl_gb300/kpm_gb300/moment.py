@@ -1,0 +1,324 @@
+"""Moment engine entry points mirroring KPM.jl's ``kpm_1d`` / ``kpm_2d``.
+
+Same names, argument meaning and error behaviour as ``src/moment.jl``:
+
+* ``kpm_1d(H, NC, NR, NH=None, *, psi_in, psi_in_l, psi_in_r, force_norm,
+  avg_output, NR_parallel)``  (``src/moment.jl:339-418``)
+* ``kpm_1d_bang(H, NC, NR, NH, mu_all, psi_in)`` / ``(..., psi_in_l, psi_in_r)``
+  (the reference's ``kpm_1d!``, ``src/moment.jl:420-556``)
+* ``kpm_2d(H, Ja, Jb, NC, NR, NH, *, psi_in | psi_in_l+psi_in_r, arr_size,
+  right_block, workspace_bytes, moment_parity, mn_sym)``
+  (``src/moment.jl:812-1103``)
+* ``kpm_2d_blocking`` (``src/moment.jl:759-810``)
+
+All arithmetic runs in libkpmgb on the GPU.  Probe blocks are NumPy arrays of
+shape (NH, NR) (column i = probe i, as in Julia) or torch CUDA tensors for the
+``*_device`` forms.  ``precision="fp64"`` is native double precision;
+``precision="ff"`` is the emulated-double (float-float) recurrence.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _native
+from ._native import KPMArgumentError
+from .operator import GB300Operator, as_operator
+
+_PREC = {"fp64": _native.PREC_FP64, "ff": _native.PREC_FF}
+_CONTRACT = {"fp64": _native.CONTRACT_FP64, "split": _native.CONTRACT_SPLIT}
+
+
+def _prec(precision) -> int:
+    try:
+        return _PREC[precision]
+    except KeyError:
+        raise KPMArgumentError(f"precision must be one of {sorted(_PREC)} (got {precision!r})")
+
+
+def normalize_by_col(psi: np.ndarray, centering: bool = False) -> None:
+    """In-place column normalisation (``src/utils/vectors.jl:14-19``)."""
+    for i in range(psi.shape[1]):
+        col = psi[:, i]
+        if centering:
+            col -= col.mean()
+        col /= np.linalg.norm(col)
+
+
+def _colmajor(psi, NH, NR, name):
+    a = np.asarray(psi)
+    if a.shape != (NH, NR):
+        raise KPMArgumentError(
+            f"Invalid `{name}` with size {a.shape}. Expecting ({NH}, {NR})")
+    return np.asfortranarray(a, dtype=np.complex128)
+
+
+def _opts1d(precision, stability_check):
+    return _native.Kpm1dOptions(_prec(precision), 1 if stability_check else 0, 0, 0)
+
+
+def kpm_1d_bang(H, NC: int, NR: int, NH: int, mu_all: np.ndarray, psi_in=None, psi_in_r=None,
+                *, precision: str = "fp64", stability_check: bool = False) -> None:
+    """``kpm_1d!``: fill ``mu_all`` (NR, NC) in place.
+
+    ``kpm_1d_bang(H, NC, NR, NH, mu_all, psi_in)`` is the doubling path
+    (NC even); ``kpm_1d_bang(H, NC, NR, NH, mu_all, psi_in_l, psi_in_r)`` the
+    bra/ket path.
+    """
+    op = as_operator(H)
+    lib = _native.load()
+    if mu_all.shape != (NR, NC):
+        raise KPMArgumentError(f"mu_all has size {mu_all.shape}; expected ({NR}, {NC})")
+    out = np.empty((NR, NC), dtype=np.complex128, order="F")
+    opts = _opts1d(precision, stability_check)
+    if psi_in_r is None:
+        if NC % 2 != 0:
+            raise KPMArgumentError("Invalid NC: NC should be even.")
+        psi = _colmajor(psi_in, NH, NR, "psi_in")
+        rc = lib.kpmgb_kpm1d(op.handle, NC, NR, NH, psi.ctypes.data, out.ctypes.data, C.byref(opts))
+    else:
+        if NC < 2:
+            raise KPMArgumentError("Invalid NC: NC should be at least 2.")
+        pl = _colmajor(psi_in, NH, NR, "psi_in_l")
+        pr = _colmajor(psi_in_r, NH, NR, "psi_in_r")
+        rc = lib.kpmgb_kpm1d_lr(op.handle, NC, NR, NH, pl.ctypes.data, pr.ctypes.data,
+                                out.ctypes.data, C.byref(opts))
+    _native.check(rc)
+    mu_all[...] = out
+
+
+def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=None,
+           psi_in_r=None, force_norm: bool = False, verbose: int = 0, avg_output: bool = True,
+           NR_parallel: bool = True, rng=None, precision: str = "fp64",
+           stability_check: bool = False):
+    """Stochastic-trace Chebyshev moments (``src/moment.jl:339-418``).
+
+    Returns the real probe average (length NC) for equal bra/ket, the complex
+    average for ``psi_in_l``/``psi_in_r``, or the (NR, NC) matrix with
+    ``avg_output=False``.  Without probes, random-phase probes are drawn from
+    ``rng`` (a NumPy Generator; the reference draws from Xoshiro).
+    """
+    NH = H.shape[0] if NH is None else int(NH)
+    NC, NR = int(NC), int(NR)
+    mu_all = np.zeros((NR, NC), dtype=np.complex128)
+    lr = False
+    if psi_in is None:
+        if psi_in_l is not None or psi_in_r is not None:
+            if psi_in_l is None or psi_in_r is None:
+                raise KPMArgumentError("must set both `psi_in_l` and `psi_in_r` or neither.")
+            lr = True
+            if force_norm:
+                normalize_by_col(psi_in_l)
+                normalize_by_col(psi_in_r)
+        else:
+            from .frontend import random_phase_vectors
+            rng = np.random.default_rng() if rng is None else rng
+            psi_in = random_phase_vectors(rng, NH, NR)
+    else:
+        if psi_in_l is not None or psi_in_r is not None:
+            raise KPMArgumentError(
+                "must either set `psi_in` or set `psi_in_l` and `psi_in_r`, but not both.")
+        if force_norm:
+            normalize_by_col(psi_in)
+    op = as_operator(H)
+    if NR_parallel:
+        if lr:
+            kpm_1d_bang(op, NC, NR, NH, mu_all, psi_in_l, psi_in_r, precision=precision,
+                        stability_check=stability_check)
+        else:
+            kpm_1d_bang(op, NC, NR, NH, mu_all, psi_in, precision=precision,
+                        stability_check=stability_check)
+    else:
+        for i in range(NR):
+            row = np.zeros((1, NC), dtype=np.complex128)
+            if lr:
+                kpm_1d_bang(op, NC, 1, NH, row, np.asarray(psi_in_l)[:, i:i + 1],
+                            np.asarray(psi_in_r)[:, i:i + 1], precision=precision)
+            else:
+                kpm_1d_bang(op, NC, 1, NH, row, np.asarray(psi_in)[:, i:i + 1],
+                            precision=precision)
+            mu_all[i] = row[0]
+    if avg_output:
+        avg = mu_all.sum(axis=0) / NR
+        return avg if lr else avg.real
+    return mu_all
+
+
+def kpm_2d_blocking(NH: int, NR: int, NC: int, *, workspace_bytes="auto", arr_size="auto",
+                    right_block="auto"):
+    """Block sizes of the reference rule (``src/moment.jl:759-810``).
+
+    Returns ``dict(arr_size=K_left, right_block=K_right, bytes=footprint)``.
+    The automatic budget is ``KPM_WORKSPACE_BYTES`` or half the free device
+    memory.
+    """
+    if NH <= 0:
+        raise KPMArgumentError(f"NH must be positive (got {NH})")
+    if NR <= 0:
+        raise KPMArgumentError(f"NR must be positive (got {NR})")
+    if NC < 2:
+        raise KPMArgumentError(f"NC must be at least 2 (got {NC})")
+    block = NH * NR * 16
+    if workspace_bytes == "auto":
+        env = os.environ.get("KPM_WORKSPACE_BYTES", "")
+        if env:
+            budget = int(env)
+        else:
+            import torch
+            free, _ = torch.cuda.mem_get_info()
+            budget = free // 2
+    elif isinstance(workspace_bytes, (int, np.integer)):
+        budget = int(workspace_bytes)
+    else:
+        raise KPMArgumentError("workspace_bytes must be :auto or an integer")
+    if budget < 0:
+        raise KPMArgumentError("workspace_bytes must be nonnegative")
+    if right_block == "auto":
+        K_right = min(NC, 16)
+    elif isinstance(right_block, (int, np.integer)) and right_block >= 1:
+        K_right = int(right_block)
+    else:
+        raise KPMArgumentError("right_block must be :auto or a positive integer")
+    base = (K_right + 7) * block
+    per_left = block + K_right * 16
+    if arr_size == "auto":
+        kmax = (budget - base) // per_left
+        if kmax < 2:
+            raise KPMArgumentError(
+                f"workspace_bytes={budget} cannot fit the minimum kpm_2d workspace "
+                f"({base + 2 * per_left} bytes at right_block={K_right})")
+        K_left = min(kmax, NC)
+    elif isinstance(arr_size, (int, np.integer)) and arr_size >= 2:
+        K_left = int(arr_size)
+    else:
+        raise KPMArgumentError("arr_size must be :auto or an integer at least 2")
+    return dict(arr_size=K_left, right_block=K_right, bytes=base + K_left * per_left)
+
+
+def _opts2d(arr_size, right_block, workspace_bytes, moment_parity, mn_sym, precision,
+            contraction):
+    if moment_parity not in _native.PARITY:
+        raise KPMArgumentError(f"moment_parity={moment_parity} not understood.")
+    if arr_size == "auto":
+        kl = 0
+    elif isinstance(arr_size, (int, np.integer)) and arr_size >= 2:
+        kl = int(arr_size)
+    else:
+        raise KPMArgumentError("arr_size must be :auto or an integer at least 2")
+    if right_block == "auto":
+        kr = 0
+    elif isinstance(right_block, (int, np.integer)) and right_block >= 1:
+        kr = int(right_block)
+    else:
+        raise KPMArgumentError("right_block must be :auto or a positive integer")
+    if workspace_bytes == "auto":
+        env = os.environ.get("KPM_WORKSPACE_BYTES", "")
+        wb = int(env) if env else -1
+    elif isinstance(workspace_bytes, (int, np.integer)) and workspace_bytes >= 0:
+        wb = int(workspace_bytes)
+    else:
+        raise KPMArgumentError("workspace_bytes must be :auto or a nonnegative integer")
+    if contraction not in _CONTRACT:
+        raise KPMArgumentError(f"contraction must be one of {sorted(_CONTRACT)}")
+    return _native.Kpm2dOptions(kl, kr, wb, _native.PARITY[moment_parity], 1 if mn_sym else 0,
+                                _prec(precision), _CONTRACT[contraction])
+
+
+def kpm_2d_bang(H, Ja, Jb, NC: int, NR: int, NH: int, mu: np.ndarray, psi_in_l, psi_in_r=None,
+                *, arr_size="auto", right_block="auto", workspace_bytes="auto",
+                moment_parity="NONE", mn_sym=False, precision="fp64", contraction="fp64",
+                verbose=0) -> None:
+    """``kpm_2d!``: overwrite ``mu`` (NC, NC) (``src/moment.jl:887-1088``)."""
+    if psi_in_r is None:
+        psi_in_r = psi_in_l
+    opts = _opts2d(arr_size, right_block, workspace_bytes, moment_parity, mn_sym, precision,
+                   contraction)
+    pl = _colmajor(psi_in_l, NH, NR, "psi_in_l")
+    pr = _colmajor(psi_in_r, NH, NR, "psi_in_r")
+    h, a, b = as_operator(H), as_operator(Ja), as_operator(Jb)
+    out = np.empty((NC, NC), dtype=np.complex128, order="F")
+    lib = _native.load()
+    rc = lib.kpmgb_kpm2d(h.handle, a.handle, b.handle, NC, NR, NH, pl.ctypes.data,
+                         pr.ctypes.data, out.ctypes.data, C.byref(opts))
+    _native.check(rc)
+    mu[...] = out
+
+
+def kpm_2d(H, Ja, Jb, NC: int, NR: int, NH: int, *, psi_in=None, psi_in_l=None, psi_in_r=None,
+           arr_size="auto", right_block="auto", workspace_bytes="auto", moment_parity="NONE",
+           mn_sym=False, verbose=0, rng=None, precision="fp64", contraction="fp64"):
+    """Two-dimensional moments mu[n, m] (NC, NC) (``src/moment.jl:812-885``)."""
+    NC, NR, NH = int(NC), int(NR), int(NH)
+    mu = np.zeros((NC, NC), dtype=np.complex128)
+    kw = dict(arr_size=arr_size, right_block=right_block, workspace_bytes=workspace_bytes,
+              moment_parity=moment_parity, mn_sym=mn_sym, precision=precision,
+              contraction=contraction)
+    if psi_in is None and psi_in_l is None and psi_in_r is None:
+        from .frontend import random_phase_vectors
+        rng = np.random.default_rng() if rng is None else rng
+        psi = random_phase_vectors(rng, NH, NR)
+        kpm_2d_bang(H, Ja, Jb, NC, NR, NH, mu, psi, psi, **kw)
+    elif psi_in is not None and psi_in_l is None and psi_in_r is None:
+        kpm_2d_bang(H, Ja, Jb, NC, NR, NH, mu, psi_in, psi_in, **kw)
+    elif psi_in is None and psi_in_l is not None and psi_in_r is not None:
+        kpm_2d_bang(H, Ja, Jb, NC, NR, NH, mu, psi_in_l, psi_in_r, **kw)
+    else:
+        raise KPMArgumentError("unimplemented")
+    return mu
+
+
+# ------------------------------------------------------------ device forms
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return C.c_void_p(getattr(stream, "cuda_stream", stream))
+
+
+def kpm_1d_device(op: GB300Operator, NC: int, psi_t, mu_t, *, psi_l_t=None,
+                  precision="fp64", stability_check=False, stream=None) -> None:
+    """Enqueue kpm_1d on torch CUDA tensors without host copies.
+
+    ``psi_t``: complex128 tensor of shape (NR, NH) (row-contiguous, i.e. the
+    column-major NH x NR block); ``mu_t``: complex128 (NC, NR).  Runs on
+    ``stream`` (default: torch's current stream) and returns immediately.
+    """
+    lib = _native.load()
+    NR, NH = psi_t.shape
+    for t, name in ((psi_t, "psi"), (mu_t, "mu")):
+        if not t.is_contiguous():
+            raise KPMArgumentError(f"{name} tensor must be contiguous")
+    if tuple(mu_t.shape) != (NC, NR):
+        raise KPMArgumentError(f"mu tensor must have shape ({NC}, {NR})")
+    opts = _opts1d(precision, stability_check)
+    if psi_l_t is None:
+        rc = lib.kpmgb_kpm1d_device(op.handle, NC, NR, NH, C.c_void_p(psi_t.data_ptr()),
+                                    C.c_void_p(mu_t.data_ptr()), C.byref(opts), _stream_ptr(stream))
+    else:
+        rc = lib.kpmgb_kpm1d_lr_device(op.handle, NC, NR, NH, C.c_void_p(psi_l_t.data_ptr()),
+                                       C.c_void_p(psi_t.data_ptr()), C.c_void_p(mu_t.data_ptr()),
+                                       C.byref(opts), _stream_ptr(stream))
+    _native.check(rc)
+
+
+def kpm_2d_device(H: GB300Operator, Ja: GB300Operator, Jb: GB300Operator, NC: int, psi_l_t,
+                  psi_r_t, mu_t, *, arr_size="auto", right_block="auto",
+                  workspace_bytes="auto", moment_parity="NONE", mn_sym=False,
+                  precision="fp64", contraction="fp64", stream=None) -> None:
+    """Enqueue kpm_2d on torch CUDA tensors; ``mu_t`` is complex128 (NC, NC) holding
+    the column-major moment matrix (mu_t[m, n] = mu[n, m])."""
+    lib = _native.load()
+    NR, NH = psi_r_t.shape
+    opts = _opts2d(arr_size, right_block, workspace_bytes, moment_parity, mn_sym, precision,
+                   contraction)
+    rc = lib.kpmgb_kpm2d_device(H.handle, Ja.handle, Jb.handle, NC, NR, NH,
+                                C.c_void_p(psi_l_t.data_ptr()), C.c_void_p(psi_r_t.data_ptr()),
+                                C.c_void_p(mu_t.data_ptr()), C.byref(opts), _stream_ptr(stream))
+    _native.check(rc)
+
+
+def sync(op: GB300Operator, stream=None) -> None:
+    """Wait for enqueued work on ``op`` and raise deferred numerical failures."""
+    _native.check(_native.load().kpmgb_operator_sync(op.handle, _stream_ptr(stream)))

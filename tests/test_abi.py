@@ -1,0 +1,94 @@
+"""C-ABI checks that need no GPU: the library builds, loads, exports every
+symbol declared in include/kpmgb.h, and rejects bad arguments before any
+device work."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def _declared_symbols():
+    text = (ROOT / "include" / "kpmgb.h").read_text()
+    return sorted(set(re.findall(r"\b(kpmgb_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_and_binding_agree():
+    from kpm_gb300 import _native
+    assert set(_declared_symbols()) == set(_native.EXPORTED_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = C.CDLL(str(built_lib))
+    missing = [s for s in _declared_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_version_and_error_without_gpu(built_lib):
+    from kpm_gb300 import _native
+    lib = _native.load()
+    assert lib.kpmgb_version().decode().startswith("kpmgb")
+    # a null operator is rejected with an argument error, no device work
+    rc = lib.kpmgb_kpm1d(None, 4, 1, 4, None, None, None)
+    assert rc == _native.ERR_ARGUMENT
+    assert lib.kpmgb_last_error().decode()
+
+
+def test_csc_validation_before_upload(built_lib):
+    from kpm_gb300 import _native
+    lib = _native.load()
+    h = C.c_void_p()
+    colptr = np.array([0, 1, 3], dtype=np.int64)   # claims 3 entries
+    rowval = np.array([0, 1], dtype=np.int64)
+    nz = np.ones(2, dtype=np.complex128)
+    rc = lib.kpmgb_operator_create(2, 2, colptr.ctypes.data, rowval.ctypes.data,
+                                   nz.ctypes.data, 0, C.byref(h))
+    assert rc == _native.ERR_ARGUMENT
+    colptr = np.array([0, 1, 2], dtype=np.int64)
+    rowval = np.array([0, 5], dtype=np.int64)      # row out of range
+    rc = lib.kpmgb_operator_create(2, 2, colptr.ctypes.data, rowval.ctypes.data,
+                                   nz.ctypes.data, 0, C.byref(h))
+    assert rc == _native.ERR_ARGUMENT
+    assert "range" in lib.kpmgb_last_error().decode()
+
+
+def test_python_argument_validation(built_lib):
+    """Front-end checks mirror the reference's ArgumentErrors (src/frontend.jl:225-327)."""
+    import kpm_gb300 as kg
+    H = sp.identity(8, dtype=complex, format="csc") * 0.5
+    h = kg.RescaledHamiltonian(H, 1.0, 0.0)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.dos_moments(h, NC=63)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.dos_moments(h, NC=64, rng=np.random.default_rng(1), psi_in=np.zeros((8, 2)))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.dos_moments(h, NC=64, psi_in=np.zeros((7, 2)))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.cond_moments(h, H, H, NC=32, psi_in=np.zeros((7, 2)))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(H, 8, 2, psi_in=np.zeros((8, 2)), psi_in_l=np.zeros((8, 2)))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(H, 8, 2, psi_in_l=np.zeros((8, 2)))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_2d(H, H, H, 8, 2, 8, psi_in=np.zeros((8, 2)), moment_parity="BOTH")
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_2d(H, H, H, 8, 2, 8, psi_in=np.zeros((8, 2)), arr_size=1)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.ConductivityMoments(np.zeros((3, 2), dtype=complex), 1.0, 0.0, 8, 1)
+
+
+def test_blocking_rule_matches_reference_arithmetic():
+    """src/moment.jl:759-810 as pinned by test/kpm2d_blocking_test.jl:119-152."""
+    import kpm_gb300 as kg
+    NH, NR, NC = 40, 3, 50
+    one = NH * NR * 16
+    c = kg.kpm_2d_blocking(NH, NR, NC, workspace_bytes=30 * one, right_block=4)
+    assert c == dict(arr_size=18, right_block=4, bytes=11 * one + 18 * (one + 64))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_2d_blocking(NH, NR, NC, workspace_bytes=10 * one - 1)
+    c = kg.kpm_2d_blocking(NH, NR, NC, workspace_bytes=10 * one, arr_size=27, right_block=9)
+    assert (c["arr_size"], c["right_block"]) == (27, 9)

@@ -1,0 +1,200 @@
+"""GPU parity of the kpm_1d moment engine against the oracle and the golden
+fixtures.  FP64 path: 1e-12 norm-wise relative (the reference's rtol);
+float-float path: 1e-9."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import relerr
+from helpers import load_golden, rand_herm
+import kpm_gb300 as kg
+from kpm_gb300 import models
+from oracle import kpm_oracle as ko
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "ff": 1e-9}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib(built_lib):
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    return built_lib
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_golden_anderson(prec):
+    f, mat = load_golden("anderson2d_L8")
+    H = mat("H")
+    mu = kg.kpm_1d(H, int(f["NC"]), 3, psi_in=f["psi"], avg_output=False, precision=prec)
+    assert relerr(mu, f["mu_dense"]) < TOL[prec]
+    assert relerr(mu, f["mu_ed"]) < max(TOL[prec], 1e-10)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_golden_haldane_lr(prec):
+    f, mat = load_golden("haldane_3x3")
+    mu = kg.kpm_1d(mat("H"), int(f["NC"]), 2, psi_in_l=f["psi_l"], psi_in_r=f["psi_r"],
+                   avg_output=False, precision=prec)
+    assert relerr(mu, f["mu_lr_dense"]) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_golden_ring_exact_trace(prec):
+    f, mat = load_golden("ring_N64")
+    H = mat("H")
+    N = H.shape[0]
+    mu = kg.kpm_1d(H, int(f["NC"]), N, psi_in=np.eye(N, dtype=complex), precision=prec)
+    assert relerr(mu, f["mu_exact"]) < TOL[prec]
+
+
+@pytest.mark.parametrize("NR", [1, 2, 3, 4, 5, 8, 12, 16, 24, 32, 33, 64, 100, 128, 130, 200])
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_probe_counts(NR, prec):
+    """Every lane-group shape and the >128-column batching."""
+    rng = np.random.default_rng(100 + NR)
+    H = models.square_anderson(16, W=2.0, rng=rng)
+    a, _, Hn = ko.normalizeH(H)
+    psi = ko.random_phase_vectors(rng, 256, NR)
+    ref = ko.kpm_1d_doubling(Hn, 64, psi)
+    got = kg.kpm_1d(Hn, 64, NR, psi_in=psi, avg_output=False, precision=prec)
+    assert relerr(got, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_config_2d_anderson_L64(prec):
+    """2D Anderson L=64 (NH=4096), W=2, NC=1024, NR=12, the CPU-runnable workload."""
+    rng = np.random.default_rng(42)
+    H = models.square_anderson(64, W=2.0, rng=rng)
+    a, _, Hn = ko.normalizeH(H)
+    psi = ko.random_phase_vectors(rng, 4096, 12)
+    ref = ko.kpm_1d_doubling(Hn, 1024, psi)
+    got = kg.kpm_1d(Hn, 1024, 12, psi_in=psi, avg_output=False, precision=prec)
+    assert relerr(got, ref) < TOL[prec]
+    # per-moment relative error of the probe average against the largest moment
+    err = np.max(np.abs(got.mean(0) - ref.mean(0))) / np.max(np.abs(ref.mean(0)))
+    assert err < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+@pytest.mark.parametrize("lr", [False, True])
+def test_complex_haldane(prec, lr):
+    rng = np.random.default_rng(7)
+    H, _, _, _ = models.haldane(24, 24, t2=0.1)
+    a, b, Hn = ko.normalizeH(H, center=True)
+    NH = Hn.shape[0]
+    pl = ko.random_phase_vectors(rng, NH, 16)
+    pr = ko.random_phase_vectors(rng, NH, 16)
+    if lr:
+        ref = ko.kpm_1d_lr(Hn, 257, pl, pr)  # odd NC, as test/gpu_smoke.jl:63-100
+        got = kg.kpm_1d(Hn, 257, 16, psi_in_l=pl, psi_in_r=pr, avg_output=False, precision=prec)
+    else:
+        ref = ko.kpm_1d_doubling(Hn, 256, pr)
+        got = kg.kpm_1d(Hn, 256, 16, psi_in=pr, avg_output=False, precision=prec)
+    assert relerr(got, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_ragged_empty_and_long_rows(prec):
+    """Rows with 0, 1, ... 40 nonzeros (several float-float chunks), complex values."""
+    rng = np.random.default_rng(3)
+    n = 300
+    rows, cols = [], []
+    for i in range(n):
+        k = (i * 7) % 41 if i % 10 else 0
+        c = rng.choice(n, size=k, replace=False)
+        rows += [i] * k
+        cols += list(c)
+    vals = rng.standard_normal(len(rows)) + 1j * rng.standard_normal(len(rows))
+    A = sp.coo_matrix((vals, (rows, cols)), shape=(n, n)).tocsr()
+    Hd = (A + A.conj().T).toarray() / 2
+    Hd /= 1.1 * np.linalg.norm(Hd, 2)
+    H = sp.csc_matrix(Hd)
+    psi = ko.random_phase_vectors(rng, n, 6)
+    ref = ko.kpm_1d_doubling(H, 96, psi)
+    got = kg.kpm_1d(H, 96, 6, psi_in=psi, avg_output=False, precision=prec)
+    assert relerr(got, ref) < TOL[prec]
+    ref = ko.kpm_1d_lr(H, 95, psi[:, ::-1].copy(), psi)
+    got = kg.kpm_1d(H, 95, 6, psi_in_l=psi[:, ::-1].copy(), psi_in_r=psi, avg_output=False,
+                    precision=prec)
+    assert relerr(got, ref) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_unnormalized_and_zero_columns(prec):
+    """mu scales as |c|^2 (test/dos_test.jl:80-93); a zero probe gives zero moments."""
+    rng = np.random.default_rng(13)
+    H = sp.csc_matrix(rand_herm(rng, 32, scale=2.0))
+    psi = ko.random_phase_vectors(rng, 32, 4) * np.array([1.0, 1e6, 1e-7, 0.0])
+    ref = ko.kpm_1d_doubling(H, 16, psi)
+    got = kg.kpm_1d(H, 16, 4, psi_in=psi, avg_output=False, precision=prec)
+    for i in range(3):
+        assert relerr(got[i], ref[i]) < TOL[prec]
+    assert np.all(got[3] == 0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_deterministic(prec):
+    rng = np.random.default_rng(11)
+    H = models.square_anderson(32, W=1.0, rng=rng)
+    _, _, Hn = ko.normalizeH(H)
+    op = kg.GB300Operator(Hn)
+    psi = ko.random_phase_vectors(rng, 1024, 8)
+    m1 = kg.kpm_1d(op, 128, 8, psi_in=psi, avg_output=False, precision=prec)
+    m2 = kg.kpm_1d(op, 128, 8, psi_in=psi, avg_output=False, precision=prec)
+    assert np.array_equal(m1, m2)
+
+
+def test_errors():
+    rng = np.random.default_rng(1)
+    H = sp.csc_matrix(rand_herm(rng, 16))
+    psi = ko.random_phase_vectors(rng, 16, 2)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(H, 7, 2, psi_in=psi)
+    op = kg.GB300Operator(H)
+    mu = np.zeros((2, 8), dtype=complex)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_bang(op, 8, 2, 15, mu, psi[:15])
+    # spectrum outside (-1, 1): the recurrence grows, the guard reports it
+    Hbad = sp.csc_matrix(3.0 * rand_herm(rng, 16, scale=1.0))
+    with pytest.raises(kg.KPMNumericalError):
+        kg.kpm_1d(Hbad, 64, 2, psi_in=psi, stability_check=True)
+    # without the guard the reference semantics hold (finite growth is returned)
+    mu_raw = kg.kpm_1d(Hbad, 16, 2, psi_in=psi)
+    assert np.all(np.isfinite(mu_raw))
+    # non-finite input is always reported
+    bad = psi.copy()
+    bad[0, 0] = np.nan
+    with pytest.raises(kg.KPMNumericalError):
+        kg.kpm_1d(H, 8, 2, psi_in=bad)
+
+
+def test_device_api_matches_host():
+    import torch
+    rng = np.random.default_rng(9)
+    H = models.square_anderson(32, W=2.0, rng=rng)
+    _, _, Hn = ko.normalizeH(H)
+    op = kg.GB300Operator(Hn)
+    psi = ko.random_phase_vectors(rng, 1024, 12)
+    host = kg.kpm_1d(op, 256, 12, psi_in=psi, avg_output=False)
+    psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    mu_t = torch.zeros((256, 12), dtype=torch.complex128, device="cuda")
+    kg.kpm_1d_device(op, 256, psi_t, mu_t)
+    kg.sync(op)
+    torch.cuda.synchronize()
+    assert np.array_equal(mu_t.cpu().numpy().T, host)
+
+
+def test_typed_frontend_delegates():
+    """dos_moments delegates to kpm_1d exactly (test/frontend_test.jl:40-55)."""
+    NH = 64
+    H = sp.diags([np.ones(NH - 1), np.ones(NH - 1)], [-1, 1], format="csc").astype(complex)
+    h = kg.rescale(H)
+    psi = kg.random_phase_vectors(np.random.default_rng(11), NH, 4)
+    m = kg.dos_moments(h, NC=64, psi_in=psi.copy())
+    ref = kg.kpm_1d(h.H, 64, 4, psi_in=psi.copy())
+    assert np.array_equal(m.mu, ref)
+    assert (m.a, m.b, m.NH, m.NR) == (h.a, h.b, NH, 4)
+    full = kg.dos_moments(h, NC=128, psi_in=np.eye(NH, dtype=complex))
+    assert abs(full.mu[0] - 1.0) < 1e-12
