@@ -218,7 +218,8 @@ def main():
     h, psi = workload(args, rank)
     NH, NR, NC = h.H.shape[0], args.NR, args.NC
     op = kg.GB300Operator(h.H)
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: every library kernel and both timing events go here
+    stream = torch.cuda.Stream()
     psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
     mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
 
@@ -232,19 +233,21 @@ def main():
 
     for _ in range(args.warmup):
         call(args.precision)
-    kg.sync(op)
+    kg.sync(op, stream)
     barrier()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     n0 = kg.kernel_launch_count()
     with ClockSampler(local) as clk:
         barrier()
+        w0 = time.perf_counter()
         ev0.record(stream)
         for _ in range(args.steps):
             call(args.precision)
         ev1.record(stream)
         barrier()
+        wall_ms = (time.perf_counter() - w0) * 1e3 / args.steps
     launches = kg.kernel_launch_count() - n0
-    kg.sync(op)
+    kg.sync(op, stream)
     ms = ev0.elapsed_time(ev1) / args.steps
     t = torch.tensor([ms], device="cuda")
     if world > 1:
@@ -300,7 +303,7 @@ def main():
         kg.kpm_1d_device(op, NC, psi_t, mu64, precision="fp64", stream=stream)
         e1.record(stream)
         barrier()
-        kg.sync(op)
+        kg.sync(op, stream)
         m64 = mu64.cpu().numpy().T
         avg_c, avg_p = mu_chosen.mean(0).real, m64.mean(0).real
         plain = {"ms_per_step": e0.elapsed_time(e1),
@@ -322,7 +325,7 @@ def main():
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "wall_ms_per_step": wall_ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": ("f64 emulated as float-float on the FP32 pipe" if args.precision == "ff"
                       else "f64"),

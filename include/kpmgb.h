@@ -70,9 +70,10 @@ typedef struct kpmgb_operator_s* kpmgb_operator;
 typedef struct kpmgb_kpm1d_options {
   int32_t precision;       /* KPMGB_PREC_*                                    */
   int32_t stability_check; /* 0: off (reference kpm_1d! semantics); 1: fail
-                              with KPMGB_ERR_NUMERICAL when a moment is not
-                              finite or a column norm grows beyond 1.5x its
-                              seed norm (chebyshev_iteration.jl:110-133)       */
+                              with KPMGB_ERR_NUMERICAL when a column norm
+                              grows beyond 1.5x its seed norm
+                              (chebyshev_iteration.jl:110-133).  A non-finite
+                              moment is always reported as NUMERICAL.          */
   int32_t use_graph;       /* 1: replay the recurrence as a CUDA graph        */
   int32_t reserved;
 } kpmgb_kpm1d_options;
@@ -134,7 +135,7 @@ int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
 
 /* Device-resident forms of the three calls above: psi/psi_l/psi_r and
  * mu_all/mu are device addresses with the same layouts.  Work is enqueued on
- * `stream` (a cudaStream_t; NULL = the operator's own stream) and the call
+ * `stream` (a cudaStream_t; 0 is CUDA's legacy default stream) and the call
  * returns without waiting; kpmgb_operator_sync waits and reports a deferred
  * numerical failure. */
 int kpmgb_kpm1d_device(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,

@@ -126,9 +126,9 @@ int ensure_sync(Operator* op, cudaStream_t s) {
   return KPMGB_OK;
 }
 
-cudaStream_t pick_stream(Operator* op, void* stream) {
-  return stream ? static_cast<cudaStream_t>(stream) : op->stream;
-}
+// Device entry points run on the caller's stream exactly as given (0 is the
+// legacy default stream, as everywhere in CUDA).
+cudaStream_t pick_stream(Operator*, void* stream) { return static_cast<cudaStream_t>(stream); }
 
 int check_precision(int precision) {
   if (precision != KPMGB_PREC_FP64 && precision != KPMGB_PREC_FF)

@@ -11,6 +11,19 @@
 namespace kpmgb {
 namespace step {
 
+// Tuning knobs of the float-float kernel: operator nonzeros gathered per chunk
+// (registers hold CH x CPL float4 neighbour values) and the minimum number of
+// resident blocks per SM requested from the register allocator.
+#ifndef KPMGB_FF_CHUNK_CPL1
+#define KPMGB_FF_CHUNK_CPL1 8
+#endif
+#ifndef KPMGB_FF_CHUNK_CPL2
+#define KPMGB_FF_CHUNK_CPL2 8
+#endif
+#ifndef KPMGB_FF_MIN_BLOCKS
+#define KPMGB_FF_MIN_BLOCKS 2
+#endif
+
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxCols = 128;  // columns per launch (larger NR runs in batches)
@@ -293,7 +306,7 @@ __device__ __forceinline__ void ffnorm2(float (&S)[2], float (&C)[2], float4 a) 
 constexpr int kFlushRows = 16;  // per-lane float accumulators fold into FP64 this often
 
 template <int LPR, int CPL, bool REALH, int DOT, int CH>
-__global__ void __launch_bounds__(kThreads) k_step_ff(KParams p) {
+__global__ void __launch_bounds__(kThreads, KPMGB_FF_MIN_BLOCKS) k_step_ff(KParams p) {
   constexpr int ND = NDots<DOT>::value;
   constexpr int NDA = ND > 0 ? ND : 1;
   constexpr int GROUPS = kThreads / LPR;
@@ -443,7 +456,7 @@ using KernelFn = void (*)(KParams);
 template <int LPR, int CPL, bool REALH, int DOT, int PREC>
 KernelFn kernel_for_prec() {
   if constexpr (PREC == KPMGB_PREC_FF) {
-    constexpr int CH = CPL >= 3 ? 4 : 8;
+    constexpr int CH = CPL >= 3 ? 4 : (CPL == 2 ? KPMGB_FF_CHUNK_CPL2 : KPMGB_FF_CHUNK_CPL1);
     return k_step_ff<LPR, CPL, REALH, DOT, CH>;
   } else {
     return k_step_f64<LPR, CPL, REALH, DOT>;

@@ -44,14 +44,20 @@ def _stale(target: Path, deps) -> bool:
     return any(Path(d).stat().st_mtime > t for d in deps)
 
 
-def build(verbose: bool = False, force: bool = False) -> Path:
-    """Compile libkpmgb.so if any source or header is newer than the library."""
+def build(verbose: bool = False, force: bool = False, defines=(), out: Path | None = None,
+          objdir: Path | None = None) -> Path:
+    """Compile libkpmgb.so if any source or header is newer than the library.
+
+    ``defines`` (e.g. ``["KPMGB_FF_MIN_BLOCKS=2"]``) set the kernels' tuning
+    macros; a tuned variant is written to ``out`` with objects in ``objdir``.
+    """
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
-    objdir = ROOT / "_build"
-    objdir.mkdir(exist_ok=True)
-    LIB_DIR.mkdir(exist_ok=True)
+    objdir = Path(objdir) if objdir else ROOT / "_build"
+    objdir.mkdir(parents=True, exist_ok=True)
+    lib_path = Path(out) if out else LIB_PATH
+    lib_path.parent.mkdir(parents=True, exist_ok=True)
     flags = ARCH + ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
-                    f"-I{INCLUDE}", f"-I{CSRC}"]
+                    f"-I{INCLUDE}", f"-I{CSRC}"] + [f"-D{d}" for d in defines]
     cc = nvcc()
 
     def compile_one(src: str) -> Path:
@@ -68,14 +74,14 @@ def build(verbose: bool = False, force: bool = False) -> Path:
 
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(SOURCES), os.cpu_count() or 1))) as ex:
         objs = list(ex.map(compile_one, SOURCES))
-    if force or _stale(LIB_PATH, objs):
-        tmp = LIB_PATH.with_suffix(".so.tmp")
+    if force or _stale(lib_path, objs):
+        tmp = lib_path.with_suffix(".so.tmp")
         cmd = [cc, *ARCH, "-shared", "-cudart", "static", "-o", str(tmp), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-        os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+        os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
