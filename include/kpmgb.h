@@ -150,6 +150,24 @@ int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
                        const void* psi_r, void* mu,
                        const kpmgb_kpm2d_options* opts, void* stream);
 
+/* kpm_1d doubling moments (FP64) for callers that cannot let the library
+ * allocate device memory: a host runtime that owns all device memory through
+ * its own pool and budget, or a loop that must not take the device-wide
+ * synchronisation of cudaMalloc/cudaFree.  This entry point has no
+ * counterpart in the reference.  All arguments are device memory owned by the
+ * caller: a row-major CSR (rowptr[NH+1], col[nnz] as 0-based int32, val[nnz]
+ * complex interleaved doubles), psi NH x NR column-major, mu_all NR x NC
+ * column-major.  Its scratch is one static device array of 64 MiB
+ * (2*NH*NR*16 bytes of recurrence vectors plus the moment partial sums must
+ * fit; larger sizes fail with KPMGB_ERR_ARGUMENT), held by every GPU that
+ * loads the library until exit.  The first call on a device resolves the
+ * array's device address; make that first call before any stream capture.
+ * Calls share the array, so calls that overlap on the GPU race.  Work runs on
+ * `stream` and the call waits for it. */
+int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int32_t* col,
+                        const double* val, int64_t NC, int64_t NR,
+                        const double* psi, double* mu_all, void* stream);
+
 /* Wait for the work enqueued on an operator and report any deferred failure
  * flagged by the kernels (non-finite moments, stability guard). */
 int kpmgb_operator_sync(kpmgb_operator op, void* stream);

@@ -32,6 +32,7 @@ EXPORTED_SYMBOLS = (
     "kpmgb_kpm2d_device",
     "kpmgb_operator_sync",
     "kpmgb_kernel_launch_count",
+    "kpmgb_kpm1d_noalloc",
 )
 
 
@@ -83,6 +84,7 @@ def _declare(lib):
     lib.kpmgb_kpm2d_device.argtypes = [vp, vp, vp, i64, i64, i64, vp, vp, vp,
                                        C.POINTER(Kpm2dOptions), vp]
     lib.kpmgb_operator_sync.argtypes = [vp, vp]
+    lib.kpmgb_kpm1d_noalloc.argtypes = [i64, vp, vp, vp, i64, i64, vp, vp, vp]
     for name in EXPORTED_SYMBOLS:
         if name not in ("kpmgb_version", "kpmgb_last_error", "kpmgb_kernel_launch_count"):
             getattr(lib, name).restype = C.c_int
