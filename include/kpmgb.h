@@ -75,7 +75,12 @@ typedef struct kpmgb_kpm1d_options {
                               (chebyshev_iteration.jl:110-133).  A non-finite
                               moment is always reported as NUMERICAL.          */
   int32_t use_graph;       /* 1: replay the recurrence as a CUDA graph        */
-  int32_t reserved;
+  int32_t kernel_variant;  /* 0: automatic; 1: register-gather step kernel;
+                              2: TMA-fed step kernel (float-float, NR >= 32,
+                              at most 16 nonzeros per row); 3: float-float
+                              kernel with per-column maxima anchors instead
+                              of per-row chunk anchors.  Automatic selection
+                              is the register-gather kernel.                    */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {
@@ -149,6 +154,33 @@ int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
                        int64_t NC, int64_t NR, int64_t NH, const void* psi_l,
                        const void* psi_r, void* mu,
                        const kpmgb_kpm2d_options* opts, void* stream);
+
+/* Batched ensemble: doubling kpm_1d moments of nseg independent members in one
+ * persistent launch (no reference counterpart as a single call; it replaces
+ * nseg calls of kpm_1d! on disorder realisations of uneven size).  H is the
+ * block-diagonal stack of the members; rows seg[i] .. seg[i+1]-1 belong to
+ * member i (seg[0] = 0, seg[nseg] = NH) and H must not couple members.  psi:
+ * host NH x NR column-major (member i's probes are its rows); mu_all: host,
+ * member i's NR x NC column-major moments at offset i*NR*NC complex values.
+ * 1 <= NR <= 32.  Blocking call. */
+int kpmgb_kpm1d_ensemble(kpmgb_operator H, int32_t nseg, const int64_t* seg,
+                         int64_t NC, int64_t NR, const double* psi,
+                         double* mu_all, const kpmgb_kpm1d_options* opts);
+
+/* Gradient of L = sum_m g[m] mu_m with respect to every stored entry of a
+ * Hermitian H, where mu are the probe-averaged doubling kpm_1d moments of
+ * kpmgb_kpm1d (src/moment.jl:420-492) and g[0..NC) are real weights dL/dmu
+ * supplied by the caller (e.g. from a DOS-window loss).  An adjoint
+ * Chebyshev recurrence runs backward over checkpoints stored every
+ * `checkpoint_every` steps (<= 0: 64) and an SDDMM accumulates the gradient
+ * on the sparsity pattern.  grad: host array of nnz complex values in the
+ * order of the CSC arrays given to kpmgb_operator_create, entry k holding
+ * dL/dRe(H_k) + i dL/dIm(H_k) (H_ij and H_ji are independent entries).
+ * FP64, 1 <= NR <= 32, NC even >= 4.  No reference counterpart (the
+ * reference differentiates through ForwardDiff duals).  Blocking call. */
+int kpmgb_kpm1d_grad(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,
+                     const double* psi, const double* g,
+                     int64_t checkpoint_every, double* grad);
 
 /* kpm_1d doubling moments (FP64) for callers that cannot let the library
  * allocate device memory: a host runtime that owns all device memory through

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -72,6 +73,7 @@ Operator::~Operator() {
   for (DevBuf* b : bufs) b->release();
   cudaFree(csr.rowptr);
   cudaFree(csr.col);
+  cudaFree(csr.perm);
   cudaFree(csr.val);
   cudaFree(csr.val_real);
   cudaFree(csr.val_ff);
@@ -109,6 +111,10 @@ int check_status(Operator* op, cudaStream_t s) {
   KPMGB_CUDA(cudaMemcpyAsync(&st, op->ws.sync.as<unsigned>() + 1, sizeof(unsigned),
                              cudaMemcpyDeviceToHost, s));
   KPMGB_CUDA(cudaStreamSynchronize(s));
+  if (st & STATUS_SCRATCH)
+    return fail(KPMGB_ERR_CUDA, "internal scratch buffer too small for the launch grid");
+  if (st & STATUS_TIMEOUT)
+    return fail(KPMGB_ERR_TIMEOUT, "a bounded wait inside a kernel expired (pipeline stalled)");
   if (st & STATUS_GROWTH)
     return fail(KPMGB_ERR_NUMERICAL,
                 "Chebyshev recurrence is unstable (a column norm grew beyond 1.5x its seed "
@@ -158,7 +164,10 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   const size_t slot = (size_t)NH * NR * 16;
   KPMGB_TRY(ws.slots.ensure(2 * slot));
   if (lr) KPMGB_TRY(ws.bra.ensure(slot));
-  KPMGB_TRY(ws.scales.ensure((size_t)(3 * NR + 2) * sizeof(double)));
+  // scales: 3*NR doubles, then 5*NR floats of column maxima (4-slot ring for
+  // the recurrence vectors + the bra), float-float path only
+  const size_t scale_bytes = (size_t)(3 * NR + 2) * sizeof(double);
+  KPMGB_TRY(ws.scales.ensure(scale_bytes + (size_t)5 * NR * sizeof(float)));
   KPMGB_TRY(ws.partials.ensure(step_partials_bytes(op->csr, NH, (int)NR, precision)));
   KPMGB_TRY(ensure_sync(op, s));
   char* slots = ws.slots.as<char>();
@@ -168,9 +177,18 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   KPMGB_TRY(launch_load_block(psi_r, sl[0], NH, (int)NR, precision, sc, false, s));
   if (lr) KPMGB_TRY(launch_load_block(psi_l, ws.bra.ptr, NH, (int)NR, precision, sc + NR, false, s));
   const double* mom_scale = nullptr;
+  float* mx = reinterpret_cast<float*>(ws.scales.as<char>() + scale_bytes);
+  auto ring = [&](int64_t k) { return mx + (k % 4) * NR; };
+  float* bmax = mx + 4 * NR;
+  const bool use_max = ff && o && o->kernel_variant == 3;
   if (ff) {
     KPMGB_TRY(launch_scale_product(sc, lr ? sc + NR : sc, sc + 2 * NR, (int)NR, s));
     mom_scale = sc + 2 * NR;
+  }
+  if (use_max) {
+    KPMGB_CUDA(cudaMemsetAsync(mx, 0, (size_t)5 * NR * sizeof(float), s));
+    KPMGB_TRY(launch_colmax(sl[0], NH, (int)NR, ring(0), s));
+    if (lr) KPMGB_TRY(launch_colmax(ws.bra.ptr, NH, (int)NR, bmax, s));
   }
   StepArgs a;
   a.H = &op->csr;
@@ -180,7 +198,9 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   a.mom_scale = mom_scale;
   a.sync = ws.sync.as<unsigned>();
   a.partials = ws.partials.ptr;
+  a.partials_bytes = ws.partials.bytes;
   a.bra = lr ? ws.bra.ptr : nullptr;
+  a.variant = o ? o->kernel_variant : 0;
   // alpha_1 = H alpha_0 with mu_0, mu_1 (src/moment.jl:440-449, :521-527)
   a.x = sl[0];
   a.z = nullptr;
@@ -190,6 +210,12 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   a.dot = lr ? DOT_LR2 : DOT_DOUBLING;
   a.mom = MOM_STORE;
   a.i0 = 0;
+  if (use_max) {
+    a.xmax = ring(0);
+    a.bmax = lr ? bmax : nullptr;
+    a.ymax_out = ring(1);
+    a.ymax_clear = ring(2);
+  }
   KPMGB_TRY(launch_step(a, precision, s));
   int ip = 1, ipp = 0;
   a.alpha = 2.0;
@@ -206,6 +232,12 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       a.mom = MOM_DOUBLING;
       a.i0 = 2 * n - 2;
       a.growth_limit = check ? 2.25 : 0.0;
+      if (use_max) {
+        a.xmax = ring(n - 1);
+        a.zmax = ring(n - 2);
+        a.ymax_out = ring(n);
+        a.ymax_clear = ring(n + 1);
+      }
       KPMGB_TRY(launch_step(a, precision, s));
       std::swap(ip, ipp);
     }
@@ -218,6 +250,12 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       a.dot = DOT_LR1;
       a.mom = MOM_STORE;
       a.i0 = n;
+      if (use_max) {
+        a.xmax = ring(n - 1);
+        a.zmax = ring(n - 2);
+        a.ymax_out = ring(n);
+        a.ymax_clear = ring(n + 1);
+      }
       KPMGB_TRY(launch_step(a, precision, s));
       std::swap(ip, ipp);
     }
@@ -326,6 +364,7 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
     a.beta = beta;
     a.sync = ws.sync.as<unsigned>();
     a.partials = ws.partials.ptr;
+    a.partials_bytes = ws.partials.bytes;
     return launch_step(a, precision, s);
   };
   // right seed Ja psi_r -> ring slot 3 (src/moment.jl:1021)
@@ -391,6 +430,7 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
       c.parity = opt.moment_parity;
       c.nmax_row = (int)nmax;
       c.mu = mu;
+      c.status = ws.sync.as<unsigned>() + 1;
       c.scratch = ws.gemm.ptr;
       c.scratch_bytes = ws.gemm.bytes;
       KPMGB_TRY(launch_contract(c, precision, opt.contraction, s));
@@ -449,17 +489,21 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
     rowptr[i + 1] += rowptr[i];
   }
   std::vector<int> col(nnz);
+  std::vector<int> perm(nnz);
   std::vector<double> val(2 * nnz);
   std::vector<int> fillp(rowptr.begin(), rowptr.end() - 1);
   int is_real = 1;
+  std::vector<double> rowsum(n, 0.0);
   for (int64_t j = 0; j < n; ++j) {
     for (int64_t k = colptr[j] - index_base; k < colptr[j + 1] - index_base; ++k) {
       const int64_t i = rowval[k] - index_base;
       const int dst = fillp[i]++;
       col[dst] = (int)j;
+      perm[dst] = (int)k;
       val[2 * dst] = nzval[2 * k];
       val[2 * dst + 1] = nzval[2 * k + 1];
       if (nzval[2 * k + 1] != 0.0) is_real = 0;
+      rowsum[i] += std::fabs(nzval[2 * k]) + std::fabs(nzval[2 * k + 1]);
     }
   }
   Operator* op = new Operator();
@@ -473,6 +517,7 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
   c.nnz = nnz;
   c.is_real = is_real;
   c.max_row_nnz = max_nnz;
+  for (int64_t i = 0; i < n; ++i) c.rmax = std::max(c.rmax, rowsum[i]);
   const size_t nz = (size_t)std::max<int64_t>(nnz, 1);
 #define CREATE_CUDA(call)                                                                   \
   do {                                                                                      \
@@ -484,12 +529,14 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
   CREATE_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
   CREATE_CUDA(cudaMalloc(&c.rowptr, (n + 1) * sizeof(int)));
   CREATE_CUDA(cudaMalloc(&c.col, nz * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&c.perm, nz * sizeof(int)));
   CREATE_CUDA(cudaMalloc(&c.val, nz * sizeof(double2)));
   if (is_real) CREATE_CUDA(cudaMalloc(&c.val_real, nz * sizeof(double)));
   CREATE_CUDA(cudaMalloc(&c.val_ff, nz * (is_real ? sizeof(float2) : sizeof(float4))));
   CREATE_CUDA(cudaMemcpy(c.rowptr, rowptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
   if (nnz > 0) {
     CREATE_CUDA(cudaMemcpy(c.col, col.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
+    CREATE_CUDA(cudaMemcpy(c.perm, perm.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
     CREATE_CUDA(cudaMemcpy(c.val, val.data(), nnz * sizeof(double2), cudaMemcpyHostToDevice));
     const int blocks = (int)std::min<int64_t>((nnz + 255) / 256, 4096);
     k_split_values<<<blocks, 256, 0, op->stream>>>(c.val, nnz, is_real, c.val_ff, c.val_real);
@@ -626,3 +673,110 @@ int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------ ensemble
+namespace kpmgb {
+int launch_ensemble(const DeviceCSR& H, const int64_t* d_seg, const int* d_order, int nseg, int NR,
+                    int64_t NC, void* slot0, void* slot1, double2* mu, const double* scale,
+                    unsigned* next, unsigned* status, int precision, cudaStream_t s);
+}
+
+extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_t* seg,
+                                    int64_t NC, int64_t NR, const double* psi, double* mu_all,
+                                    const kpmgb_kpm1d_options* opts) {
+  clear_error();
+  if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  if (nseg < 1 || !seg || !psi || !mu_all) return fail(KPMGB_ERR_ARGUMENT, "invalid ensemble arguments");
+  if (NC < 2 || NC % 2 != 0) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be even.");
+  if (NR < 1 || NR > 32) return fail(KPMGB_ERR_ARGUMENT, "the ensemble path supports 1 <= NR <= 32");
+  const int precision = opts ? opts->precision : KPMGB_PREC_FP64;
+  KPMGB_TRY(check_precision(precision));
+  Operator* op = as_op(h);
+  const int64_t NH = op->csr.n;
+  if (seg[0] != 0 || seg[nseg] != NH)
+    return fail(KPMGB_ERR_ARGUMENT, "segment table must run from 0 to the operator size %lld",
+                (long long)NH);
+  std::vector<int> order(nseg);
+  for (int i = 0; i < nseg; ++i) {
+    if (seg[i + 1] <= seg[i]) return fail(KPMGB_ERR_ARGUMENT, "segment %d is empty or unordered", i);
+    order[i] = i;
+  }
+  // largest members first: the persistent grid drains the queue evenly
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return seg[a + 1] - seg[a] > seg[b + 1] - seg[b];
+  });
+  Guard g(op);
+  cudaStream_t s = op->stream;
+  Workspace& ws = op->ws;
+  const size_t slot = (size_t)NH * NR * 16;
+  KPMGB_TRY(ws.psi_in.ensure(slot));
+  KPMGB_TRY(ws.slots.ensure(2 * slot));
+  KPMGB_TRY(ws.mu.ensure((size_t)nseg * NC * NR * 16));
+  KPMGB_TRY(ws.scales.ensure((size_t)(3 * NR + 2) * sizeof(double)));
+  // segment table + order + work counter in the partials buffer (small)
+  const size_t meta = (size_t)(nseg + 1) * sizeof(int64_t) + (size_t)nseg * sizeof(int) + 64;
+  KPMGB_TRY(ws.partials.ensure(std::max(meta, ws.partials.bytes)));
+  KPMGB_TRY(ensure_sync(op, s));
+  char* mp = ws.partials.as<char>();
+  int64_t* d_seg = reinterpret_cast<int64_t*>(mp);
+  int* d_order = reinterpret_cast<int*>(mp + (size_t)(nseg + 1) * sizeof(int64_t));
+  unsigned* next = ws.sync.as<unsigned>() + 2;
+  KPMGB_CUDA(cudaMemcpyAsync(d_seg, seg, (size_t)(nseg + 1) * sizeof(int64_t),
+                             cudaMemcpyHostToDevice, s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_order, order.data(), (size_t)nseg * sizeof(int),
+                             cudaMemcpyHostToDevice, s));
+  KPMGB_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned), s));
+  KPMGB_CUDA(cudaMemcpyAsync(ws.psi_in.ptr, psi, slot, cudaMemcpyHostToDevice, s));
+  char* slots = ws.slots.as<char>();
+  double* sc = ws.scales.as<double>();
+  const bool ff = precision == KPMGB_PREC_FF;
+  KPMGB_TRY(launch_load_block(ws.psi_in.ptr, slots, NH, (int)NR, precision, sc, false, s));
+  const double* scale = nullptr;
+  if (ff) {
+    KPMGB_TRY(launch_scale_product(sc, sc, sc + 2 * NR, (int)NR, s));
+    scale = sc + 2 * NR;
+  }
+  KPMGB_TRY(launch_ensemble(op->csr, d_seg, d_order, nseg, (int)NR, NC, slots, slots + slot,
+                            ws.mu.as<double2>(), scale, next, ws.sync.as<unsigned>() + 1,
+                            precision, s));
+  KPMGB_CUDA(cudaMemcpyAsync(mu_all, ws.mu.ptr, (size_t)nseg * NC * NR * 16,
+                             cudaMemcpyDeviceToHost, s));
+  return check_status(op, s);
+}
+
+// ------------------------------------------------------------ adjoint
+namespace kpmgb {
+int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, int64_t NH,
+                   const double2* psi_rowmajor, const double* g, int64_t C, double2* d_grad_csr,
+                   double2* d_grad_csc, DevBuf& work, cudaStream_t s);
+}
+
+extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH,
+                                const double* psi, const double* g, int64_t checkpoint_every,
+                                double* grad) {
+  clear_error();
+  if (!h || !psi || !g || !grad) return fail(KPMGB_ERR_ARGUMENT, "null argument");
+  if (NC < 4 || NC % 2 != 0) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be even and >= 4.");
+  if (NR < 1 || NR > 32) return fail(KPMGB_ERR_ARGUMENT, "the gradient path supports 1 <= NR <= 32");
+  Operator* op = as_op(h);
+  if (NH != op->csr.n) return fail(KPMGB_ERR_ARGUMENT, "psi has %lld rows; the operator has %lld",
+                                   (long long)NH, (long long)op->csr.n);
+  if (op->csr.nnz < 1) return fail(KPMGB_ERR_ARGUMENT, "empty operator");
+  Guard gd(op);
+  cudaStream_t s = op->stream;
+  Workspace& ws = op->ws;
+  const size_t blk = (size_t)NH * NR * 16;
+  KPMGB_TRY(ws.psi_in.ensure(2 * blk));
+  KPMGB_TRY(ws.gemm.ensure(std::max(ws.gemm.bytes, (size_t)2 * op->csr.nnz * 16)));
+  KPMGB_TRY(ensure_sync(op, s));
+  char* in = ws.psi_in.as<char>();
+  KPMGB_CUDA(cudaMemcpyAsync(in, psi, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(launch_load_block(in, in + blk, NH, (int)NR, KPMGB_PREC_FP64, nullptr, false, s));
+  double2* gcsr = ws.gemm.as<double2>();
+  double2* gcsc = gcsr + op->csr.nnz;
+  KPMGB_TRY(run_kpm1d_grad(op->csr, op->csr.perm, NC, (int)NR, NH,
+                           reinterpret_cast<const double2*>(in + blk), g,
+                           checkpoint_every > 0 ? checkpoint_every : 64, gcsr, gcsc, ws.split, s));
+  KPMGB_CUDA(cudaMemcpyAsync(grad, gcsc, (size_t)op->csr.nnz * 16, cudaMemcpyDeviceToHost, s));
+  return check_status(op, s);
+}

@@ -1,14 +1,573 @@
-// kpm_2d contraction on the tensor cores (split-precision form).
+// kpm_2d moment-matrix contraction on the tensor cores (tcgen05), split form.
+//
+// Gamma[a, b] = sum_k R[a][k] conj(L[b][k]) is one real GEMM over K' = 2K:
+// row a of A holds (Re R_0, Im R_0, Re R_1, ...), row b of B holds
+// (Re L_0, Im L_0, ...) for the real part and row nl + b holds
+// (-Im L_0, Re L_0, ...) for the imaginary part.
+//
+// Precision (slicing in the manner of Ozaki's scheme): every row is scaled by
+// 2^-e (e: exponent of the row's largest entry) and written as five signed
+// 8-bit digits d_0..d_4 (|d| <= 128), stored pre-scaled as BF16 planes
+// p_i = d_i 2^(-8i) (exact), so that
+//     v = 2^(e-7) * sum_i p_i          (truncation < 2^-40 of the row max)
+// and every plane product carries its own weight.  The 15 plane pairs with
+// i + j <= 4 feed three TMEM accumulators (128 x 64 FP32 each): level 0
+// (p_0 q_0, integers), level 1 (p_0 q_1 + p_1 q_0, multiples of 2^-8) and
+// levels >= 2 together.  Over a chunk of 256 K' elements the first two stay
+// below 2^22 and 2^15 and are therefore exact in the tensor core's FP32
+// accumulation; the third holds contributions below 2^-16 of the first, so
+// its FP32 rounding is below 2^-39 of the result.  After each chunk the
+// epilogue warps fold the three accumulators into one int64 per output in
+// units of 2^-16 (exact for levels 0-1) and the chunk accumulators are reused.
+//
+// Data movement: the digit planes are pre-tiled in global memory in the
+// canonical no-swizzle K-major UMMA layout, so each pipeline stage is two
+// bulk copies (cp.async.bulk, 40 KiB of A planes and 20 KiB of B planes)
+// completed on an mbarrier.  Warp roles per CTA: 0 producer, 1 MMA issuer
+// (one thread), 2-5 epilogue (one TMEM lane each).  All waits are bounded.
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
 
 #include "kpmgb_internal.h"
 
 namespace kpmgb {
 
-size_t contract_split_scratch_bytes(int64_t, int, int) { return 0; }
+namespace {
 
-int launch_contract_split(const ContractArgs&, int, cudaStream_t) {
-  return fail(KPMGB_ERR_ARGUMENT, "split-precision contraction is not available in this build");
+constexpr int TC_M = 128;      // A rows per tile
+constexpr int TC_N = 64;       // B rows per tile
+constexpr int TC_KT = 32;      // real K' elements per k-tile
+constexpr int TC_SLICES = 5;   // digit planes per operand
+constexpr int TC_ACC = 3;      // TMEM accumulators: level 0, level 1, levels >= 2
+constexpr int TC_CHUNK = 8;    // k-tiles per exact chunk (256 K' elements)
+constexpr int TC_STAGES = 3;
+constexpr uint32_t A_TILE = TC_M * TC_KT * 2;  // 8 KiB per plane
+constexpr uint32_t B_TILE = TC_N * TC_KT * 2;  // 4 KiB per plane
+constexpr uint32_t A_STAGE = A_TILE * TC_SLICES;
+constexpr uint32_t B_STAGE = B_TILE * TC_SLICES;
+constexpr uint32_t STAGE_BYTES = A_STAGE + B_STAGE;
+constexpr int TMEM_COLS = 512;  // 2 buffers x 3 accumulators x 64 columns (384 used)
+constexpr int TMEM_BUF = TC_ACC * TC_N;
+constexpr int kSpin = 1 << 22;
+constexpr int kThreadsTC = 192;  // 6 warps
+
+// --------------------------------------------------------------- PTX helpers
+__device__ __forceinline__ uint32_t saddr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bar_init(uint32_t b, uint32_t n) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(b), "r"(n) : "memory");
+}
+__device__ __forceinline__ void bar_expect(uint32_t b, uint32_t tx) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(tx)
+               : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint32_t b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(b) : "memory");
+}
+__device__ __forceinline__ bool bar_wait(uint32_t b, uint32_t parity) {
+  for (int i = 0; i < kSpin; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(b), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_copy(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
+      : "memory");
+}
+// UMMA shared-memory descriptor, no swizzle, K-major: LBO = 128 B between the
+// two K-adjacent 8x16-byte core matrices, SBO = 256 B between 8-row groups.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)(128 >> 4) << 16;
+  d |= (uint64_t)(256 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+                            ((uint32_t)(TC_M >> 4) << 24);
+
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
+        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
+        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// --------------------------------------------------------------- pre-passes
+// Byte offset of element (r, k) inside a ROWS x TC_KT tile (canonical layout).
+template <int ROWS>
+__host__ __device__ __forceinline__ uint32_t tile_off(int r, int k) {
+  return (uint32_t)((k >> 4) * (ROWS * 32) + (r >> 3) * 256 + ((k >> 3) & 1) * 128 + (r & 7) * 16 +
+                    (k & 7) * 2);
+}
+
+template <bool FF>
+__device__ __forceinline__ void load_pair(const void* base, int64_t idx, float& rh, float& rl,
+                                          float& ih, float& il) {
+  if constexpr (FF) {
+    const float4 v = __ldg(static_cast<const float4*>(base) + idx);
+    rh = v.x; rl = v.y; ih = v.z; il = v.w;
+  } else {
+    const double2 v = __ldg(static_cast<const double2*>(base) + idx);
+    rh = __double2float_rn(v.x); rl = __double2float_rn(v.x - (double)rh);
+    ih = __double2float_rn(v.y); il = __double2float_rn(v.y - (double)ih);
+  }
+}
+
+// Exponent e of each vector with max |entry| < 2^e (0 for a zero vector).
+template <bool FF>
+__global__ void __launch_bounds__(256) k_vec_exp(const void* vecs, int64_t K, int nvec, int* exps) {
+  const int v = blockIdx.x;
+  if (v >= nvec) return;
+  float m = 0.f;
+  for (int64_t k = threadIdx.x; k < K; k += 256) {
+    float rh, rl, ih, il;
+    load_pair<FF>(vecs, (int64_t)v * K + k, rh, rl, ih, il);
+    m = fmaxf(m, fmaxf(fabsf(rh), fabsf(ih)));
+  }
+  __shared__ float red[256];
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const float mx = red[0];
+    int e = 0;
+    if (mx > 0.f && isfinite(mx)) {
+      frexpf(mx, &e);  // mx in [2^(e-1), 2^e)
+      // (hi + lo) stays below 2^e as well: |lo| <= ulp(hi)/2
+    }
+    exps[v] = e;
+  }
+}
+
+// Five signed digits of the scaled value (vh + vl) * 2^-e.
+__device__ __forceinline__ void digits(float vh, float vl, int e, float (&d)[TC_SLICES]) {
+  const float th = ldexpf(vh, 7 - e), tl = ldexpf(vl, 7 - e);
+  d[0] = rintf(th);
+  float r = __fadd_rn(__fsub_rn(th, d[0]), tl);
+#pragma unroll
+  for (int i = 1; i < TC_SLICES; ++i) {
+    const float t = __fmul_rn(r, 256.f);
+    d[i] = rintf(t);
+    r = __fsub_rn(t, d[i]);
+  }
+}
+
+// Write the digit planes of A (R vectors) or B/B' (L vectors) in the
+// pre-tiled layout.  One thread per (row, group of 8 real K' elements).
+template <bool FF, bool IS_B>
+__global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int nvec,
+                                               const int* exps, int64_t ktiles, int rows_pad,
+                                               uint8_t* planes) {
+  constexpr int ROWS = IS_B ? TC_N : TC_M;
+  constexpr uint32_t TILE = IS_B ? B_TILE : A_TILE;
+  const int64_t groups = ktiles * (TC_KT / 8);
+  const int64_t total = (int64_t)nvec * groups;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(idx / groups);
+    const int64_t g = idx - (int64_t)v * groups;
+    const int64_t kp0 = g * 8;  // first real K' element
+    const int e = exps[v];
+    float d[8][TC_SLICES];
+    float dq[8][TC_SLICES];  // B' digits (IS_B only)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t kc = kp0 / 2 + j;  // complex element
+      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+      if (kc < K) load_pair<FF>(vecs, (int64_t)v * K + kc, rh, rl, ih, il);
+      digits(rh, rl, e, d[2 * j]);
+      digits(ih, il, e, d[2 * j + 1]);
+      if constexpr (IS_B) {
+#pragma unroll
+        for (int i = 0; i < TC_SLICES; ++i) {
+          dq[2 * j][i] = -d[2 * j + 1][i];
+          dq[2 * j + 1][i] = d[2 * j][i];
+        }
+      }
+    }
+    const int64_t kt = kp0 / TC_KT;
+    const int kin = (int)(kp0 % TC_KT);
+    auto store = [&](int row, float (&dd)[8][TC_SLICES]) {
+      const int tile = row / ROWS, r = row % ROWS;
+      uint8_t* tbase = planes + ((size_t)(tile * ktiles + kt) * TC_SLICES) * TILE;
+#pragma unroll
+      for (int i = 0; i < TC_SLICES; ++i) {
+        __nv_bfloat16 h[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(ldexpf(dd[q][i], -8 * i));
+        *reinterpret_cast<uint4*>(tbase + (size_t)i * TILE + tile_off<ROWS>(r, kin)) =
+            *reinterpret_cast<const uint4*>(h);
+      }
+    };
+    store(v, d);
+    if constexpr (IS_B) store(nvec + v, dq);
+  }
+}
+
+// Zero the padding rows of a plane array (rows nrows..rows_pad-1).
+__global__ void k_zero(uint8_t* p, size_t bytes) {
+  for (size_t i = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * 16; i < bytes;
+       i += (size_t)gridDim.x * blockDim.x * 16)
+    *reinterpret_cast<uint4*>(p + i) = make_uint4(0, 0, 0, 0);
+}
+
+// --------------------------------------------------------------- GEMM
+struct TcArgs {
+  const uint8_t* A;      // planes [mtiles][ktiles][4][A_TILE]
+  const uint8_t* B;      // planes [ntiles][ktiles][4][B_TILE]
+  int64_t ktiles;
+  int64_t kt_per_split;
+  int nr, ncols;         // real rows of A, real rows of B (2 nl)
+  const int* expA;
+  const int* expB;       // per B row (L vector index = row % nl)
+  int nl;
+  double* part;          // [split][nr][ncols]
+  unsigned* status;
+};
+
+__global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  __shared__ __align__(8) uint64_t bars[4 * TC_STAGES];  // full, empty, tfull, tempty
+  __shared__ uint32_t s_tmem;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y, sp = blockIdx.z;
+  const int64_t kt0 = (int64_t)sp * p.kt_per_split;
+  const int64_t kt1 = min(p.ktiles, kt0 + p.kt_per_split);
+  const int64_t nkt = kt1 > kt0 ? kt1 - kt0 : 0;
+  const int64_t nchunks = (nkt + TC_CHUNK - 1) / TC_CHUNK;
+  const uint32_t full0 = saddr(&bars[0]), empty0 = saddr(&bars[TC_STAGES]);
+  const uint32_t tfull0 = saddr(&bars[2 * TC_STAGES]), tempty0 = saddr(&bars[3 * TC_STAGES]);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      bar_init(full0 + 8 * s, 1);
+      bar_init(empty0 + 8 * s, 1);
+      bar_init(tfull0 + 8 * s, 1);
+      bar_init(tempty0 + 8 * s, 4);
+    }
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     saddr(&s_tmem)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = s_tmem;
+  const uint32_t sm0 = saddr(smem);
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      for (int64_t i = 0; i < nkt; ++i) {
+        const int s = (int)(i % TC_STAGES);
+        const uint32_t ph = (uint32_t)((i / TC_STAGES) & 1);
+        if (!bar_wait(empty0 + 8 * s, ph ^ 1)) {
+          atomicOr(p.status, (unsigned)STATUS_TIMEOUT);
+          break;
+        }
+        const int64_t kt = kt0 + i;
+        bar_expect(full0 + 8 * s, STAGE_BYTES);
+        bulk_copy(sm0 + s * STAGE_BYTES,
+                  p.A + ((size_t)(mt * p.ktiles + kt) * TC_SLICES) * A_TILE, A_STAGE,
+                  full0 + 8 * s);
+        bulk_copy(sm0 + s * STAGE_BYTES + A_STAGE,
+                  p.B + ((size_t)(nt * p.ktiles + kt) * TC_SLICES) * B_TILE, B_STAGE,
+                  full0 + 8 * s);
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      int64_t i = 0;
+      bool ok = true;
+      for (int64_t c = 0; c < nchunks && ok; ++c) {
+        const int buf = (int)(c & 1);
+        if (!bar_wait(tempty0 + 8 * buf, (uint32_t)(((c >> 1) & 1) ^ 1))) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        bool started[TC_ACC] = {false, false, false};
+        const int64_t rem = nkt - c * TC_CHUNK;
+        const int64_t tiles = rem < TC_CHUNK ? rem : TC_CHUNK;
+        for (int64_t t = 0; t < tiles; ++t, ++i) {
+          const int s = (int)(i % TC_STAGES);
+          if (!bar_wait(full0 + 8 * s, (uint32_t)((i / TC_STAGES) & 1))) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t a0 = sm0 + s * STAGE_BYTES, b0 = a0 + A_STAGE;
+#pragma unroll
+          for (int ks = 0; ks < TC_KT / 16; ++ks) {
+#pragma unroll
+            for (int ia = 0; ia < TC_SLICES; ++ia)
+#pragma unroll
+              for (int ib = 0; ib < TC_SLICES - ia; ++ib) {
+                const int acc = ia + ib < 2 ? ia + ib : 2;
+                const uint64_t ad = umma_desc(a0 + ia * A_TILE + ks * (TC_M * 32));
+                const uint64_t bd = umma_desc(b0 + ib * B_TILE + ks * (TC_N * 32));
+                umma(tmem + buf * TMEM_BUF + acc * TC_N, ad, bd, started[acc] ? 1u : 0u);
+                started[acc] = true;
+              }
+          }
+          umma_commit(empty0 + 8 * s);  // stage free once these MMAs retire
+        }
+        if (ok) umma_commit(tfull0 + 8 * buf);
+      }
+      if (!ok) atomicOr(p.status, (unsigned)STATUS_TIMEOUT);
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int q = warp & 3;          // TMEM lane quarter this warp may access
+    const int row = q * 32 + lane;   // tile row = TMEM lane
+    long long acc[TC_N];
+#pragma unroll
+    for (int j = 0; j < TC_N; ++j) acc[j] = 0;
+    bool ok = true;
+    for (int64_t c = 0; c < nchunks; ++c) {
+      const int buf = (int)(c & 1);
+      if (!bar_wait(tfull0 + 8 * buf, (uint32_t)((c >> 1) & 1))) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int ac = 0; ac < TC_ACC; ++ac) {
+        // in units of 2^-16: level 0 is an integer, level 1 a multiple of
+        // 2^-8 (both exact), levels >= 2 rounded to 2^-16
+        const float unit = ac == 0 ? 1.f : (ac == 1 ? 256.f : 65536.f);
+        const int shift = ac == 0 ? 16 : (ac == 1 ? 8 : 0);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          uint32_t v[32];
+          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * TMEM_BUF + ac * TC_N + h * 32, v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const long long iv =
+                (long long)__float2int_rn(__fmul_rn(__uint_as_float(v[j]), unit));
+            acc[h * 32 + j] += iv << shift;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) bar_arrive(tempty0 + 8 * buf);
+    }
+    if (!ok) atomicOr(p.status, (unsigned)STATUS_TIMEOUT);
+    const int a = mt * TC_M + row;
+    if (a < p.nr) {
+      // value = acc * 2^-16 * 2^(eA - 7) * 2^(eB - 7)
+      const int ea = p.expA[a];
+#pragma unroll
+      for (int j = 0; j < TC_N; ++j) {
+        const int col = nt * TC_N + j;
+        if (col < p.ncols) {
+          const int eb = p.expB[col % p.nl];
+          const double vv = ldexp((double)acc[j], ea + eb - 30);
+          p.part[((size_t)sp * p.nr + a) * p.ncols + col] = vv;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+__device__ __forceinline__ bool keep_parity(int parity, int n, int m) {
+  if (parity == KPMGB_PARITY_NONE) return true;
+  const bool odd = ((n + m) & 1) != 0;
+  return parity == KPMGB_PARITY_ODD ? odd : !odd;
+}
+
+__global__ void k_tc_reduce(const double* __restrict__ part, int nsplit, int nr, int nl, int n0,
+                            int m0, int NC, double inv_nr, const double* __restrict__ dscale,
+                            int parity, int nmax_row, double2* __restrict__ mu) {
+  const int64_t total = (int64_t)nr * nl;
+  const int ncols = 2 * nl;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(e / nl), b = (int)(e % nl);
+    const int n = n0 + a, m = m0 + b;
+    if (n >= nmax_row || !keep_parity(parity, n, m)) continue;
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < nsplit; ++s) {
+      re += part[((size_t)s * nr + a) * ncols + b];
+      im += part[((size_t)s * nr + a) * ncols + nl + b];
+    }
+    const double f = dscale ? inv_nr * dscale[0] : inv_nr;
+    double2* dst = mu + (size_t)n + (size_t)NC * m;
+    dst->x += re * f;
+    dst->y += im * f;
+  }
+}
+
+int sm_count() {
+  static int n = [] {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
+struct TcPlan {
+  int mtiles, ntiles, nsplit;
+  int64_t ktiles, kt_per_split;
+  size_t a_bytes, b_bytes, exp_bytes, part_bytes;
+};
+
+TcPlan plan_for(int64_t K, int nr, int nl) {
+  TcPlan pl;
+  pl.mtiles = (nr + TC_M - 1) / TC_M;
+  pl.ntiles = (2 * nl + TC_N - 1) / TC_N;
+  pl.ktiles = (2 * K + TC_KT - 1) / TC_KT;
+  const int64_t tiles = (int64_t)pl.mtiles * pl.ntiles;
+  int64_t want = std::max<int64_t>(1, (2 * (int64_t)sm_count() + tiles - 1) / tiles);
+  want = std::min<int64_t>(want, std::max<int64_t>(1, pl.ktiles / (4 * TC_CHUNK)));
+  pl.kt_per_split = (pl.ktiles + want - 1) / want;
+  pl.kt_per_split = (pl.kt_per_split + TC_CHUNK - 1) / TC_CHUNK * TC_CHUNK;
+  pl.nsplit = (int)((pl.ktiles + pl.kt_per_split - 1) / pl.kt_per_split);
+  pl.a_bytes = (size_t)pl.mtiles * pl.ktiles * TC_SLICES * A_TILE;
+  pl.b_bytes = (size_t)pl.ntiles * pl.ktiles * TC_SLICES * B_TILE;
+  pl.exp_bytes = ((size_t)(nr + nl) * sizeof(int) + 255) & ~size_t(255);
+  pl.part_bytes = (size_t)pl.nsplit * nr * 2 * nl * sizeof(double);
+  return pl;
+}
+
+}  // namespace
+
+size_t contract_split_scratch_bytes(int64_t K, int nr, int nl) {
+  // the largest plan over sub-blocks nr' <= nr, nl' <= nl is the full block's
+  // (plane sizes grow with nr, nl; partials stay within 2*SMs tiles of work)
+  const TcPlan pl = plan_for(K, nr, nl);
+  const size_t part_bound = (size_t)(2 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N *
+                            sizeof(double);
+  return pl.a_bytes + pl.b_bytes + pl.exp_bytes + std::max(pl.part_bytes, part_bound) + 1024;
+}
+
+int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) {
+  const TcPlan pl = plan_for(a.K, a.nr, a.nl);
+  const size_t part_bound =
+      (size_t)(2 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N * sizeof(double);
+  const size_t need = pl.a_bytes + pl.b_bytes + pl.exp_bytes +
+                      std::max(pl.part_bytes, part_bound) + 1024;
+  if (need > a.scratch_bytes) return fail(KPMGB_ERR_ALLOC, "split contraction scratch too small");
+  if (!a.status) return fail(KPMGB_ERR_ARGUMENT, "split contraction needs a status word");
+  uint8_t* base = static_cast<uint8_t*>(a.scratch);
+  base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023));
+  uint8_t* A = base;
+  uint8_t* B = A + pl.a_bytes;
+  int* expA = reinterpret_cast<int*>(B + pl.b_bytes);
+  int* expB = expA + a.nr;
+  double* part = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(expA) + pl.exp_bytes);
+  const bool ff = precision == KPMGB_PREC_FF;
+  // exponents
+  if (ff) {
+    k_vec_exp<true><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
+    k_vec_exp<true><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
+  } else {
+    k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
+    k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
+  }
+  KPMGB_LAUNCHED();
+  // digit planes (padding rows zeroed first)
+  const int rowsA = pl.mtiles * TC_M, rowsB = pl.ntiles * TC_N;
+  if (rowsA > a.nr || rowsB > 2 * a.nl) {
+    k_zero<<<2048, 256, 0, s>>>(A, pl.a_bytes + pl.b_bytes);
+    KPMGB_LAUNCHED();
+  }
+  const int64_t groupsA = (int64_t)a.nr * pl.ktiles * (TC_KT / 8);
+  const int64_t groupsB = (int64_t)a.nl * pl.ktiles * (TC_KT / 8);
+  const int gA = (int)std::min<int64_t>((groupsA + 255) / 256, 65535 * 16);
+  const int gB = (int)std::min<int64_t>((groupsB + 255) / 256, 65535 * 16);
+  if (ff) {
+    k_slice<true, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A);
+    k_slice<true, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
+  } else {
+    k_slice<false, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A);
+    k_slice<false, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
+  }
+  KPMGB_LAUNCHED();
+  // GEMM
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(k_contract_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)(TC_STAGES * STAGE_BYTES));
+  });
+  if (attr_err != cudaSuccess)
+    return fail(KPMGB_ERR_CUDA, "cannot configure the tensor-core contraction: %s",
+                cudaGetErrorString(attr_err));
+  TcArgs t;
+  t.A = A;
+  t.B = B;
+  t.ktiles = pl.ktiles;
+  t.kt_per_split = pl.kt_per_split;
+  t.nr = a.nr;
+  t.ncols = 2 * a.nl;
+  t.expA = expA;
+  t.expB = expB;
+  t.nl = a.nl;
+  t.part = part;
+  t.status = a.status;
+  dim3 grid(pl.mtiles, pl.ntiles, pl.nsplit);
+  k_contract_tc<<<grid, kThreadsTC, TC_STAGES * STAGE_BYTES, s>>>(t);
+  KPMGB_LAUNCHED();
+  const int64_t total = (int64_t)a.nr * a.nl;
+  const int blocks = (int)std::min<int64_t>((total + 255) / 256, 2048);
+  k_tc_reduce<<<std::max(blocks, 1), 256, 0, s>>>(part, pl.nsplit, a.nr, a.nl, a.n0, a.m0, a.NC,
+                                                  a.inv_nr, a.dscale, a.parity, a.nmax_row, a.mu);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
 }
 
 }  // namespace kpmgb

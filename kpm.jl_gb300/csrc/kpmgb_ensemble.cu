@@ -1,0 +1,339 @@
+// Batched ensemble of independent kpm_1d problems in one persistent launch.
+//
+// The members (e.g. disorder realisations of different sizes) are stacked as
+// one block-diagonal operator with a segment table seg[0..nseg] of row
+// offsets.  Each CTA takes whole members from a work queue (largest first)
+// and runs the complete doubling recurrence of its member (NC/2 steps) with
+// CTA barriers between steps, so one launch replaces nseg * NC/2 launches and
+// a member's vectors stay hot in L2 while it is processed.  The per-step
+// moment reductions are CTA-local and fixed-order, so the moments of a member
+// do not depend on which SM ran it.
+//
+// Arithmetic is FP64 or float-float (the same anchored accumulation as the
+// single-problem kernels).  Inside the loop the vector slots are read with
+// coherent loads (they are rewritten by the same CTA between steps).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
+#include "kpmgb_ffmath.cuh"
+#include "kpmgb_internal.h"
+
+namespace kpmgb {
+namespace {
+
+constexpr int kEnsThreads = 256;
+constexpr int kEnsWarps = kEnsThreads / 32;
+
+struct EnsParams {
+  const int* rowptr;
+  const int* col;
+  const void* val;       // double/double2 (FP64) or float2/float4 (FF)
+  const int64_t* seg;    // nseg + 1 row offsets
+  const int* order;      // members in processing order
+  int nseg;
+  int NR;
+  int64_t NC;
+  void* slot0;           // probes (row-major, working precision), overwritten
+  void* slot1;
+  double2* mu;           // [nseg][NC][NR]
+  const double* scale;   // per column moment factor (FF), or null
+  unsigned* next;        // work counter (zeroed before the launch)
+  unsigned* status;
+};
+
+// ---------------------------------------------------------------- arithmetic
+template <bool FF, bool REALH>
+struct Arith;
+
+template <bool REALH>
+struct Arith<false, REALH> {
+  using V = double2;
+  using HV = typename std::conditional<REALH, double, double2>::type;
+  struct Acc {
+    double2 a;
+  };
+  static __device__ __forceinline__ V zero() { return make_double2(0.0, 0.0); }
+  static __device__ __forceinline__ void mac(double2& acc, double h, double2 v) {
+    acc.x = fma(h, v.x, acc.x);
+    acc.y = fma(h, v.y, acc.y);
+  }
+  static __device__ __forceinline__ void mac(double2& acc, double2 h, double2 v) {
+    acc.x = fma(h.x, v.x, acc.x);
+    acc.x = fma(-h.y, v.y, acc.x);
+    acc.y = fma(h.x, v.y, acc.y);
+    acc.y = fma(h.y, v.x, acc.y);
+  }
+};
+
+__device__ __forceinline__ float ens_habs(float2 h) { return fabsf(h.x); }
+__device__ __forceinline__ float ens_habs(float4 h) { return fabsf(h.x) + fabsf(h.z); }
+
+__device__ __forceinline__ void ens_ffmac(float& Ar, float& Cr, float& Ai, float& Ci, float2 h,
+                                          float4 v) {
+  ff::amac(Ar, Cr, h.x, h.y, v.x, v.y);
+  ff::amac(Ai, Ci, h.x, h.y, v.z, v.w);
+}
+__device__ __forceinline__ void ens_ffmac(float& Ar, float& Cr, float& Ai, float& Ci, float4 h,
+                                          float4 v) {
+  ff::amac(Ar, Cr, h.x, h.y, v.x, v.y);
+  ff::amac(Ar, Cr, -h.z, -h.w, v.z, v.w);
+  ff::amac(Ai, Ci, h.x, h.y, v.z, v.w);
+  ff::amac(Ai, Ci, h.z, h.w, v.x, v.y);
+}
+
+__device__ __forceinline__ float2 ens_epi(float S, float C, float alpha, bool sub, float zh,
+                                          float zl) {
+  const float u = __fmul_rn(alpha, S), c = __fmul_rn(alpha, C);
+  float h, l;
+  if (!sub) {
+    ff::renorm(u, c, h, l);
+  } else {
+    float s, e;
+    ff::two_sum(u, -zh, s, e);
+    ff::renorm(s, __fadd_rn(e, __fsub_rn(c, zl)), h, l);
+  }
+  return make_float2(h, l);
+}
+
+// One row of y = alpha H x - [sub] z for column cc (LPR lanes per row).
+template <bool FF, bool REALH, int CH>
+__device__ __forceinline__ void row_value(const EnsParams& p, const void* xv, int64_t r, int cc,
+                                          float alpha_f, double alpha, bool sub, const void* zv,
+                                          void* yv, double2& xout, double2& yout, float4& xff,
+                                          float4& yff) {
+  const int k0 = p.rowptr[r], k1 = p.rowptr[r + 1];
+  const int64_t idx = r * p.NR + cc;
+  if constexpr (!FF) {
+    using HV = typename Arith<false, REALH>::HV;
+    const double2* x = static_cast<const double2*>(xv);
+    const HV* val = static_cast<const HV*>(p.val);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int k = k0; k < k1; ++k) Arith<false, REALH>::mac(acc, val[k], x[(int64_t)p.col[k] * p.NR + cc]);
+    double2 y = make_double2(alpha * acc.x, alpha * acc.y);
+    if (sub) {
+      const double2 z = static_cast<const double2*>(zv)[idx];
+      y.x -= z.x;
+      y.y -= z.y;
+    }
+    static_cast<double2*>(yv)[idx] = y;
+    xout = x[idx];
+    yout = y;
+  } else {
+    using HV = typename std::conditional<REALH, float2, float4>::type;
+    const float4* x = static_cast<const float4*>(xv);
+    const HV* val = static_cast<const HV*>(p.val);
+    float Sr = 0.f, Cr = 0.f, Si = 0.f, Ci = 0.f;
+    for (int kc = k0; kc < k1; kc += CH) {
+      const int cnt = min(CH, k1 - kc);
+      HV hv[CH];
+      float4 xs[CH];
+      float R = 0.f, M = 0.f;
+#pragma unroll
+      for (int u = 0; u < CH; ++u) {
+        if (u < cnt) {
+          hv[u] = val[kc + u];
+          xs[u] = x[(int64_t)p.col[kc + u] * p.NR + cc];
+        } else {
+          if constexpr (REALH) hv[u] = make_float2(0.f, 0.f);
+          else hv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+          xs[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        R = __fadd_rn(R, ens_habs(hv[u]));
+        M = fmaxf(M, fmaxf(fabsf(xs[u].x), fabsf(xs[u].z)));
+      }
+      const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+      const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+      float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+      for (int u = 0; u < CH; ++u)
+        if (u < cnt) ens_ffmac(Ar, cr, Ai, ci, hv[u], xs[u]);
+      const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+      if (kc == k0) {
+        Sr = sr; Cr = cr; Si = si; Ci = ci;
+      } else {
+        float s, e;
+        ff::two_sum(Sr, sr, s, e);
+        Sr = s;
+        Cr = __fadd_rn(Cr, __fadd_rn(cr, e));
+        ff::two_sum(Si, si, s, e);
+        Si = s;
+        Ci = __fadd_rn(Ci, __fadd_rn(ci, e));
+      }
+    }
+    float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (sub) z = static_cast<const float4*>(zv)[idx];
+    const float2 yr = ens_epi(Sr, Cr, alpha_f, sub, z.x, z.y);
+    const float2 yi = ens_epi(Si, Ci, alpha_f, sub, z.z, z.w);
+    yff = make_float4(yr.x, yr.y, yi.x, yi.y);
+    static_cast<float4*>(yv)[idx] = yff;
+    xff = x[idx];
+  }
+}
+
+__device__ __forceinline__ void ffdacc(float& S, float& C, float ah, float al, float bh, float bl) {
+  ff::dacc(S, C, ah, al, bh, bl);
+}
+
+// Persistent ensemble kernel: LPR lanes per row, one column per lane (NR <= 32).
+template <bool FF, bool REALH, int LPR>
+__global__ void __launch_bounds__(kEnsThreads) k_ensemble(EnsParams p) {
+  constexpr int GROUPS = kEnsThreads / LPR;
+  __shared__ int s_q;
+  __shared__ double2 red[kEnsWarps][2][32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = tid / LPR, cc = tid % LPR;
+  const bool active_col = cc < p.NR;
+  for (;;) {
+    if (tid == 0) s_q = (int)atomicAdd(p.next, 1u);
+    __syncthreads();
+    const int q = s_q;
+    __syncthreads();
+    if (q >= p.nseg) break;
+    const int seg = p.order[q];
+    const int64_t r0 = p.seg[seg], r1 = p.seg[seg + 1];
+    void* sl[2] = {p.slot0, p.slot1};
+    double2* mu = p.mu + (size_t)seg * p.NC * p.NR;
+    double2 mu0 = make_double2(0.0, 0.0), mu1 = make_double2(0.0, 0.0);
+    int ip = 1, ipp = 0;
+    for (int64_t n = 1; n <= p.NC / 2; ++n) {
+      const bool first = n == 1;
+      const void* x = first ? sl[0] : sl[ip];
+      void* y = first ? sl[1] : sl[ipp];
+      const double alpha = first ? 1.0 : 2.0;
+      double2 d0 = make_double2(0.0, 0.0), d1 = make_double2(0.0, 0.0);
+      float S[3] = {0.f, 0.f, 0.f}, C[3] = {0.f, 0.f, 0.f};
+      for (int64_t r = r0 + g; r < r1; r += GROUPS) {
+        if (!active_col) continue;
+        double2 xo, yo;
+        float4 xf, yf;
+        row_value<FF, REALH, 8>(p, x, r, cc, (float)alpha, alpha, !first, y, y, xo, yo, xf, yf);
+        if constexpr (!FF) {
+          d0.x = fma(xo.x, xo.x, d0.x);
+          d0.x = fma(xo.y, xo.y, d0.x);
+          d1.x = fma(xo.x, yo.x, d1.x);
+          d1.x = fma(xo.y, yo.y, d1.x);
+          d1.y = fma(xo.x, yo.y, d1.y);
+          d1.y = fma(-xo.y, yo.x, d1.y);
+        } else {
+          ffdacc(S[0], C[0], xf.x, xf.y, xf.x, xf.y);
+          ffdacc(S[0], C[0], xf.z, xf.w, xf.z, xf.w);
+          ffdacc(S[1], C[1], xf.x, xf.y, yf.x, yf.y);
+          ffdacc(S[1], C[1], xf.z, xf.w, yf.z, yf.w);
+          ffdacc(S[2], C[2], xf.x, xf.y, yf.z, yf.w);
+          ffdacc(S[2], C[2], -xf.z, -xf.w, yf.x, yf.y);
+        }
+      }
+      if constexpr (FF) {
+        d0.x = ff::join(S[0], C[0]);
+        d1.x = ff::join(S[1], C[1]);
+        d1.y = ff::join(S[2], C[2]);
+      }
+      // CTA reduction per column (fixed order)
+#pragma unroll
+      for (int off = LPR; off < 32; off <<= 1) {
+        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, off);
+        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, off);
+        d1.y += __shfl_xor_sync(0xffffffffu, d1.y, off);
+      }
+      if (lane < LPR) {
+        red[warp][0][lane] = d0;
+        red[warp][1][lane] = d1;
+      }
+      __syncthreads();
+      if (tid < p.NR) {
+        double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
+        for (int w = 0; w < kEnsWarps; ++w) {
+          a.x += red[w][0][tid].x;
+          b.x += red[w][1][tid].x;
+          b.y += red[w][1][tid].y;
+        }
+        const double f = p.scale ? p.scale[tid] : 1.0;
+        a.x *= f;
+        b.x *= f;
+        b.y *= f;
+        if (first) {
+          mu[tid] = a;
+          mu[p.NR + tid] = b;
+        } else {
+          const double2 m0 = mu[tid], m1 = mu[p.NR + tid];
+          double2 o0 = make_double2(2.0 * a.x - m0.x, 2.0 * a.y - m0.y);
+          double2 o1 = make_double2(2.0 * b.x - m1.x, 2.0 * b.y - m1.y);
+          mu[(2 * n - 2) * p.NR + tid] = o0;
+          mu[(2 * n - 1) * p.NR + tid] = o1;
+          if (!isfinite(o0.x) || !isfinite(o1.x) || !isfinite(o1.y))
+            atomicOr(p.status, (unsigned)STATUS_NONFINITE);
+        }
+      }
+      __syncthreads();  // y complete and red free before the next step
+      if (!first) {
+        const int t = ip;
+        ip = ipp;
+        ipp = t;
+      }
+      (void)mu0;
+      (void)mu1;
+    }
+  }
+}
+
+template <bool FF, bool REALH>
+using EnsFn = void (*)(EnsParams);
+
+void* pick_ensemble(bool ff, bool real, int NR) {
+  const int lpr = NR <= 1 ? 1 : NR <= 2 ? 2 : NR <= 4 ? 4 : NR <= 8 ? 8 : NR <= 16 ? 16 : 32;
+#define KPMGB_ENS(FFV, RV)                                           \
+  switch (lpr) {                                                     \
+    case 1: return (void*)k_ensemble<FFV, RV, 1>;                    \
+    case 2: return (void*)k_ensemble<FFV, RV, 2>;                    \
+    case 4: return (void*)k_ensemble<FFV, RV, 4>;                    \
+    case 8: return (void*)k_ensemble<FFV, RV, 8>;                    \
+    case 16: return (void*)k_ensemble<FFV, RV, 16>;                  \
+    default: return (void*)k_ensemble<FFV, RV, 32>;                  \
+  }
+  if (ff) {
+    if (real) { KPMGB_ENS(true, true) } else { KPMGB_ENS(true, false) }
+  } else {
+    if (real) { KPMGB_ENS(false, true) } else { KPMGB_ENS(false, false) }
+  }
+#undef KPMGB_ENS
+  return nullptr;
+}
+
+}  // namespace
+
+int launch_ensemble(const DeviceCSR& H, const int64_t* d_seg, const int* d_order, int nseg, int NR,
+                    int64_t NC, void* slot0, void* slot1, double2* mu, const double* scale,
+                    unsigned* next, unsigned* status, int precision, cudaStream_t s) {
+  if (NR < 1 || NR > 32) return fail(KPMGB_ERR_ARGUMENT, "the ensemble kernel supports 1 <= NR <= 32");
+  const bool ff = precision == KPMGB_PREC_FF;
+  EnsParams p;
+  p.rowptr = H.rowptr;
+  p.col = H.col;
+  p.val = ff ? H.val_ff : (H.is_real ? (const void*)H.val_real : (const void*)H.val);
+  p.seg = d_seg;
+  p.order = d_order;
+  p.nseg = nseg;
+  p.NR = NR;
+  p.NC = NC;
+  p.slot0 = slot0;
+  p.slot1 = slot1;
+  p.mu = mu;
+  p.scale = scale;
+  p.next = next;
+  p.status = status;
+  void* fn = pick_ensemble(ff, H.is_real != 0, NR);
+  int per_sm = 1, dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kEnsThreads, 0);
+  const int grid = std::max(1, std::min(nseg, std::max(per_sm, 1) * sms));
+  void* args[] = {&p};
+  KPMGB_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(kEnsThreads), args, 0, s));
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+}  // namespace kpmgb

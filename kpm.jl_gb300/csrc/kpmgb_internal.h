@@ -72,12 +72,16 @@ struct DeviceCSR {
   void* val_ff = nullptr;
   int is_real = 0;
   int max_row_nnz = 0;
+  double rmax = 0.0;  // max over rows of sum_k (|Re H_rk| + |Im H_rk|)
+  int* perm = nullptr;  // CSR position -> position in the caller's CSC arrays
 };
 
 // Device status words written by kernels (read back by the host at sync).
 enum StatusBits : unsigned {
   STATUS_NONFINITE = 1u,
   STATUS_GROWTH = 2u,
+  STATUS_TIMEOUT = 4u,
+  STATUS_SCRATCH = 8u,
 };
 
 struct Workspace {
@@ -138,6 +142,16 @@ struct StepArgs {
   double growth_limit = 0.0; // >0: flag if <x|x> > growth_limit * mu[0] (doubling)
   unsigned* sync = nullptr;  // ticket counter + status word
   void* partials = nullptr;
+  size_t partials_bytes = 0;  // 0: capacity not checked
+  int variant = 0;           // 0 auto, 1 register-gather kernel, 2 TMA-fed kernel,
+                             // 3 maxima-anchored kernel
+  // per-column maxima (float-float moment steps): when xmax is set the
+  // maxima-anchored kernel is used and writes the maxima of y
+  const float* xmax = nullptr;
+  const float* zmax = nullptr;
+  const float* bmax = nullptr;
+  float* ymax_out = nullptr;
+  float* ymax_clear = nullptr;
 };
 
 // precision: KPMGB_PREC_FP64 or KPMGB_PREC_FF.  Returns KPMGB_OK or an error.
@@ -154,6 +168,10 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
 int launch_load_block(const void* psi_colmajor, void* slot, int64_t NH, int NR,
                       int precision, double* col_scale, bool uniform,
                       cudaStream_t s);
+
+// Per-column max |hi| of a row-major float-float block, atomically merged into
+// out[0..NR) (out must be zeroed first).
+int launch_colmax(const void* slot, int64_t NH, int NR, float* out, cudaStream_t s);
 
 // Moment-scale helpers for the float-float path.
 int launch_scale_product(const double* sa, const double* sb, double* out, int NR,
@@ -179,6 +197,7 @@ struct ContractArgs {
   int parity = KPMGB_PARITY_NONE;
   int nmax_row = 0;       // only rows n < nmax_row are written (mn_sym)
   double2* mu = nullptr;  // device NC x NC column-major, accumulated into
+  unsigned* status = nullptr;  // device status word (bounded-wait expiry)
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
 };

@@ -27,6 +27,7 @@
 #include <unordered_map>
 
 #include "kpmgb_step.cuh"
+#include "kpmgb_step_tma.cuh"
 
 namespace kpmgb {
 namespace {
@@ -96,6 +97,19 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
       const int G = grid_for(fn, NH, s.lpr);
       worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
     }
+    if (precision == KPMGB_PREC_FF) {
+      for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
+        KernelFn fn = select_kernel_ffg(s, dot, H.is_real != 0);
+        const int G = grid_for(fn, NH, s.lpr);
+        worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
+      }
+    }
+    // the TMA-fed kernel launches min(SMs, ceil(NH / consumer warps)) blocks
+    // with at least 4 consumer warps per block
+    if (precision == KPMGB_PREC_FF && ncols >= 32) {
+      const int64_t G = std::max<int64_t>(1, std::min<int64_t>(num_sms(), (NH + 3) / 4));
+      worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
+    }
   }
   return worst;
 }
@@ -134,6 +148,45 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     p.growth_limit = a.growth_limit;
     p.sync = a.sync;
     p.partials = static_cast<double2*>(a.partials);
+    p.partials_cap = (int64_t)(a.partials_bytes / sizeof(double2));
+    p.xmax = a.xmax;
+    p.zmax = a.zmax;
+    p.bmax = a.bmax;
+    p.ymax_out = a.ymax_out;
+    p.ymax_clear = a.ymax_clear;
+    p.rmax = (float)(H.rmax * (1.0 + 1e-6));
+    p.anchor_slack = (float)((2.0 * H.max_row_nnz + 4.0) * 0x1p-22 + 0x1p-20);
+    if (precision == KPMGB_PREC_FF && a.xmax && a.dot != DOT_NONE && a.variant == 3) {
+      const Shape sh = pick_shape(p.ncols);
+      KernelFn fn = select_kernel_ffg(sh, a.dot, H.is_real != 0);
+      const int G = grid_for(fn, a.NH, sh.lpr);
+      fn<<<G, kThreads, 0, s>>>(p);
+      KPMGB_LAUNCHED();
+      continue;
+    }
+    // The TMA-fed kernel serves float-float steps with at least one warp of
+    // columns and at most 16 nonzeros per row; variant 1 forces the
+    // register-gather kernel, variant 2 requires the TMA-fed one.
+    const bool tma_ok = precision == KPMGB_PREC_FF && p.ncols >= 32 &&
+                        tma_chmax(H.max_row_nnz) > 0;
+    if (a.variant == 2 && !tma_ok)
+      return fail(KPMGB_ERR_ARGUMENT, "the TMA-fed kernel needs float-float precision, NR >= 32 "
+                                      "and at most 16 nonzeros per row");
+    // Automatic selection keeps the register-gather kernel: measured on GB300
+    // it sustains ~1.8x the TMA-fed kernel's bandwidth on the 3D Anderson
+    // workload (the producer's dependent CSR loads limit the latter).
+    if (tma_ok && a.variant == 2) {
+      const TmaGeom g = select_kernel_ff_tma(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz);
+      if (!g.fn)
+        return fail(KPMGB_ERR_ARGUMENT,
+                    "the TMA-fed kernel's shared-memory stages do not fit for this NR and row length");
+      const int ncw = g.threads / 32 - 1;
+      const int G = (int)std::max<int64_t>(
+          1, std::min<int64_t>(num_sms(), (a.NH + ncw - 1) / ncw));
+      g.fn<<<G, g.threads, g.smem, s>>>(p);
+      KPMGB_LAUNCHED();
+      continue;
+    }
     const Shape sh = pick_shape(p.ncols);
     KernelFn fn = select_kernel(sh, precision, a.dot, H.is_real != 0);
     const int G = grid_for(fn, a.NH, sh.lpr);
@@ -217,6 +270,15 @@ __global__ void k_uniform_scale(double* s, int n) {
   s[n] = m;
 }
 
+__global__ void k_colmax(const float4* __restrict__ v, int64_t n, int NR, float* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float4 e = v[i];
+    const float m = fmaxf(fabsf(e.x), fabsf(e.z));
+    if (m > 0.f) atomicMax(reinterpret_cast<unsigned*>(out) + (i % NR), __float_as_uint(m));
+  }
+}
+
 __global__ void k_scale_product(const double* a, const double* b, double* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = a[i] * b[i];
@@ -248,6 +310,14 @@ int launch_load_block(const void* psi, void* slot, int64_t NH, int NR, int preci
   else
     k_transpose_in<false><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
                                                nullptr);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+int launch_colmax(const void* slot, int64_t NH, int NR, float* out, cudaStream_t s) {
+  const int64_t n = NH * NR;
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4 * 1024);
+  k_colmax<<<std::max(blocks, 1), 256, 0, s>>>(static_cast<const float4*>(slot), n, NR, out);
   KPMGB_LAUNCHED();
   return KPMGB_OK;
 }

@@ -48,6 +48,15 @@ struct KParams {
   double growth_limit;
   unsigned* sync;
   double2* partials;
+  int64_t partials_cap;  // capacity in double2 elements (0: unchecked)
+  // maxima-anchored float-float kernel (k_step_ffg)
+  const float* xmax;     // per-column max |hi| of x, z and the bra
+  const float* zmax;
+  const float* bmax;
+  float* ymax_out;       // per-column max |hi| of y (atomicMax, pre-zeroed)
+  float* ymax_clear;     // maxima array zeroed by block 0 for the next step
+  float rmax;            // max over rows of sum |H_rk| (re + im)
+  float anchor_slack;    // relative slack of the H x anchor bound
 };
 
 template <int DOT>
@@ -57,13 +66,16 @@ struct NDots {
 
 // ------------------------------------------------------------------ reduction
 // Sum per-lane dot accumulators over the grid and write the moments.
-template <int ND, int LPR, int CPL>
+// NW warps per block (all of them reach this point; warps that own no rows
+// pass zero accumulators).
+template <int ND, int LPR, int CPL, int NW = kWarps>
 __device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CPL],
                                                 const KParams& p) {
+  constexpr int THREADS = NW * 32;
   if constexpr (ND == 0) {
     return;
   } else {
-    __shared__ double2 red[kWarps][ND][LPR * CPL];
+    __shared__ double2 red[NW][ND][LPR * CPL];
     __shared__ unsigned s_ticket;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -85,11 +97,16 @@ __device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CP
     }
     __syncthreads();
     const int NE = ND * p.ncols;
-    for (int e = threadIdx.x; e < NE; e += kThreads) {
+    // the partial sums of every block must fit the scratch buffer
+    if (p.partials_cap > 0 && (int64_t)gridDim.x * NE > p.partials_cap) {
+      if (threadIdx.x == 0 && blockIdx.x == 0) atomicOr(&p.sync[1], (unsigned)STATUS_SCRATCH);
+      return;
+    }
+    for (int e = threadIdx.x; e < NE; e += THREADS) {
       const int k = e / p.ncols, c = e - k * p.ncols;
       double2 s = make_double2(0.0, 0.0);
 #pragma unroll
-      for (int w = 0; w < kWarps; ++w) {
+      for (int w = 0; w < NW; ++w) {
         s.x += red[w][k][c].x;
         s.y += red[w][k][c].y;
       }
@@ -103,12 +120,12 @@ __device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CP
     __threadfence();
     // Last block: fixed-order sum over blocks.  Threads split the blocks into
     // P interleaved parts, then the parts are added in order.
-    double2* tmp = &red[0][0][0];  // reuse (capacity kWarps*ND*LPR*CPL >= 256? see below)
-    const int P = max(1, min(kThreads / NE, (int)(sizeof(red) / sizeof(double2)) / NE));
-    const int e = threadIdx.x % NE;
-    const int part = threadIdx.x / NE;
+    // reuse `red` (NW*ND*LPR*CPL entries) for the P x NE part sums
+    double2* tmp = &red[0][0][0];
+    const int P = max(1, min(THREADS / NE, (int)(sizeof(red) / sizeof(double2)) / NE));
     __syncthreads();
-    if (part < P) {
+    for (int idx = threadIdx.x; idx < P * NE; idx += THREADS) {
+      const int part = idx / NE, e = idx - part * NE;
       double2 s = make_double2(0.0, 0.0);
       for (int b = part; b < (int)gridDim.x; b += P) {
         const double2 v = __ldcg(p.partials + (size_t)b * NE + e);
@@ -118,7 +135,7 @@ __device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CP
       tmp[part * NE + e] = s;
     }
     __syncthreads();
-    for (int ee = threadIdx.x; ee < NE; ee += kThreads) {
+    for (int ee = threadIdx.x; ee < NE; ee += THREADS) {
       double2 s = make_double2(0.0, 0.0);
       for (int q = 0; q < P; ++q) {
         s.x += tmp[q * NE + ee].x;
@@ -495,6 +512,10 @@ KernelFn select_kernel_impl(Shape s, int dot, bool real) {
 
 KernelFn select_kernel_f64(Shape s, int dot, bool real);
 KernelFn select_kernel_ff(Shape s, int dot, bool real);
+KernelFn select_kernel_ffg(Shape s, int dot, bool real);
+
+struct TmaGeom;
+int tma_chmax(int max_row_nnz);
 
 }  // namespace step
 }  // namespace kpmgb

@@ -31,7 +31,7 @@ struct Kpm1dOptions
     precision::Int32
     stability_check::Int32
     use_graph::Int32
-    reserved::Int32
+    kernel_variant::Int32
 end
 
 struct Kpm2dOptions

@@ -8,7 +8,7 @@ from ._native import (KPMArgumentError, KPMDeviceError, KPMLibraryError, KPMNume
                       kernel_launch_count, version)
 from .frontend import (ConductivityMoments, DosMoments, RescaledHamiltonian, cond_moments,
                        dos_moments, normalizeH, on_device, random_phase_vectors, rescale)
-from .moment import (kpm_1d, kpm_1d_bang, kpm_1d_device, kpm_2d, kpm_2d_bang, kpm_2d_blocking,
+from .moment import (kpm_1d, kpm_1d_bang, kpm_1d_device, kpm_1d_ensemble, kpm_2d, kpm_2d_bang, kpm_2d_blocking,
                      kpm_2d_device, normalize_by_col, sync)
 from .operator import GB300Operator, as_operator
 
@@ -16,7 +16,7 @@ __all__ = [
     "KPMArgumentError", "KPMDeviceError", "KPMLibraryError", "KPMNumericalError",
     "kernel_launch_count", "version", "ConductivityMoments", "DosMoments",
     "RescaledHamiltonian", "cond_moments", "dos_moments", "normalizeH", "on_device",
-    "random_phase_vectors", "rescale", "kpm_1d", "kpm_1d_bang", "kpm_1d_device", "kpm_2d",
+    "random_phase_vectors", "rescale", "kpm_1d", "kpm_1d_bang", "kpm_1d_device", "kpm_1d_ensemble", "kpm_2d",
     "kpm_2d_bang", "kpm_2d_blocking", "kpm_2d_device", "normalize_by_col", "sync",
     "GB300Operator", "as_operator",
 ]

@@ -33,6 +33,8 @@ EXPORTED_SYMBOLS = (
     "kpmgb_operator_sync",
     "kpmgb_kernel_launch_count",
     "kpmgb_kpm1d_noalloc",
+    "kpmgb_kpm1d_ensemble",
+    "kpmgb_kpm1d_grad",
 )
 
 
@@ -54,7 +56,7 @@ class KPMDeviceError(RuntimeError):
 
 class Kpm1dOptions(C.Structure):
     _fields_ = [("precision", C.c_int32), ("stability_check", C.c_int32),
-                ("use_graph", C.c_int32), ("reserved", C.c_int32)]
+                ("use_graph", C.c_int32), ("kernel_variant", C.c_int32)]
 
 
 class Kpm2dOptions(C.Structure):
@@ -84,6 +86,8 @@ def _declare(lib):
     lib.kpmgb_kpm2d_device.argtypes = [vp, vp, vp, i64, i64, i64, vp, vp, vp,
                                        C.POINTER(Kpm2dOptions), vp]
     lib.kpmgb_operator_sync.argtypes = [vp, vp]
+    lib.kpmgb_kpm1d_ensemble.argtypes = [vp, i32, vp, i64, i64, vp, vp, C.POINTER(Kpm1dOptions)]
+    lib.kpmgb_kpm1d_grad.argtypes = [vp, i64, i64, i64, vp, vp, i64, vp]
     lib.kpmgb_kpm1d_noalloc.argtypes = [i64, vp, vp, vp, i64, i64, vp, vp, vp]
     for name in EXPORTED_SYMBOLS:
         if name not in ("kpmgb_version", "kpmgb_last_error", "kpmgb_kernel_launch_count"):

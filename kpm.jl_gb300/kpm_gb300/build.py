@@ -25,9 +25,13 @@ SOURCES = [
     "kpmgb_recurrence.cu",
     "kpmgb_step_f64.cu",
     "kpmgb_step_ff.cu",
+    "kpmgb_step_ff_tma.cu",
+    "kpmgb_step_ffg.cu",
     "kpmgb_contract.cu",
     "kpmgb_contract_tc.cu",
     "kpmgb_noalloc.cu",
+    "kpmgb_ensemble.cu",
+    "kpmgb_adjoint.cu",
 ]
 
 

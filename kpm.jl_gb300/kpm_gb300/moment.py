@@ -55,12 +55,18 @@ def _colmajor(psi, NH, NR, name):
     return np.asfortranarray(a, dtype=np.complex128)
 
 
-def _opts1d(precision, stability_check):
-    return _native.Kpm1dOptions(_prec(precision), 1 if stability_check else 0, 0, 0)
+_VARIANT = {"auto": 0, "gather": 1, "tma": 2, "anchored": 3}
+
+
+def _opts1d(precision, stability_check, kernel="auto"):
+    if kernel not in _VARIANT:
+        raise KPMArgumentError(f"kernel must be one of {sorted(_VARIANT)}")
+    return _native.Kpm1dOptions(_prec(precision), 1 if stability_check else 0, 0, _VARIANT[kernel])
 
 
 def kpm_1d_bang(H, NC: int, NR: int, NH: int, mu_all: np.ndarray, psi_in=None, psi_in_r=None,
-                *, precision: str = "fp64", stability_check: bool = False) -> None:
+                *, precision: str = "fp64", stability_check: bool = False,
+                kernel: str = "auto") -> None:
     """``kpm_1d!``: fill ``mu_all`` (NR, NC) in place.
 
     ``kpm_1d_bang(H, NC, NR, NH, mu_all, psi_in)`` is the doubling path
@@ -72,7 +78,7 @@ def kpm_1d_bang(H, NC: int, NR: int, NH: int, mu_all: np.ndarray, psi_in=None, p
     if mu_all.shape != (NR, NC):
         raise KPMArgumentError(f"mu_all has size {mu_all.shape}; expected ({NR}, {NC})")
     out = np.empty((NR, NC), dtype=np.complex128, order="F")
-    opts = _opts1d(precision, stability_check)
+    opts = _opts1d(precision, stability_check, kernel)
     if psi_in_r is None:
         if NC % 2 != 0:
             raise KPMArgumentError("Invalid NC: NC should be even.")
@@ -92,7 +98,7 @@ def kpm_1d_bang(H, NC: int, NR: int, NH: int, mu_all: np.ndarray, psi_in=None, p
 def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=None,
            psi_in_r=None, force_norm: bool = False, verbose: int = 0, avg_output: bool = True,
            NR_parallel: bool = True, rng=None, precision: str = "fp64",
-           stability_check: bool = False):
+           stability_check: bool = False, kernel: str = "auto"):
     """Stochastic-trace Chebyshev moments (``src/moment.jl:339-418``).
 
     Returns the real probe average (length NC) for equal bra/ket, the complex
@@ -126,10 +132,10 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
     if NR_parallel:
         if lr:
             kpm_1d_bang(op, NC, NR, NH, mu_all, psi_in_l, psi_in_r, precision=precision,
-                        stability_check=stability_check)
+                        stability_check=stability_check, kernel=kernel)
         else:
             kpm_1d_bang(op, NC, NR, NH, mu_all, psi_in, precision=precision,
-                        stability_check=stability_check)
+                        stability_check=stability_check, kernel=kernel)
     else:
         for i in range(NR):
             row = np.zeros((1, NC), dtype=np.complex128)
@@ -278,7 +284,8 @@ def _stream_ptr(stream):
 
 
 def kpm_1d_device(op: GB300Operator, NC: int, psi_t, mu_t, *, psi_l_t=None,
-                  precision="fp64", stability_check=False, stream=None) -> None:
+                  precision="fp64", stability_check=False, stream=None,
+                  kernel="auto") -> None:
     """Enqueue kpm_1d on torch CUDA tensors without host copies.
 
     ``psi_t``: complex128 tensor of shape (NR, NH) (row-contiguous, i.e. the
@@ -292,7 +299,7 @@ def kpm_1d_device(op: GB300Operator, NC: int, psi_t, mu_t, *, psi_l_t=None,
             raise KPMArgumentError(f"{name} tensor must be contiguous")
     if tuple(mu_t.shape) != (NC, NR):
         raise KPMArgumentError(f"mu tensor must have shape ({NC}, {NR})")
-    opts = _opts1d(precision, stability_check)
+    opts = _opts1d(precision, stability_check, kernel)
     if psi_l_t is None:
         rc = lib.kpmgb_kpm1d_device(op.handle, NC, NR, NH, C.c_void_p(psi_t.data_ptr()),
                                     C.c_void_p(mu_t.data_ptr()), C.byref(opts), _stream_ptr(stream))
@@ -322,3 +329,39 @@ def kpm_2d_device(H: GB300Operator, Ja: GB300Operator, Jb: GB300Operator, NC: in
 def sync(op: GB300Operator, stream=None) -> None:
     """Wait for enqueued work on ``op`` and raise deferred numerical failures."""
     _native.check(_native.load().kpmgb_operator_sync(op.handle, _stream_ptr(stream)))
+
+
+def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: bool = True):
+    """Doubling moments of many independent members in one persistent launch.
+
+    ``Hs``: list of (rescaled) sparse operators of any sizes; ``psis``: list of
+    probe blocks (NH_i, NR) with a common NR <= 32.  Equivalent to
+    ``[kpm_1d(H_i, NC, NR, psi_in=psi_i) for ...]`` (``src/moment.jl:339-492``
+    per member).  Returns a list of length-NC real averages, or of (NR, NC)
+    matrices with ``avg_output=False``.
+    """
+    import scipy.sparse as sp
+    if len(Hs) != len(psis) or not Hs:
+        raise KPMArgumentError("Hs and psis must be non-empty lists of equal length")
+    NR = int(np.asarray(psis[0]).shape[1])
+    sizes = [H.shape[0] for H in Hs]
+    for H, p in zip(Hs, psis):
+        if np.asarray(p).shape != (H.shape[0], NR):
+            raise KPMArgumentError("every probe block must be (NH_i, NR) with a common NR")
+    if NC % 2 != 0:
+        raise KPMArgumentError("Invalid NC: NC should be even.")
+    Hb = sp.block_diag([sp.csc_matrix(H, dtype=np.complex128) for H in Hs], format="csc")
+    op = GB300Operator(Hb)
+    seg = np.zeros(len(Hs) + 1, dtype=np.int64)
+    seg[1:] = np.cumsum(sizes)
+    psi = np.asfortranarray(np.vstack([np.asarray(p, dtype=np.complex128) for p in psis]))
+    out = np.empty((len(Hs), NC, NR), dtype=np.complex128)
+    opts = _opts1d(precision, False)
+    lib = _native.load()
+    rc = lib.kpmgb_kpm1d_ensemble(op.handle, len(Hs), seg.ctypes.data, NC, NR, psi.ctypes.data,
+                                  out.ctypes.data, C.byref(opts))
+    _native.check(rc)
+    res = [np.ascontiguousarray(out[i].T) for i in range(len(Hs))]
+    if avg_output:
+        return [m.sum(axis=0).real / NR for m in res]
+    return res

@@ -1,0 +1,51 @@
+"""Batched ensemble (one persistent launch for many realisations) against the
+per-member kpm_1d and the oracle."""
+import numpy as np
+import pytest
+
+from conftest import relerr
+import kpm_gb300 as kg
+from kpm_gb300 import models
+from oracle import kpm_oracle as ko
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"fp64": 1e-12, "ff": 1e-9}
+
+
+def _members(rng, count, lo, hi):
+    Hs, psis = [], []
+    for _ in range(count):
+        L = int(rng.integers(lo, hi + 1))
+        W = float(rng.uniform(1.0, 8.0))
+        H = models.square_anderson(L, W=W, rng=rng)
+        Hs.append((H / (4.0 + W / 2 + 0.1)).tocsc())   # Gershgorin bound keeps |E| < 1
+        psis.append(ko.random_phase_vectors(rng, L * L, 8))
+    return Hs, psis
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_ensemble_matches_oracle(built_lib, prec):
+    rng = np.random.default_rng(4)
+    Hs, psis = _members(rng, 12, 6, 20)
+    got = kg.kpm_1d_ensemble(Hs, 128, psis, precision=prec, avg_output=False)
+    for H, psi, m in zip(Hs, psis, got):
+        assert relerr(m, ko.kpm_1d_doubling(H, 128, psi)) < TOL[prec]
+
+
+def test_ensemble_matches_single_calls(built_lib):
+    rng = np.random.default_rng(8)
+    Hs, psis = _members(rng, 40, 8, 24)
+    got = kg.kpm_1d_ensemble(Hs, 64, psis, avg_output=False)
+    for H, psi, m in zip(Hs, psis, got):
+        ref = kg.kpm_1d(H, 64, 8, psi_in=psi, avg_output=False)
+        assert relerr(m, ref) < 1e-12
+
+
+def test_ensemble_validation(built_lib):
+    rng = np.random.default_rng(1)
+    Hs, psis = _members(rng, 2, 4, 5)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_ensemble(Hs, 63, psis)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_ensemble(Hs, 64, [psis[0], psis[1][:, :4]])

@@ -198,3 +198,65 @@ def test_typed_frontend_delegates():
     assert (m.a, m.b, m.NH, m.NR) == (h.a, h.b, NH, 4)
     full = kg.dos_moments(h, NC=128, psi_in=np.eye(NH, dtype=complex))
     assert abs(full.mu[0] - 1.0) < 1e-12
+
+
+@pytest.mark.parametrize("NR", [32, 40, 64, 96, 128, 160])
+@pytest.mark.parametrize("lr", [False, True])
+def test_tma_kernel_matches_oracle(NR, lr):
+    """The TMA-fed float-float kernel (NR >= 32, <= 16 nonzeros per row) on
+    real and complex operators, doubling and bra/ket paths."""
+    rng = np.random.default_rng(500 + NR)
+    # complex Haldane rows (10 nonzeros) for NR <= 64; 7-nonzero real rows above,
+    # where 16-nonzero complex stages would not fit in shared memory
+    H = models.cubic_anderson(8, W=4.0, rng=rng) if (NR % 64 == 0 or NR > 64) \
+        else models.haldane(12, 12)[0]
+    a, b, Hn = ko.normalizeH(H, center=True)
+    NH = Hn.shape[0]
+    pl = ko.random_phase_vectors(rng, NH, NR)
+    pr = ko.random_phase_vectors(rng, NH, NR)
+    if lr:
+        ref = ko.kpm_1d_lr(Hn, 65, pl, pr)
+        got = kg.kpm_1d(Hn, 65, NR, psi_in_l=pl, psi_in_r=pr, avg_output=False, precision="ff",
+                        kernel="tma")
+    else:
+        ref = ko.kpm_1d_doubling(Hn, 128, pr)
+        got = kg.kpm_1d(Hn, 128, NR, psi_in=pr, avg_output=False, precision="ff", kernel="tma")
+    assert relerr(got, ref) < TOL["ff"]
+
+
+def test_tma_and_gather_kernels_agree():
+    rng = np.random.default_rng(3)
+    H = models.cubic_anderson(16, W=16.5, rng=rng)
+    _, _, Hn = ko.normalizeH(H, center=True)
+    op = kg.GB300Operator(Hn)
+    psi = ko.random_phase_vectors(rng, Hn.shape[0], 64)
+    m_tma = kg.kpm_1d(op, 512, 64, psi_in=psi, avg_output=False, precision="ff", kernel="tma")
+    m_gat = kg.kpm_1d(op, 512, 64, psi_in=psi, avg_output=False, precision="ff", kernel="gather")
+    m_64 = kg.kpm_1d(op, 512, 64, psi_in=psi, avg_output=False, precision="fp64")
+    assert relerr(m_tma, m_64) < TOL["ff"]
+    assert relerr(m_gat, m_64) < TOL["ff"]
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(op, 16, 8, psi_in=psi[:, :8], precision="ff", kernel="tma")
+
+
+@pytest.mark.parametrize("NR", [1, 5, 12, 16, 33, 64, 100, 130])
+@pytest.mark.parametrize("lr", [False, True])
+def test_anchored_kernel_matches_oracle(NR, lr):
+    """The maxima-anchored float-float kernel (the default for float-float
+    moments) on real and complex operators, both moment paths."""
+    rng = np.random.default_rng(700 + NR)
+    H = models.cubic_anderson(8, W=10.0, rng=rng) if NR % 2 == 0 else models.haldane(10, 10)[0]
+    a, b, Hn = ko.normalizeH(H, center=True)
+    NH = Hn.shape[0]
+    pl = ko.random_phase_vectors(rng, NH, NR)
+    pr = ko.random_phase_vectors(rng, NH, NR) * np.geomspace(1e-3, 1e3, NR)
+    if lr:
+        ref = ko.kpm_1d_lr(Hn, 97, pl, pr)
+        got = kg.kpm_1d(Hn, 97, NR, psi_in_l=pl, psi_in_r=pr, avg_output=False, precision="ff",
+                        kernel="anchored")
+    else:
+        ref = ko.kpm_1d_doubling(Hn, 256, pr)
+        got = kg.kpm_1d(Hn, 256, NR, psi_in=pr, avg_output=False, precision="ff",
+                        kernel="anchored")
+    for i in range(NR):
+        assert relerr(got[i], ref[i]) < TOL["ff"]

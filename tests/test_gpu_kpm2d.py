@@ -108,3 +108,59 @@ def test_typed_cond_moments_delegates():
     ref = kg.kpm_2d(h.H, Jx, 0.7 * Jx, 32, 4, NH, psi_in=psi.copy())
     assert np.array_equal(m2.mu, ref)
     assert relerr(ref, ko.kpm_2d(h.H, Jx, 0.7 * Jx, 32, psi, psi, 32, 32)) < 1e-12
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+@pytest.mark.parametrize("NC", [17, 24, 160])
+def test_split_contraction_vs_dense(prec, NC):
+    """BF16-digit tensor-core contraction (tcgen05) against the dense reference."""
+    rng = np.random.default_rng(900 + NC)
+    H, Ja, Jb = blocking_model(rng, 6)
+    pl = ko.random_phase_vectors(rng, 36, 3)
+    pr = ko.random_phase_vectors(rng, 36, 3)
+    ref = ko.kpm2d_dense_reference(H, Ja, Jb, pl, pr, NC) if NC <= 24 else \
+        ko.kpm_2d(H, Ja, Jb, NC, pl, pr, NC, NC)
+    got = kg.kpm_2d(sp.csc_matrix(H), sp.csc_matrix(Ja), sp.csc_matrix(Jb), NC, 3, 36,
+                    psi_in_l=pl, psi_in_r=pr, precision=prec, contraction="split")
+    assert relerr(got, ref) < 1e-9
+
+
+@pytest.mark.parametrize("kw", [dict(arr_size=5, right_block=3), dict(moment_parity="ODD"),
+                                dict(mn_sym=True, arr_size=7, right_block=4)])
+def test_split_contraction_blocking_parity(kw):
+    rng = np.random.default_rng(803)
+    NC = 17
+    H, Ja, Jb = (sp.csc_matrix(M) for M in blocking_model(rng, 6))
+    psi = ko.random_phase_vectors(rng, 36, 3)
+    ref = kg.kpm_2d(H, Ja, Jb, NC, 3, 36, psi_in=psi, **kw)
+    got = kg.kpm_2d(H, Ja, Jb, NC, 3, 36, psi_in=psi, contraction="split", **kw)
+    assert relerr(got, ref) < 1e-9
+
+
+def test_split_contraction_haldane_hall():
+    """Quantized sigma_xy from tensor-core moments, and 1e-9 agreement with FP64."""
+    t2 = 0.2
+    H, Jx, Jy, area = models.haldane(6, 6, t=1.0, t2=t2)
+    D = H.shape[0]
+    a, b, Hn = ko.normalizeH(H, center=True)
+    psi = np.eye(D, dtype=complex)
+    ops = [kg.GB300Operator(M) for M in (Hn, Jx, Jy)]
+    m64 = kg.kpm_2d(*ops, 96, D, D, psi_in=psi)
+    msp = kg.kpm_2d(*ops, 96, D, D, psi_in=psi, precision="ff", contraction="split")
+    assert relerr(msp, m64) < 1e-9
+    s_kpm = ko.kubo_bastin_cond(msp, a, 0.0, b=b, NH=D, area=area)
+    s_ed = ed.ed_hall_conductivity_T0(H, Jx, Jy, area, 0.0)
+    assert abs(s_kpm - s_ed) < 0.03
+
+
+def test_split_contraction_large_k():
+    """K = NH*NR large enough for many exact 256-element chunks and K-splits."""
+    rng = np.random.default_rng(5)
+    H, Jx, Jy, _ = models.haldane(32, 32, t2=0.1)
+    a, b, Hn = ko.normalizeH(H, center=True)
+    NH = Hn.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, 16)
+    ops = [kg.GB300Operator(M) for M in (Hn, Jx, Jy)]
+    m64 = kg.kpm_2d(*ops, 64, 16, NH, psi_in=psi)
+    msp = kg.kpm_2d(*ops, 64, 16, NH, psi_in=psi, contraction="split")
+    assert relerr(msp, m64) < 1e-9
