@@ -167,15 +167,41 @@ int kpmgb_kpm1d_ensemble(kpmgb_operator H, int32_t nseg, const int64_t* seg,
                          int64_t NC, int64_t NR, const double* psi,
                          double* mu_all, const kpmgb_kpm1d_options* opts);
 
+/* Kubo-Bastin DC conductivity sigma(Ef) in e^2/h for nE Fermi energies
+ * (src/applications/conductivity.jl:101-157, kubo_bastin_cond, one Ef per
+ * call there).  mu2d: host, column-major complex (interleaved re/im) with
+ * leading dimension ld; the leading NC x NC block is used.  damping: NC
+ * kernel factors g_n (NULL = Jackson, src/kernels/jackson_kernel.jl:7-8);
+ * h_n is applied here.  beta = INFINITY selects the T = 0 step with weight
+ * 1/2 at Ef (src/utils/physics.jl:15-39).  quad_N Gauss-Chebyshev nodes,
+ * nodes with |x| >= 1 - edge_cutoff dropped, as in the reference.  The
+ * Ef-independent node sums run once on the device (two FP64 GEMMs with a
+ * fused epilogue), then one reduction per Ef.  Argument errors mirror the
+ * reference's ArgumentErrors.  Blocking call on the current device. */
+int kpmgb_kubo_bastin(const double* mu2d, int64_t ld, int64_t NC, double a,
+                      double b, const double* Ef, int64_t nE, int64_t NH,
+                      double area, double beta, const double* damping,
+                      int64_t quad_N, double edge_cutoff, double* sigma);
+
+/* DOS reconstruction rho(E_e) = sum_n h_n g_n mu_n T_n(x_e) / (a pi
+ * sqrt(1 - x_e^2)), x_e = (E_e - b)/a, zero outside |E_e - b| < a
+ * (src/applications/dos.jl:76-161 with dE_order = 0).  mu: NC real moments;
+ * damping: NC kernel factors (NULL = Jackson).  Blocking call. */
+int kpmgb_dos(const double* mu, int64_t NC, double a, double b,
+              const double* damping, const double* E, int64_t nE, double* rho);
+
 /* Gradient of L = sum_m g[m] mu_m with respect to every stored entry of a
  * Hermitian H, where mu are the probe-averaged doubling kpm_1d moments of
  * kpmgb_kpm1d (src/moment.jl:420-492) and g[0..NC) are real weights dL/dmu
  * supplied by the caller (e.g. from a DOS-window loss).  An adjoint
  * Chebyshev recurrence runs backward over checkpoints stored every
- * `checkpoint_every` steps (<= 0: 64) and an SDDMM accumulates the gradient
+ * `checkpoint_every` steps and an SDDMM accumulates the gradient
  * on the sparsity pattern.  grad: host array of nnz complex values in the
  * order of the CSC arrays given to kpmgb_operator_create, entry k holding
  * dL/dRe(H_k) + i dL/dIm(H_k) (H_ij and H_ji are independent entries).
+ * checkpoint_every <= 0 picks the spacing: every vector stays resident
+ * (a single forward pass) when that fits in half of the free device memory,
+ * else the spacing shrinks towards sqrt(NC/2).
  * FP64, 1 <= NR <= 32, NC even >= 4.  No reference counterpart (the
  * reference differentiates through ForwardDiff duals).  Blocking call. */
 int kpmgb_kpm1d_grad(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,

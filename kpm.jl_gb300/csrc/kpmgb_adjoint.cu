@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "kpmgb_internal.h"
@@ -159,8 +160,22 @@ int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, in
                    const double2* psi_rowmajor, const double* g, int64_t C, double2* d_grad_csr,
                    double2* d_grad_csc, DevBuf& work, cudaStream_t s) {
   const int64_t N = NC / 2;
-  if (C < 1) C = 1;
   const size_t blk = (size_t)NH * NR * sizeof(double2);
+  auto need_for = [&](int64_t c) { return (2 * ((N + c - 1) / c) + (c + 2) + 3) * blk; };
+  if (C < 1) {
+    // automatic: keep every vector of the recurrence resident when half of the
+    // free device memory holds them (one forward pass), else the largest
+    // spacing that fits (sqrt(N) minimises the footprint)
+    size_t free_b = 0, total_b = 0;
+    KPMGB_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = free_b / 2 + work.bytes;
+    C = N;
+    while (C > 1 && need_for(C) > budget) {
+      const int64_t r = (int64_t)std::ceil(std::sqrt((double)N));
+      C = C > 2 * r ? C / 2 : (C > r ? r : C - 1);
+    }
+  }
+  C = std::min<int64_t>(C, N);
   const int64_t nseg = (N + C - 1) / C;
   // layout: [checkpoint pairs (v_sC, v_sC+1): 2*nseg blocks][segment: C+2][lambda ring: 3]
   const size_t need = (2 * nseg + (C + 2) + 3) * blk;
@@ -179,15 +194,20 @@ int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, in
   double2* b = seg(1);
   KPMGB_CUDA(cudaMemcpyAsync(a, ck(0, 0), blk, cudaMemcpyDeviceToDevice, s));
   KPMGB_CUDA(cudaMemcpyAsync(b, ck(0, 1), blk, cudaMemcpyDeviceToDevice, s));
-  for (int64_t k = 1; k + 1 <= N; ++k) {
+  // with a = v_{kn-1}, b = v_kn: store the pair (v_kn, v_kn+1) when kn starts a segment
+  auto checkpoint = [&](int64_t kn) -> int {
+    if (kn % C != 0 || kn / C >= nseg) return KPMGB_OK;
+    const int64_t i = kn / C;
+    KPMGB_CUDA(cudaMemcpyAsync(ck(i, 0), b, blk, cudaMemcpyDeviceToDevice, s));
+    return adjoint_forward_step(H, NH, NR, b, a, ck(i, 1), 2.0, -1.0, s);
+  };
+  // the forward pass only has to reach the start of the last segment; each
+  // segment recomputes its own vectors from its checkpoint pair
+  KPMGB_TRY(checkpoint(1));
+  for (int64_t k = 1; k + 1 <= (nseg - 1) * C; ++k) {
     KPMGB_TRY(adjoint_forward_step(H, NH, NR, b, a, a, 2.0, -1.0, s));  // a := v_{k+1}
     std::swap(a, b);                                                    // a = v_k, b = v_{k+1}
-    const int64_t kn = k + 1;
-    if (kn % C == 0 && kn / C < nseg) {
-      const int64_t i = kn / C;
-      KPMGB_CUDA(cudaMemcpyAsync(ck(i, 0), b, blk, cudaMemcpyDeviceToDevice, s));
-      KPMGB_TRY(adjoint_forward_step(H, NH, NR, b, a, ck(i, 1), 2.0, -1.0, s));
-    }
+    KPMGB_TRY(checkpoint(k + 1));
   }
   // ---- coefficients
   auto Gw = [&](int64_t m) { return (m >= 0 && m < NC) ? g[m] : 0.0; };

@@ -776,7 +776,7 @@ extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_
   double2* gcsc = gcsr + op->csr.nnz;
   KPMGB_TRY(run_kpm1d_grad(op->csr, op->csr.perm, NC, (int)NR, NH,
                            reinterpret_cast<const double2*>(in + blk), g,
-                           checkpoint_every > 0 ? checkpoint_every : 64, gcsr, gcsc, ws.split, s));
+                           checkpoint_every, gcsr, gcsc, ws.split, s));
   KPMGB_CUDA(cudaMemcpyAsync(grad, gcsc, (size_t)op->csr.nnz * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
 }

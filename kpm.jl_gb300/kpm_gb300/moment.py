@@ -365,3 +365,35 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     if avg_output:
         return [m.sum(axis=0).real / NR for m in res]
     return res
+
+
+def kpm_1d_grad(H, NC: int, psi_in, g, *, checkpoint_every: int = 0):
+    """Gradient of ``L = sum_m g[m] * kpm_1d(H, NC, NR, psi_in=psi_in)[m]``.
+
+    ``g`` holds the real weights dL/dmu_m (length NC), e.g. from
+    :func:`kpm_gb300.frontend.dos_basis` for a loss on the reconstructed DOS.
+    Runs the adjoint Chebyshev recurrence on the GPU (checkpoints every
+    ``checkpoint_every`` steps; 0 keeps every vector resident when half of the
+    free device memory holds them) and returns the gradient on H's sparsity
+    pattern: a CSC matrix whose stored value k is dL/dRe(H_k) + i dL/dIm(H_k)
+    (H_ij and H_ji are independent entries; for a Hermitian parameter t on
+    both, dL/dt sums the two).  No reference counterpart: KPM.jl obtains such
+    derivatives by ForwardDiff duals through ``src/moment.jl:420-492``.
+    """
+    import scipy.sparse as sp
+    op = as_operator(H)
+    NH = op.shape[0]
+    a = np.asarray(psi_in)
+    if a.ndim != 2 or a.shape[0] != NH:
+        raise KPMArgumentError(f"Invalid `psi_in` with size {a.shape}. Expecting ({NH}, NR)")
+    NR = a.shape[1]
+    psi = _colmajor(a, NH, NR, "psi_in")
+    gw = np.ascontiguousarray(g, dtype=np.float64)
+    if gw.shape != (int(NC),):
+        raise KPMArgumentError(f"g must have length NC={NC} (got {gw.shape})")
+    out = np.empty(op.nnz, dtype=np.complex128)
+    lib = _native.load()
+    rc = lib.kpmgb_kpm1d_grad(op.handle, int(NC), NR, NH, psi.ctypes.data, gw.ctypes.data,
+                              int(checkpoint_every), out.ctypes.data)
+    _native.check(rc)
+    return sp.csc_matrix((out, op.indices, op.indptr), shape=op.shape)

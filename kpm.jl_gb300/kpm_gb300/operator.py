@@ -36,6 +36,10 @@ class GB300Operator:
         self._h = h
         self._lib = lib
         self.shape = M.shape
+        # CSC pattern in the order the device operator was built from; the
+        # gradient entry point returns values in this order.
+        self.indptr = colptr
+        self.indices = rowval
         self.nnz = int(M.nnz)
         n, nnz, real = C.c_int64(), C.c_int64(), C.c_int32()
         _native.check(lib.kpmgb_operator_info(h, C.byref(n), C.byref(nnz), C.byref(real)))
