@@ -74,13 +74,21 @@ typedef struct kpmgb_kpm1d_options {
                               grows beyond 1.5x its seed norm
                               (chebyshev_iteration.jl:110-133).  A non-finite
                               moment is always reported as NUMERICAL.          */
-  int32_t use_graph;       /* 1: replay the recurrence as a CUDA graph        */
+  int32_t use_graph;       /* 1: capture the recurrence into a CUDA graph on
+                              the first call and replay it while sizes,
+                              options and device buffers repeat (host entry
+                              points, and device entry points on a created
+                              stream; ignored on the legacy default stream)  */
   int32_t kernel_variant;  /* 0: automatic; 1: register-gather step kernel;
                               2: TMA-fed step kernel (float-float, NR >= 32,
                               at most 16 nonzeros per row); 3: float-float
                               kernel with per-column maxima anchors instead
-                              of per-row chunk anchors.  Automatic selection
-                              is the register-gather kernel.                    */
+                              of per-row chunk anchors; 4: autotune — time
+                              the register-gather shapes (and the TMA-fed
+                              kernel where it applies) once per (NR,
+                              precision, path) on this operator and reuse the
+                              fastest.  Automatic selection (0) is the
+                              register-gather kernel with the default shape. */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {
@@ -166,6 +174,26 @@ int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
 int kpmgb_kpm1d_ensemble(kpmgb_operator H, int32_t nseg, const int64_t* seg,
                          int64_t NC, int64_t NR, const double* psi,
                          double* mu_all, const kpmgb_kpm1d_options* opts);
+
+/* kpm_1d_current!: mu_all[i, n] = <psi_i| J_a T_n(H) |psi_i>
+ * = <J_a^dagger psi_i | T_n(H) psi_i>, n = 0 .. NC-1, no doubling
+ * (src/moment.jl:656-714).  Jadj: an operator holding J_a^dagger (created
+ * from the conjugate transpose of J_a).  psi: column-major NH x NR complex;
+ * mu_all: column-major NR x NC complex.  opts as kpmgb_kpm1d.  Blocking. */
+int kpmgb_kpm1d_current(kpmgb_operator H, kpmgb_operator Jadj, int64_t NC,
+                        int64_t NR, int64_t NH, const double* psi,
+                        double* mu_all, const kpmgb_kpm1d_options* opts);
+
+/* chebyshev_action!: out[:, :, k] = sum_{n=1}^{NC} C[n, k] T_{n-1}(H) V
+ * (src/utils/chebyshev_action.jl:47-122), coefficients used verbatim (no h_n,
+ * no damping).  V: column-major NH x NR complex; C: column-major NC x K
+ * complex; out: column-major NH x NR x K complex (overwritten, must not alias
+ * V).  check_every > 0 runs the reference's growth guard every check_every
+ * iterations and at the last (KPMGB_ERR_NUMERICAL on growth > 1.5 of a seed
+ * column norm); 0 disables it.  FP64.  Blocking call. */
+int kpmgb_chebyshev_action(kpmgb_operator H, int64_t NH, int64_t NR,
+                           const double* V, int64_t NC, int64_t K,
+                           const double* C, int64_t check_every, double* out);
 
 /* Kubo-Bastin DC conductivity sigma(Ef) in e^2/h for nE Fermi energies
  * (src/applications/conductivity.jl:101-157, kubo_bastin_cond, one Ef per

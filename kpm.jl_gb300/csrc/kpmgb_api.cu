@@ -65,9 +65,17 @@ void DevBuf::release() {
   bytes = 0;
 }
 
+void GraphCache::release() {
+  if (exec) cudaGraphExecDestroy(exec);
+  exec = nullptr;
+  key.clear();
+  launches = 0;
+}
+
 Operator::~Operator() {
   cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
+  graph.release();
   DevBuf* bufs[] = {&ws.slots, &ws.bra,  &ws.partials, &ws.sync,  &ws.scales, &ws.mu,
                     &ws.psi_in, &ws.left, &ws.right,   &ws.ring,  &ws.gemm,   &ws.split};
   for (DevBuf* b : bufs) b->release();
@@ -190,6 +198,38 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
     KPMGB_TRY(launch_colmax(sl[0], NH, (int)NR, ring(0), s));
     if (lr) KPMGB_TRY(launch_colmax(ws.bra.ptr, NH, (int)NR, bmax, s));
   }
+  // kernel_variant 4: time the candidate kernels once per (NR, precision,
+  // path) on this operator with the first recurrence step, then reuse.
+  int chosen_variant = o ? o->kernel_variant : 0, chosen_shape = 0;
+  if (chosen_variant == 4) {
+    const std::string tkey = std::to_string(NR) + "/" + std::to_string(precision) + (lr ? "/lr" : "/d");
+    auto it = op->tuned.find(tkey);
+    if (it == op->tuned.end()) {
+      StepArgs t;
+      t.H = &op->csr;
+      t.NH = NH;
+      t.NR = (int)NR;
+      t.mu = mu;
+      t.mom_scale = mom_scale;
+      t.sync = ws.sync.as<unsigned>();
+      t.partials = ws.partials.ptr;
+      t.partials_bytes = ws.partials.bytes;
+      t.bra = lr ? ws.bra.ptr : nullptr;
+      t.x = sl[0];
+      t.y = sl[1];
+      t.dot = lr ? DOT_LR2 : DOT_DOUBLING;
+      t.mom = MOM_STORE;
+      int v = 1, sh = 0;
+      KPMGB_TRY(tune_step(t, precision, s, &v, &sh));
+      it = op->tuned.emplace(tkey, std::make_pair(v, sh)).first;
+    }
+    chosen_variant = it->second.first;
+    chosen_shape = it->second.second;
+  }
+  // The recurrence proper: NC/2 (doubling) or NC-1 (bra/ket) step launches.
+  // With use_graph on a non-legacy stream it is captured once into a CUDA
+  // graph and replayed while sizes, options and device pointers repeat.
+  auto recurrence = [&]() -> int {
   StepArgs a;
   a.H = &op->csr;
   a.NH = NH;
@@ -200,7 +240,8 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   a.partials = ws.partials.ptr;
   a.partials_bytes = ws.partials.bytes;
   a.bra = lr ? ws.bra.ptr : nullptr;
-  a.variant = o ? o->kernel_variant : 0;
+  a.variant = chosen_variant;
+  a.shape = chosen_shape;
   // alpha_1 = H alpha_0 with mu_0, mu_1 (src/moment.jl:440-449, :521-527)
   a.x = sl[0];
   a.z = nullptr;
@@ -260,6 +301,46 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       std::swap(ip, ipp);
     }
   }
+  return KPMGB_OK;
+  };
+  const bool graph = o && o->use_graph && s != nullptr && s != cudaStreamLegacy &&
+                     s != cudaStreamPerThread;
+  if (!graph) return recurrence();
+  std::string key;
+  auto put = [&](const void* v, size_t n) { key.append(static_cast<const char*>(v), n); };
+  const int64_t ints[] = {NC, NR, NH, precision, chosen_variant, chosen_shape, o->stability_check,
+                          lr ? 1 : 0, (int64_t)ws.partials.bytes};
+  const void* ptrs[] = {mu, ws.slots.ptr, ws.bra.ptr, ws.scales.ptr, ws.partials.ptr, ws.sync.ptr,
+                        op->csr.rowptr, op->csr.col, op->csr.val, op->csr.val_ff};
+  put(ints, sizeof ints);
+  put(ptrs, sizeof ptrs);
+  if (op->graph.exec && op->graph.key == key) {
+    KPMGB_CUDA(cudaGraphLaunch(op->graph.exec, s));
+    g_launches.fetch_add(op->graph.launches, std::memory_order_relaxed);
+    return KPMGB_OK;
+  }
+  op->graph.release();
+  KPMGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  const int64_t n0 = g_launches.load();
+  const int rc = recurrence();
+  const int64_t nl = g_launches.load() - n0;
+  cudaGraph_t gr = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+  if (rc != KPMGB_OK) {
+    if (gr) cudaGraphDestroy(gr);
+    return rc;
+  }
+  KPMGB_CUDA(ce);
+  cudaGraphExec_t ex = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&ex, gr, 0);
+  cudaGraphDestroy(gr);
+  KPMGB_CUDA(ie);
+  op->graph.exec = ex;
+  op->graph.key = key;
+  op->graph.launches = nl;
+  g_launches.fetch_sub(nl, std::memory_order_relaxed);  // captured, not yet run
+  KPMGB_CUDA(cudaGraphLaunch(ex, s));
+  g_launches.fetch_add(nl, std::memory_order_relaxed);
   return KPMGB_OK;
 }
 
@@ -778,5 +859,93 @@ extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_
                            reinterpret_cast<const double2*>(in + blk), g,
                            checkpoint_every, gcsr, gcsc, ws.split, s));
   KPMGB_CUDA(cudaMemcpyAsync(grad, gcsc, (size_t)op->csr.nnz * 16, cudaMemcpyDeviceToHost, s));
+  return check_status(op, s);
+}
+
+// ------------------------------------------------------- chebyshev_action
+namespace kpmgb {
+int run_chebyshev_action(Operator* op, int64_t NH, int64_t NR, const double2* V_dev, int64_t NC,
+                         int64_t K, const double2* Ct_dev, int64_t check_every, double2* out_dev,
+                         cudaStream_t s);
+}
+
+extern "C" int kpmgb_chebyshev_action(kpmgb_operator h, int64_t NH, int64_t NR, const double* V,
+                                      int64_t NC, int64_t K, const double* C,
+                                      int64_t check_every, double* out) {
+  clear_error();
+  if (!h || !V || !C || !out) return fail(KPMGB_ERR_ARGUMENT, "null argument");
+  if (NC < 1) return fail(KPMGB_ERR_ARGUMENT, "C must have at least one coefficient row");
+  if (NR < 1) return fail(KPMGB_ERR_ARGUMENT, "V must have at least one column");
+  if (K < 1) return fail(KPMGB_ERR_ARGUMENT, "C must have at least one coefficient column");
+  Operator* op = as_op(h);
+  if (NH != op->csr.n)
+    return fail(KPMGB_ERR_ARGUMENT, "size(Hn, 2) = %lld must equal size(V, 1) = %lld",
+                (long long)op->csr.n, (long long)NH);
+  if (check_every < 0) return fail(KPMGB_ERR_ARGUMENT, "check_every must be >= 0");
+  const size_t blk = (size_t)NH * NR * 16;
+  const char* vb = reinterpret_cast<const char*>(V);
+  const char* ob = reinterpret_cast<const char*>(out);
+  if (ob < vb + blk && vb < ob + K * blk) return fail(KPMGB_ERR_ARGUMENT, "out must not alias V");
+  Guard gd(op);
+  cudaStream_t s = op->stream;
+  Workspace& ws = op->ws;
+  // C (column-major NC x K) -> Ct [NC][K] on the host, then one copy
+  std::vector<double> ct((size_t)2 * NC * K);
+  for (int64_t k = 0; k < K; ++k)
+    for (int64_t n = 0; n < NC; ++n) {
+      ct[2 * (n * K + k)] = C[2 * (n + k * NC)];
+      ct[2 * (n * K + k) + 1] = C[2 * (n + k * NC) + 1];
+    }
+  KPMGB_TRY(ws.psi_in.ensure(blk));
+  KPMGB_TRY(ws.right.ensure((size_t)K * blk));
+  KPMGB_TRY(ws.gemm.ensure(std::max(ws.gemm.bytes, ct.size() * sizeof(double))));
+  KPMGB_TRY(ensure_sync(op, s));
+  KPMGB_CUDA(cudaMemcpyAsync(ws.psi_in.ptr, V, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_CUDA(cudaMemcpyAsync(ws.gemm.ptr, ct.data(), ct.size() * sizeof(double),
+                             cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(run_chebyshev_action(op, NH, NR, ws.psi_in.as<double2>(), NC, K,
+                                 ws.gemm.as<double2>(), check_every, ws.right.as<double2>(), s));
+  KPMGB_CUDA(cudaMemcpyAsync(out, ws.right.ptr, (size_t)K * blk, cudaMemcpyDeviceToHost, s));
+  return check_status(op, s);
+}
+
+// --------------------------------------------------------- kpm_1d_current
+extern "C" int kpmgb_kpm1d_current(kpmgb_operator h, kpmgb_operator jadj, int64_t NC, int64_t NR,
+                                   int64_t NH, const double* psi, double* mu_all,
+                                   const kpmgb_kpm1d_options* opts) {
+  clear_error();
+  if (!h || !jadj) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  if (!psi || !mu_all) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
+  if (NR < 1 || NH < 1) return fail(KPMGB_ERR_ARGUMENT, "invalid sizes");
+  if (NC < 2) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be at least 2.");
+  Operator* op = as_op(h);
+  Operator* jo = as_op(jadj);
+  if (NH != op->csr.n || NH != jo->csr.n)
+    return fail(KPMGB_ERR_ARGUMENT, "Invalid `psi_in` with size (%lld, %lld). Expecting %lld, %lld",
+                (long long)NH, (long long)NR, (long long)op->csr.n, (long long)NR);
+  if (jo->device != op->device)
+    return fail(KPMGB_ERR_ARGUMENT, "H and J must live on the same device");
+  Guard g(op);
+  cudaStream_t s = op->stream;
+  Workspace& ws = op->ws;
+  const size_t blk = (size_t)NH * NR * 16;
+  KPMGB_TRY(ws.psi_in.ensure(3 * blk));
+  KPMGB_TRY(ws.mu.ensure((size_t)NR * NC * 16));
+  char* in = ws.psi_in.as<char>();
+  // J^dagger psi (FP64, row-major) -> column-major bra
+  KPMGB_CUDA(cudaMemcpyAsync(in, psi, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(launch_load_block(in, in + blk, NH, (int)NR, KPMGB_PREC_FP64, nullptr, false, s));
+  StepArgs a;
+  a.H = &jo->csr;
+  a.NH = NH;
+  a.NR = (int)NR;
+  a.x = in + blk;
+  a.y = in + 2 * blk;
+  KPMGB_TRY(launch_step(a, KPMGB_PREC_FP64, s));
+  KPMGB_TRY(launch_rowmajor_to_colmajor(reinterpret_cast<const double2*>(in + 2 * blk),
+                                        reinterpret_cast<double2*>(in + blk), NH, (int)NR, 1, s));
+  // <J^dagger psi | T_n(H) psi>: the bra/ket recurrence, no doubling
+  KPMGB_TRY(run_kpm1d(op, NC, NR, NH, in + blk, in, ws.mu.as<double2>(), opts, s, true));
+  KPMGB_CUDA(cudaMemcpyAsync(mu_all, ws.mu.ptr, (size_t)NR * NC * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
 }

@@ -6,6 +6,7 @@
 #include <atomic>
 #include <cstddef>
 #include <cstdint>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -99,12 +100,24 @@ struct Workspace {
   DevBuf split;      // kpm_2d split-precision operand slices
 };
 
+// One instantiated CUDA graph of a kpm_1d recurrence, replayed while the
+// launch parameters (sizes, options and every device pointer) are unchanged.
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  std::string key;
+  int64_t launches = 0;  // kernel nodes per replay
+  void release();
+};
+
 struct Operator {
   DeviceCSR csr;
   int device = 0;
   cudaStream_t stream = nullptr;
   std::mutex mtx;
   Workspace ws;
+  GraphCache graph;
+  // autotuned (variant, shape) per (NR, precision, bra/ket) key
+  std::map<std::string, std::pair<int, int>> tuned;
   ~Operator();
 };
 
@@ -145,6 +158,8 @@ struct StepArgs {
   size_t partials_bytes = 0;  // 0: capacity not checked
   int variant = 0;           // 0 auto, 1 register-gather kernel, 2 TMA-fed kernel,
                              // 3 maxima-anchored kernel
+  int shape = 0;             // lanes-per-row * 10 + columns-per-lane of the
+                             // register-gather kernel; 0 = automatic
   // per-column maxima (float-float moment steps): when xmax is set the
   // maxima-anchored kernel is used and writes the maxima of y
   const float* xmax = nullptr;
@@ -156,6 +171,11 @@ struct StepArgs {
 
 // precision: KPMGB_PREC_FP64 or KPMGB_PREC_FF.  Returns KPMGB_OK or an error.
 int launch_step(const StepArgs& a, int precision, cudaStream_t s);
+// Autotuning: times every (variant, shape) candidate of the step `a` (which
+// must not write its own inputs: y aliasing neither x nor z) with CUDA events
+// on `s`, after one warm launch each, and returns the fastest in
+// *variant / *shape.  Synchronises `s`.
+int tune_step(const StepArgs& a, int precision, cudaStream_t s, int* variant, int* shape);
 // Bytes of partial-sum scratch that launch_step needs for this shape.
 size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision);
 
@@ -168,6 +188,10 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
 int launch_load_block(const void* psi_colmajor, void* slot, int64_t NH, int NR,
                       int precision, double* col_scale, bool uniform,
                       cudaStream_t s);
+
+// Row-major NH x NR FP64 blocks (K of them, consecutive) -> column-major.
+int launch_rowmajor_to_colmajor(const double2* in, double2* out, int64_t NH, int NR, int K,
+                                cudaStream_t s);
 
 // Per-column max |hi| of a row-major float-float block, atomically merged into
 // out[0..NR) (out must be zeroed first).

@@ -1,0 +1,338 @@
+// Reconstruction from Chebyshev moments on the device: the Kubo-Bastin DC
+// conductivity (src/applications/conductivity.jl:101-157) for a batch of
+// Fermi energies, and the DOS (src/applications/dos.jl:76-161).
+//
+// Kubo-Bastin.  With mu~[n,m] = mu[n,m] k_n k_m (k = damping * h_n,
+// src/kernels/kernels.jl:14-50), Gauss-Chebyshev nodes x_j = cos(theta_j)
+// with |x_j| < 1 - edge_cutoff, s_j = sqrt(1 - x_j^2):
+//   U[n,j] = sum_m mu~[m,n] T_m(x_j),   V[n,j] = sum_m mu~[n,m] T_m(x_j)
+//   S_j    = sum_n U[n,j] (x_j - i n s_j) e^{i n theta_j}
+//                + V[n,j] (x_j + i n s_j) e^{-i n theta_j}
+//   sigma(Ef) = -2 NH / (area a^2) * sum_j w_j f(a x_j + b; Ef) / s_j^3 Re S_j.
+// S_j does not depend on Ef, so one node pass (two FP64 GEMMs with the
+// epilogue fused) serves every Fermi energy; each Ef is then a dot product
+// over the nodes.  The reference evaluates the whole chain per Ef.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "kpmgb_internal.h"
+
+namespace kpmgb {
+namespace {
+
+constexpr int kTN = 32;   // moment rows n per block
+constexpr int kTJ = 64;   // quadrature nodes per block
+constexpr int kKC = 16;   // inner (m) chunk
+constexpr int kReconThreads = 256;
+
+// T[m * Q + j] = cos(m theta_j)
+__global__ void k_cheb_table(const double* theta, int64_t Q, int NC, double* T) {
+  const int64_t total = (int64_t)NC * Q;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = e / Q, j = e % Q;
+    T[e] = cos((double)m * theta[j]);
+  }
+}
+
+// partial[nb * Q + j] = sum over the block's rows n of U[n,j] WM[n,j] + V[n,j] WN[n,j]
+__global__ void __launch_bounds__(kReconThreads)
+k_kubo_nodes(const double2* __restrict__ mu, int NC, const double* __restrict__ kv,
+             const double* __restrict__ T, int64_t Q, const double* __restrict__ x,
+             const double* __restrict__ theta, const double* __restrict__ sn,
+             double2* __restrict__ partial) {
+  __shared__ double2 sU[kKC][kTN];      // mu~[m0+mm, n0+t]
+  __shared__ double2 sV[kKC][kTN];      // mu~[n0+t, m0+mm]
+  __shared__ double sT[kKC][kTJ];       // T[m0+mm, j0+jj]
+  __shared__ double2 red[kTN / 2][kTJ];
+  const int n0 = blockIdx.x * kTN;
+  const int64_t j0 = (int64_t)blockIdx.y * kTJ;
+  const int tid = threadIdx.x, tn = tid >> 4, tj = tid & 15;
+  double2 U[2][4], V[2][4];
+#pragma unroll
+  for (int r = 0; r < 2; ++r)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) U[r][q] = V[r][q] = make_double2(0.0, 0.0);
+
+  for (int m0 = 0; m0 < NC; m0 += kKC) {
+    for (int e = tid; e < kKC * kTN; e += kReconThreads) {
+      {  // column-major mu: mu[m + n NC]; consecutive e walk m
+        const int mm = e % kKC, t = e / kKC;
+        const int m = m0 + mm, n = n0 + t;
+        double2 v = make_double2(0.0, 0.0);
+        if (m < NC && n < NC) {
+          v = mu[(size_t)m + (size_t)n * NC];
+          const double k = kv[m] * kv[n];
+          v.x *= k;
+          v.y *= k;
+        }
+        sU[mm][t] = v;
+      }
+      {  // consecutive e walk n
+        const int t = e % kTN, mm = e / kTN;
+        const int m = m0 + mm, n = n0 + t;
+        double2 v = make_double2(0.0, 0.0);
+        if (m < NC && n < NC) {
+          v = mu[(size_t)n + (size_t)m * NC];
+          const double k = kv[m] * kv[n];
+          v.x *= k;
+          v.y *= k;
+        }
+        sV[mm][t] = v;
+      }
+    }
+    for (int e = tid; e < kKC * kTJ; e += kReconThreads) {
+      const int jj = e % kTJ, mm = e / kTJ;
+      const int m = m0 + mm;
+      const int64_t j = j0 + jj;
+      sT[mm][jj] = (m < NC && j < Q) ? T[(size_t)m * Q + j] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int mm = 0; mm < kKC; ++mm) {
+      double tv[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tv[q] = sT[mm][tj + 16 * q];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const double2 a = sU[mm][tn + 16 * r];
+        const double2 b = sV[mm][tn + 16 * r];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          U[r][q].x = fma(a.x, tv[q], U[r][q].x);
+          U[r][q].y = fma(a.y, tv[q], U[r][q].y);
+          V[r][q].x = fma(b.x, tv[q], V[r][q].x);
+          V[r][q].y = fma(b.y, tv[q], V[r][q].y);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // epilogue: weights WM = (x - i n s) e^{i n th}, WN = conj(WM)
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int64_t j = j0 + tj + 16 * q;
+    double2 c = make_double2(0.0, 0.0);
+    if (j < Q) {
+      const double xj = x[j], th = theta[j], sj = sn[j];
+#pragma unroll
+      for (int r = 0; r < 2; ++r) {
+        const int n = n0 + tn + 16 * r;
+        if (n < NC) {
+          double si, co;
+          sincos((double)n * th, &si, &co);
+          const double ns = (double)n * sj;
+          const double wr = xj * co + ns * si;
+          const double wi = xj * si - ns * co;
+          c.x += (U[r][q].x * wr - U[r][q].y * wi) + (V[r][q].x * wr + V[r][q].y * wi);
+          c.y += (U[r][q].x * wi + U[r][q].y * wr) + (V[r][q].y * wr - V[r][q].x * wi);
+        }
+      }
+    }
+    red[tn][tj + 16 * q] = c;
+  }
+  __syncthreads();
+  if (tid < kTJ) {
+    const int64_t j = j0 + tid;
+    double2 s = make_double2(0.0, 0.0);
+    for (int t = 0; t < kTN / 2; ++t) {
+      s.x += red[t][tid].x;
+      s.y += red[t][tid].y;
+    }
+    if (j < Q) partial[(size_t)blockIdx.x * Q + j] = s;
+  }
+}
+
+// sigma[e] = scale * sum_j w f(a x_j + b; Ef_e) / s_j^3 * Re(sum_nb partial[nb][j])
+__global__ void __launch_bounds__(kReconThreads)
+k_kubo_fermi(const double2* __restrict__ partial, int nb, int64_t Q, const double* __restrict__ x,
+             const double* __restrict__ sn, double w, double a, double b,
+             const double* __restrict__ Ef, double beta, double scale, double* __restrict__ sigma) {
+  __shared__ double red[kReconThreads];
+  const double ef = Ef[blockIdx.x];
+  double acc = 0.0;
+  for (int64_t j = threadIdx.x; j < Q; j += kReconThreads) {
+    const double E = a * x[j] + b;
+    double f;
+    if (isinf(beta)) {
+      f = ((E < ef ? 1.0 : 0.0) + (E <= ef ? 1.0 : 0.0)) / 2.0;
+    } else {
+      f = 1.0 / (exp((E - ef) * beta) + 1.0);
+    }
+    if (f == 0.0) continue;
+    double s = 0.0;
+    for (int k = 0; k < nb; ++k) s += partial[(size_t)k * Q + j].x;
+    const double s3 = sn[j] * sn[j] * sn[j];
+    acc += w * f / s3 * s;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = kReconThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sigma[blockIdx.x] = scale * red[0];
+}
+
+// rho[e] = sum_n c_n cos(n theta_e) / (a pi sin theta_e) inside |E - b| < a, else 0
+__global__ void k_dos(const double* __restrict__ c, int NC, double a, double b,
+                      const double* __restrict__ E, int64_t nE, double* __restrict__ rho) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nE;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double d = E[e] - b;
+    if (!(fabs(d) < a)) {
+      rho[e] = 0.0;
+      continue;
+    }
+    const double xe = d / a;
+    const double th = acos(xe);
+    double s = 0.0;
+    for (int n = 0; n < NC; ++n) s += c[n] * cos((double)n * th);
+    rho[e] = s / (a * M_PI * sqrt(1.0 - xe * xe));
+  }
+}
+
+// Jackson damping g_n (src/kernels/jackson_kernel.jl:7-8)
+void jackson(int64_t N, std::vector<double>& g) {
+  g.resize(N);
+  const double c = M_PI / (double)(N + 1);
+  for (int64_t n = 0; n < N; ++n)
+    g[n] = ((double)(N + 1 - n) * std::cos(c * n) + std::sin(c * n) / std::tan(c)) /
+           (double)(N + 1);
+}
+
+// Scratch device memory for one blocking call, freed on every exit path.
+struct CallScratch {
+  std::vector<void*> ptrs;
+  cudaStream_t s = nullptr;
+  ~CallScratch() {
+    if (s) cudaStreamSynchronize(s);
+    for (void* p : ptrs) cudaFree(p);
+    if (s) cudaStreamDestroy(s);
+  }
+  template <typename T>
+  int alloc(T** p, size_t count) {
+    void* q = nullptr;
+    KPMGB_CUDA(cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T)));
+    ptrs.push_back(q);
+    *p = static_cast<T*>(q);
+    return KPMGB_OK;
+  }
+};
+
+int grid1d(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8192)); }
+
+}  // namespace
+}  // namespace kpmgb
+
+using namespace kpmgb;
+
+extern "C" int kpmgb_kubo_bastin(const double* mu2d, int64_t ld, int64_t NC, double a, double b,
+                                 const double* Ef, int64_t nE, int64_t NH, double area,
+                                 double beta, const double* damping, int64_t quad_N,
+                                 double edge_cutoff, double* sigma) {
+  clear_error();
+  if (!mu2d || !Ef || !sigma) return fail(KPMGB_ERR_ARGUMENT, "null argument");
+  if (!(a > 0)) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: a must be positive.");
+  if (!(area > 0)) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: area must be positive.");
+  if (NH <= 0) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: NH must be positive.");
+  if (quad_N <= 0) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: quad_N must be positive.");
+  if (!(edge_cutoff >= 0 && edge_cutoff < 1))
+    return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: edge_cutoff must be in [0, 1).");
+  if (NC < 1 || ld < NC) return fail(KPMGB_ERR_ARGUMENT, "need 1 <= NC <= ld");
+  if (nE < 0) return fail(KPMGB_ERR_ARGUMENT, "nE must be >= 0");
+  if (nE == 0) return KPMGB_OK;
+  if (NC > (1 << 20)) return fail(KPMGB_ERR_ARGUMENT, "NC too large");
+  // Gauss-Chebyshev nodes cos((2k-1) pi / 2n), k = n..1, weight pi/n; keep |x| < 1 - cutoff
+  std::vector<double> xs, th, sn;
+  for (int64_t k = quad_N; k >= 1; --k) {
+    const double xk = std::cos((double)(2 * k - 1) * M_PI / (double)(2 * quad_N));
+    if (std::fabs(xk) < 1.0 - edge_cutoff) {
+      xs.push_back(xk);
+      th.push_back(std::acos(xk));
+      sn.push_back(std::sqrt(1.0 - xk * xk));
+    }
+  }
+  const int64_t Q = (int64_t)xs.size();
+  if (Q == 0) {
+    for (int64_t e = 0; e < nE; ++e) sigma[e] = 0.0;
+    return KPMGB_OK;
+  }
+  std::vector<double> kv;
+  if (damping) {
+    kv.assign(damping, damping + NC);
+  } else {
+    jackson(NC, kv);
+  }
+  for (int64_t n = 1; n < NC; ++n) kv[n] *= 2.0;  // h_n
+  CallScratch cs;
+  KPMGB_CUDA(cudaStreamCreateWithFlags(&cs.s, cudaStreamNonBlocking));
+  const int nb = (int)((NC + kTN - 1) / kTN);
+  double2 *d_mu = nullptr, *d_part = nullptr;
+  double *d_kv = nullptr, *d_x = nullptr, *d_th = nullptr, *d_sn = nullptr, *d_T = nullptr,
+         *d_ef = nullptr, *d_sig = nullptr;
+  KPMGB_TRY(cs.alloc(&d_mu, (size_t)NC * NC));
+  KPMGB_TRY(cs.alloc(&d_kv, NC));
+  KPMGB_TRY(cs.alloc(&d_x, Q));
+  KPMGB_TRY(cs.alloc(&d_th, Q));
+  KPMGB_TRY(cs.alloc(&d_sn, Q));
+  KPMGB_TRY(cs.alloc(&d_T, (size_t)NC * Q));
+  KPMGB_TRY(cs.alloc(&d_part, (size_t)nb * Q));
+  KPMGB_TRY(cs.alloc(&d_ef, nE));
+  KPMGB_TRY(cs.alloc(&d_sig, nE));
+  KPMGB_CUDA(cudaMemcpy2DAsync(d_mu, NC * sizeof(double2), mu2d, ld * sizeof(double2),
+                               NC * sizeof(double2), NC, cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_kv, kv.data(), NC * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_x, xs.data(), Q * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_th, th.data(), Q * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_sn, sn.data(), Q * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_ef, Ef, nE * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  k_cheb_table<<<grid1d((int64_t)NC * Q), 256, 0, cs.s>>>(d_th, Q, (int)NC, d_T);
+  KPMGB_LAUNCHED();
+  const int64_t jt = (Q + kTJ - 1) / kTJ;
+  if (jt > 65535) return fail(KPMGB_ERR_ARGUMENT, "quad_N too large");
+  k_kubo_nodes<<<dim3(nb, (unsigned)jt), kReconThreads, 0, cs.s>>>(d_mu, (int)NC, d_kv, d_T, Q,
+                                                                    d_x, d_th, d_sn, d_part);
+  KPMGB_LAUNCHED();
+  const double scale = -2.0 * (double)NH / (area * a * a);
+  k_kubo_fermi<<<(unsigned)nE, kReconThreads, 0, cs.s>>>(d_part, nb, Q, d_x, d_sn,
+                                                          M_PI / (double)quad_N, a, b, d_ef, beta,
+                                                          scale, d_sig);
+  KPMGB_LAUNCHED();
+  KPMGB_CUDA(cudaMemcpyAsync(sigma, d_sig, nE * sizeof(double), cudaMemcpyDeviceToHost, cs.s));
+  KPMGB_CUDA(cudaStreamSynchronize(cs.s));
+  return KPMGB_OK;
+}
+
+extern "C" int kpmgb_dos(const double* mu, int64_t NC, double a, double b, const double* damping,
+                         const double* E, int64_t nE, double* rho) {
+  clear_error();
+  if (!mu || !E || !rho) return fail(KPMGB_ERR_ARGUMENT, "null argument");
+  if (!(a > 0)) return fail(KPMGB_ERR_ARGUMENT, "dos: the rescale factor a must be positive");
+  if (NC < 1) return fail(KPMGB_ERR_ARGUMENT, "dos: NC must be >= 1");
+  if (nE < 0) return fail(KPMGB_ERR_ARGUMENT, "nE must be >= 0");
+  if (nE == 0) return KPMGB_OK;
+  std::vector<double> c;
+  if (damping) {
+    c.assign(damping, damping + NC);
+  } else {
+    jackson(NC, c);
+  }
+  for (int64_t n = 0; n < NC; ++n) c[n] *= mu[n] * (n ? 2.0 : 1.0);
+  CallScratch cs;
+  KPMGB_CUDA(cudaStreamCreateWithFlags(&cs.s, cudaStreamNonBlocking));
+  double *d_c = nullptr, *d_E = nullptr, *d_rho = nullptr;
+  KPMGB_TRY(cs.alloc(&d_c, NC));
+  KPMGB_TRY(cs.alloc(&d_E, nE));
+  KPMGB_TRY(cs.alloc(&d_rho, nE));
+  KPMGB_CUDA(cudaMemcpyAsync(d_c, c.data(), NC * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_E, E, nE * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  k_dos<<<grid1d(nE), 256, 0, cs.s>>>(d_c, (int)NC, a, b, d_E, nE, d_rho);
+  KPMGB_LAUNCHED();
+  KPMGB_CUDA(cudaMemcpyAsync(rho, d_rho, nE * sizeof(double), cudaMemcpyDeviceToHost, cs.s));
+  KPMGB_CUDA(cudaStreamSynchronize(cs.s));
+  return KPMGB_OK;
+}

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <vector>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -45,6 +46,29 @@ Shape pick_shape(int ncols) {
   if (ncols <= 32) return {32, 1};
   if (ncols <= 64) return {32, 2};
   return {32, 4};
+}
+
+// Register-gather shapes that cover ncols columns with at most 4x idle lanes,
+// the automatic one first (candidates of the autotuner).
+std::vector<Shape> candidate_shapes(int ncols) {
+  static const Shape all[] = {{1, 1}, {2, 1}, {4, 1}, {8, 1}, {4, 3},
+                              {16, 1}, {32, 1}, {32, 2}, {32, 4}};
+  std::vector<Shape> out{pick_shape(ncols)};
+  for (const Shape& s : all) {
+    const int cover = s.lpr * s.cpl;
+    if (cover >= ncols && cover <= 4 * std::max(ncols, 8) &&
+        !(s.lpr == out[0].lpr && s.cpl == out[0].cpl))
+      out.push_back(s);
+  }
+  return out;
+}
+
+Shape shape_for(const StepArgs& a, int ncols) {
+  if (a.shape > 0) {
+    const Shape s{a.shape / 10, a.shape % 10};
+    if (s.lpr * s.cpl >= ncols) return s;
+  }
+  return pick_shape(ncols);
 }
 
 KernelFn select_kernel(Shape s, int precision, int dot, bool real) {
@@ -92,11 +116,12 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
   for (int c0 = 0; c0 < NR; c0 += kMaxCols) {
     const int ncols = std::min(kMaxCols, NR - c0);
     const Shape s = pick_shape(ncols);
-    for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
-      KernelFn fn = select_kernel(s, precision, dot, H.is_real != 0);
-      const int G = grid_for(fn, NH, s.lpr);
-      worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
-    }
+    for (const Shape& c : candidate_shapes(ncols))
+      for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
+        KernelFn fn = select_kernel(c, precision, dot, H.is_real != 0);
+        const int G = grid_for(fn, NH, c.lpr);
+        worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
+      }
     if (precision == KPMGB_PREC_FF) {
       for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
         KernelFn fn = select_kernel_ffg(s, dot, H.is_real != 0);
@@ -187,13 +212,63 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
       KPMGB_LAUNCHED();
       continue;
     }
-    const Shape sh = pick_shape(p.ncols);
+    const Shape sh = shape_for(a, p.ncols);
     KernelFn fn = select_kernel(sh, precision, a.dot, H.is_real != 0);
     const int G = grid_for(fn, a.NH, sh.lpr);
     fn<<<G, kThreads, 0, s>>>(p);
     KPMGB_LAUNCHED();
   }
   return KPMGB_OK;
+}
+
+int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, int* shape) {
+  *variant = 1;
+  *shape = 0;
+  if (a0.NR > kMaxCols) return KPMGB_OK;  // several column batches: keep the default
+  struct Cand {
+    int variant, shape;
+  };
+  std::vector<Cand> cands;
+  for (const Shape& c : candidate_shapes(a0.NR)) cands.push_back({1, c.lpr * 10 + c.cpl});
+  if (precision == KPMGB_PREC_FF && a0.NR >= 32 && tma_chmax(a0.H->max_row_nnz) > 0)
+    cands.push_back({2, 0});
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  KPMGB_CUDA(cudaEventCreate(&e0));
+  cudaError_t ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) {
+    cudaEventDestroy(e0);
+    KPMGB_CUDA(ce);
+  }
+  float best = 0.f;
+  int rc = KPMGB_OK;
+  for (const Cand& c : cands) {
+    StepArgs a = a0;
+    a.variant = c.variant;
+    a.shape = c.shape;
+    a.xmax = nullptr;
+    if (launch_step(a, precision, s) != KPMGB_OK) {  // e.g. TMA stages that do not fit
+      clear_error();
+      continue;
+    }
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 3 && rc == KPMGB_OK; ++r) rc = launch_step(a, precision, s);
+    cudaEventRecord(e1, s);
+    if (rc != KPMGB_OK) break;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = fail(KPMGB_ERR_CUDA, "autotuning: %s", cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (best == 0.f || ms < best) {
+      best = ms;
+      *variant = c.variant;
+      *shape = c.shape;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
 }
 
 // ------------------------------------------------------------ block loading

@@ -35,6 +35,10 @@ EXPORTED_SYMBOLS = (
     "kpmgb_kpm1d_noalloc",
     "kpmgb_kpm1d_ensemble",
     "kpmgb_kpm1d_grad",
+    "kpmgb_kubo_bastin",
+    "kpmgb_dos",
+    "kpmgb_chebyshev_action",
+    "kpmgb_kpm1d_current",
 )
 
 
@@ -71,6 +75,7 @@ _lock = threading.Lock()
 
 def _declare(lib):
     vp, i32, i64, dp = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)
+    f64 = C.c_double
     lib.kpmgb_version.restype = C.c_char_p
     lib.kpmgb_last_error.restype = C.c_char_p
     lib.kpmgb_kernel_launch_count.restype = i64
@@ -87,6 +92,11 @@ def _declare(lib):
                                        C.POINTER(Kpm2dOptions), vp]
     lib.kpmgb_operator_sync.argtypes = [vp, vp]
     lib.kpmgb_kpm1d_ensemble.argtypes = [vp, i32, vp, i64, i64, vp, vp, C.POINTER(Kpm1dOptions)]
+    lib.kpmgb_kubo_bastin.argtypes = [vp, i64, i64, f64, f64, vp, i64, i64, f64, f64, vp, i64,
+                                      f64, vp]
+    lib.kpmgb_kpm1d_current.argtypes = [vp, vp, i64, i64, i64, vp, vp, C.POINTER(Kpm1dOptions)]
+    lib.kpmgb_chebyshev_action.argtypes = [vp, i64, i64, vp, i64, i64, vp, i64, vp]
+    lib.kpmgb_dos.argtypes = [vp, i64, f64, f64, vp, vp, i64, vp]
     lib.kpmgb_kpm1d_grad.argtypes = [vp, i64, i64, i64, vp, vp, i64, vp]
     lib.kpmgb_kpm1d_noalloc.argtypes = [i64, vp, vp, vp, i64, i64, vp, vp, vp]
     for name in EXPORTED_SYMBOLS:

@@ -32,6 +32,8 @@ SOURCES = [
     "kpmgb_noalloc.cu",
     "kpmgb_ensemble.cu",
     "kpmgb_adjoint.cu",
+    "kpmgb_recon.cu",
+    "kpmgb_action.cu",
 ]
 
 

@@ -177,3 +177,129 @@ def on_device(h: RescaledHamiltonian) -> RescaledHamiltonian:
     if isinstance(h.H, GB300Operator):
         return h
     return RescaledHamiltonian(GB300Operator(h.H), h.a, h.b)
+
+
+def jackson_kernel(n, N):
+    """Jackson damping factors g_n for an N-moment expansion
+    (``src/kernels/jackson_kernel.jl:7-8``)."""
+    n = np.asarray(n, dtype=np.float64)
+    c = np.pi / (N + 1)
+    return ((N + 1 - n) * np.cos(c * n) + np.sin(c * n) / np.tan(c)) / (N + 1) * (n < N)
+
+
+def dos_basis(NC: int, a: float, b: float, E_grid, kernel=jackson_kernel) -> np.ndarray:
+    """Matrix Phi (len(E_grid), NC) with rho(E_e) = Phi[e] @ mu.
+
+    The reconstruction of ``src/applications/dos.jl:76-161``
+    (rho(E) = sum_n h_n g_n mu_n T_n(x) / (a pi sqrt(1 - x^2)), x = (E - b)/a,
+    zero outside |E - b| < a) written as a linear map, so that a loss on the
+    DOS turns into moment weights for :func:`kpm_1d_grad`:
+    g = Phi.T @ dL/drho.
+    """
+    E = np.asarray(E_grid, dtype=np.float64)
+    n = np.arange(int(NC))
+    w = np.asarray(kernel(n, int(NC)), dtype=np.float64) * np.where(n != 0, 2.0, 1.0)
+    Phi = np.zeros((E.size, int(NC)))
+    inside = np.abs(E - b) < a
+    x = (E[inside] - b) / a
+    Phi[inside] = np.cos(np.outer(np.arccos(x), n)) * w / (a * np.pi * np.sqrt(1 - x * x))[:, None]
+    return Phi
+
+
+def _damping(kernel, NC: int):
+    if kernel is None:
+        return None
+    g = np.ascontiguousarray(np.broadcast_to(kernel(np.arange(NC), NC), (NC,)), dtype=np.float64)
+    return g
+
+
+def kubo_bastin_cond(mu2D, a: float, Ef, *, b: float = 0.0, NH: int, area: float,
+                     beta: float = math.inf, kernel=jackson_kernel, NC: int | None = None,
+                     quad_N: int | None = None, edge_cutoff: float = 1e-3):
+    """DC conductivity sigma_ab(Ef) in e^2/h (``src/applications/conductivity.jl:101-157``).
+
+    ``mu2D``: NC x NC moments of ``kpm_2d``.  ``Ef`` may be a scalar (returns
+    a float, as the reference) or an array of Fermi energies (returns an
+    array): the Ef-independent node sums run once on the GPU for all of them.
+    """
+    import ctypes as C
+    from . import _native
+    if not a > 0:
+        raise KPMArgumentError("kubo_bastin_cond: a must be positive.")
+    if not area > 0:
+        raise KPMArgumentError("kubo_bastin_cond: area must be positive.")
+    if not NH > 0:
+        raise KPMArgumentError("kubo_bastin_cond: NH must be positive.")
+    mu = np.asfortranarray(mu2D, dtype=np.complex128)
+    if mu.ndim != 2:
+        raise KPMArgumentError("kubo_bastin_cond: mu2D must be a matrix")
+    NCx = min(mu.shape) if NC is None else min(int(NC), *mu.shape)
+    quad_N = 8 * NCx if quad_N is None else int(quad_N)
+    if quad_N <= 0:
+        raise KPMArgumentError("kubo_bastin_cond: quad_N must be positive.")
+    if not 0 <= edge_cutoff < 1:
+        raise KPMArgumentError("kubo_bastin_cond: edge_cutoff must be in [0, 1).")
+    scalar = np.ndim(Ef) == 0
+    ef = np.ascontiguousarray(np.atleast_1d(np.asarray(Ef, dtype=np.float64)))
+    out = np.empty(ef.size, dtype=np.float64)
+    g = _damping(kernel, NCx)
+    lib = _native.load()
+    rc = lib.kpmgb_kubo_bastin(mu.ctypes.data, mu.shape[0], NCx, float(a), float(b),
+                               ef.ctypes.data, ef.size, int(NH), float(area), float(beta),
+                               g.ctypes.data if g is not None else None, quad_N,
+                               float(edge_cutoff), out.ctypes.data)
+    _native.check(rc)
+    return float(out[0]) if scalar else out
+
+
+def dos(mu_or_H, H_rescale_factor=None, *, b: float = 0.0, E_grid=None, N_tilde: int = 0,
+        E_range=None, NC: int = 0, NR: int = 12, kernel=jackson_kernel, dE_order: int = 0,
+        fix_normalization: float = 0.0, center: bool = False, rng=None):
+    """Density of states (``src/applications/dos.jl:43-161``); returns (E_grid, rho).
+
+    ``dos(mu, a; ...)`` reconstructs from moments on the GPU; ``dos(H; ...)``
+    first rescales H (``normalizeH``) and computes NC moments with NR
+    random-phase probes.
+    """
+    from . import _native
+    if H_rescale_factor is None:
+        H = mu_or_H
+        NCm = 1024 if NC == 0 else int(NC)
+        if center:
+            a, b, Hn = normalizeH(H, fixed_a=fix_normalization, center=True)
+        else:
+            a, Hn = normalizeH(H, fixed_a=fix_normalization)
+            b = 0.0
+        NH = Hn.shape[0]
+        psi = random_phase_vectors(np.random.default_rng() if rng is None else rng, NH, NR)
+        mu = kpm_1d(Hn, NCm, NR, NH, psi_in=psi)
+        return dos(mu, a, b=b, E_grid=E_grid, E_range=E_range, N_tilde=N_tilde, kernel=kernel,
+                   NC=NCm, dE_order=dE_order)
+    mu = np.asarray(mu_or_H)
+    if mu.ndim != 1:
+        raise KPMArgumentError("The input need to be 1D array")
+    a = float(H_rescale_factor)
+    if not a > 0:
+        raise KPMArgumentError("the rescale factor must be positive")
+    if dE_order != 0:
+        raise KPMArgumentError("dos: only dE_order = 0 is implemented by the GPU reconstruction")
+    NC = len(mu) if NC == 0 else min(int(NC), len(mu))
+    if E_grid is None:
+        N_tilde = NC * 2 if N_tilde == 0 else N_tilde
+        if E_range is None:
+            E_range = [b - 0.99 * a, b + 0.99 * a]
+        E_grid = np.arange(N_tilde + 1) * (E_range[1] - E_range[0]) / N_tilde + E_range[0]
+    else:
+        if E_range is not None:
+            raise KPMArgumentError("Should not set `E_grid` and `E_range` simultaneously.")
+        if N_tilde != 0 and len(E_grid) != N_tilde:
+            raise KPMArgumentError("`N_tilde` does not match with `E_grid`.")
+    E = np.ascontiguousarray(E_grid, dtype=np.float64)
+    m = np.ascontiguousarray(np.real(mu[:NC]), dtype=np.float64)
+    g = _damping(kernel, NC)
+    rho = np.empty(E.size, dtype=np.float64)
+    lib = _native.load()
+    _native.check(lib.kpmgb_dos(m.ctypes.data, NC, a, float(b),
+                                g.ctypes.data if g is not None else None, E.ctypes.data, E.size,
+                                rho.ctypes.data))
+    return E, rho

@@ -55,30 +55,32 @@ def _colmajor(psi, NH, NR, name):
     return np.asfortranarray(a, dtype=np.complex128)
 
 
-_VARIANT = {"auto": 0, "gather": 1, "tma": 2, "anchored": 3}
+_VARIANT = {"auto": 0, "gather": 1, "tma": 2, "anchored": 3, "tune": 4}
 
 
-def _opts1d(precision, stability_check, kernel="auto"):
+def _opts1d(precision, stability_check, kernel="auto", use_graph=False):
     if kernel not in _VARIANT:
         raise KPMArgumentError(f"kernel must be one of {sorted(_VARIANT)}")
-    return _native.Kpm1dOptions(_prec(precision), 1 if stability_check else 0, 0, _VARIANT[kernel])
+    return _native.Kpm1dOptions(_prec(precision), 1 if stability_check else 0,
+                                1 if use_graph else 0, _VARIANT[kernel])
 
 
 def kpm_1d_bang(H, NC: int, NR: int, NH: int, mu_all: np.ndarray, psi_in=None, psi_in_r=None,
                 *, precision: str = "fp64", stability_check: bool = False,
-                kernel: str = "auto") -> None:
+                kernel: str = "auto", use_graph: bool = False) -> None:
     """``kpm_1d!``: fill ``mu_all`` (NR, NC) in place.
 
     ``kpm_1d_bang(H, NC, NR, NH, mu_all, psi_in)`` is the doubling path
     (NC even); ``kpm_1d_bang(H, NC, NR, NH, mu_all, psi_in_l, psi_in_r)`` the
-    bra/ket path.
+    bra/ket path.  ``use_graph`` replays the recurrence as a CUDA graph
+    (captured on the first call, reused while sizes and buffers repeat).
     """
     op = as_operator(H)
     lib = _native.load()
     if mu_all.shape != (NR, NC):
         raise KPMArgumentError(f"mu_all has size {mu_all.shape}; expected ({NR}, {NC})")
     out = np.empty((NR, NC), dtype=np.complex128, order="F")
-    opts = _opts1d(precision, stability_check, kernel)
+    opts = _opts1d(precision, stability_check, kernel, use_graph)
     if psi_in_r is None:
         if NC % 2 != 0:
             raise KPMArgumentError("Invalid NC: NC should be even.")
@@ -98,7 +100,7 @@ def kpm_1d_bang(H, NC: int, NR: int, NH: int, mu_all: np.ndarray, psi_in=None, p
 def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=None,
            psi_in_r=None, force_norm: bool = False, verbose: int = 0, avg_output: bool = True,
            NR_parallel: bool = True, rng=None, precision: str = "fp64",
-           stability_check: bool = False, kernel: str = "auto"):
+           stability_check: bool = False, kernel: str = "auto", use_graph: bool = False):
     """Stochastic-trace Chebyshev moments (``src/moment.jl:339-418``).
 
     Returns the real probe average (length NC) for equal bra/ket, the complex
@@ -132,10 +134,10 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
     if NR_parallel:
         if lr:
             kpm_1d_bang(op, NC, NR, NH, mu_all, psi_in_l, psi_in_r, precision=precision,
-                        stability_check=stability_check, kernel=kernel)
+                        stability_check=stability_check, kernel=kernel, use_graph=use_graph)
         else:
             kpm_1d_bang(op, NC, NR, NH, mu_all, psi_in, precision=precision,
-                        stability_check=stability_check, kernel=kernel)
+                        stability_check=stability_check, kernel=kernel, use_graph=use_graph)
     else:
         for i in range(NR):
             row = np.zeros((1, NC), dtype=np.complex128)
@@ -285,7 +287,7 @@ def _stream_ptr(stream):
 
 def kpm_1d_device(op: GB300Operator, NC: int, psi_t, mu_t, *, psi_l_t=None,
                   precision="fp64", stability_check=False, stream=None,
-                  kernel="auto") -> None:
+                  kernel="auto", use_graph=False) -> None:
     """Enqueue kpm_1d on torch CUDA tensors without host copies.
 
     ``psi_t``: complex128 tensor of shape (NR, NH) (row-contiguous, i.e. the
@@ -299,7 +301,7 @@ def kpm_1d_device(op: GB300Operator, NC: int, psi_t, mu_t, *, psi_l_t=None,
             raise KPMArgumentError(f"{name} tensor must be contiguous")
     if tuple(mu_t.shape) != (NC, NR):
         raise KPMArgumentError(f"mu tensor must have shape ({NC}, {NR})")
-    opts = _opts1d(precision, stability_check, kernel)
+    opts = _opts1d(precision, stability_check, kernel, use_graph)
     if psi_l_t is None:
         rc = lib.kpmgb_kpm1d_device(op.handle, NC, NR, NH, C.c_void_p(psi_t.data_ptr()),
                                     C.c_void_p(mu_t.data_ptr()), C.byref(opts), _stream_ptr(stream))
@@ -397,3 +399,120 @@ def kpm_1d_grad(H, NC: int, psi_in, g, *, checkpoint_every: int = 0):
                               int(checkpoint_every), out.ctypes.data)
     _native.check(rc)
     return sp.csc_matrix((out, op.indices, op.indptr), shape=op.shape)
+
+
+def chebyshev_action_bang(out, Hn, V, C, *, check_every: int = 16, verbose: int = 0) -> None:
+    """``chebyshev_action!``: out[:, :, k] = sum_n C[n, k] T_{n-1}(Hn) V
+    (``src/utils/chebyshev_action.jl:47-122``), overwriting ``out``.
+
+    Coefficients are used verbatim (no h_n, no damping).  ``V``: (NH, NR) or
+    (NH,); ``C``: (NC, K) or (NC,); ``out``: complex (NH, NR, K), or the shape
+    with the vector axes of ``V`` / ``C`` dropped.  ``check_every`` runs the
+    reference's growth guard (0 disables it).
+    """
+    op = as_operator(Hn)
+    Vm = np.asarray(V)
+    Cm = np.asarray(C)
+    Vm2 = Vm.reshape(Vm.shape[0], -1) if Vm.ndim == 1 else Vm
+    Cm2 = Cm.reshape(-1, 1) if Cm.ndim == 1 else Cm
+    if Vm2.ndim != 2 or Cm2.ndim != 2:
+        raise KPMArgumentError("V and C must be vectors or matrices")
+    NH, NR = Vm2.shape
+    NC, K = Cm2.shape
+    if NC < 1:
+        raise KPMArgumentError("C must have at least one coefficient row")
+    if NR < 1:
+        raise KPMArgumentError("V must have at least one column")
+    if K < 1:
+        raise KPMArgumentError("C must have at least one coefficient column")
+    if op.shape[1] != NH:
+        raise KPMArgumentError(f"size(Hn, 2) = {op.shape[1]} must equal size(V, 1) = {NH}")
+    if check_every < 0:
+        raise KPMArgumentError("check_every must be >= 0")
+    if not isinstance(out, np.ndarray) or not np.iscomplexobj(out):
+        raise KPMArgumentError("out must be a complex numpy array")
+    if np.shares_memory(out, Vm):
+        raise KPMArgumentError("out must not alias V")
+    expect = [NH, NR, K]
+    if out.ndim == 2 and Cm.ndim == 1:
+        expect = [NH, NR]
+    elif out.ndim == 2 and Vm.ndim == 1:
+        expect = [NH, K]
+    elif out.ndim == 1:
+        expect = [NH]
+    if list(out.shape) != expect:
+        raise KPMArgumentError(f"out must be {' x '.join(map(str, expect))}, got {out.shape}")
+    Vf = np.asfortranarray(Vm2, dtype=np.complex128)
+    Cf = np.asfortranarray(Cm2, dtype=np.complex128)
+    res = np.empty((NH, NR, K), dtype=np.complex128, order="F")
+    lib = _native.load()
+    _native.check(lib.kpmgb_chebyshev_action(op.handle, NH, NR, Vf.ctypes.data, NC, K,
+                                             Cf.ctypes.data, int(check_every), res.ctypes.data))
+    out[...] = res.reshape(out.shape, order="F") if out.ndim < 3 else res
+
+
+def chebyshev_action(Hn, V, C, **kw):
+    """Allocating form of :func:`chebyshev_action_bang`; vector ``V`` drops the
+    probe axis, vector ``C`` the coefficient axis (``src/utils/chebyshev_action.jl:148-160``)."""
+    Vm, Cm = np.asarray(V), np.asarray(C)
+    NH = Vm.shape[0]
+    shape = [NH]
+    if Vm.ndim == 2:
+        shape.append(Vm.shape[1])
+    if Cm.ndim == 2:
+        shape.append(Cm.shape[1])
+    out = np.zeros(shape, dtype=np.complex128)
+    chebyshev_action_bang(out, Hn, V, C, **kw)
+    return out
+
+
+def kpm_1d_current(H, Ja, NC: int, NR: int, NH: int | None = None, *, psi_in=None,
+                   psi_in_l=None, psi_in_r=None, force_norm: bool = False, verbose: int = 0,
+                   avg_output: bool = True, NR_parallel: bool = True, rng=None,
+                   precision: str = "fp64", kernel: str = "auto"):
+    """Current moments mu_n = <psi| J_a T_n(H) |psi> (``src/moment.jl:558-714``).
+
+    No doubling: the bra J_a^dagger psi is formed on the GPU once and the
+    bra/ket recurrence runs NC - 1 steps.  ``Ja`` may be a SciPy matrix (its
+    adjoint is uploaded) or a ``GB300Operator`` that already holds
+    J_a^dagger.  Returns the complex probe average (length NC), or the
+    (NR, NC) matrix with ``avg_output=False``.  The separate-bra form
+    (``psi_in_l``/``psi_in_r``) is unimplemented, as in the reference.
+    """
+    import scipy.sparse as sp
+    NH = H.shape[0] if NH is None else int(NH)
+    NC, NR = int(NC), int(NR)
+    if psi_in is None:
+        if psi_in_l is not None or psi_in_r is not None:
+            if psi_in_l is None or psi_in_r is None:
+                raise KPMArgumentError("must set both `psi_in_l` and `psi_in_r` or neither.")
+            raise KPMArgumentError("unimplemented.")
+        from .frontend import random_phase_vectors
+        rng = np.random.default_rng() if rng is None else rng
+        psi_in = random_phase_vectors(rng, NH, NR)
+    elif psi_in_l is not None or psi_in_r is not None:
+        raise KPMArgumentError(
+            "must either set `psi_in` or set `psi_in_l` and `psi_in_r`, but not both.")
+    elif force_norm:
+        normalize_by_col(psi_in)
+    op = as_operator(H)
+    jadj = Ja if isinstance(Ja, GB300Operator) else GB300Operator(
+        sp.csc_matrix(Ja, dtype=np.complex128).conj().T)
+    psi = _colmajor(psi_in, NH, NR, "psi_in")
+    lib = _native.load()
+    opts = _opts1d(precision, False, kernel)
+    out = np.empty((NR, NC), dtype=np.complex128, order="F")
+    if NR_parallel:
+        _native.check(lib.kpmgb_kpm1d_current(op.handle, jadj.handle, NC, NR, NH,
+                                              psi.ctypes.data, out.ctypes.data, C.byref(opts)))
+    else:
+        for i in range(NR):
+            col = np.asfortranarray(psi[:, i:i + 1])
+            row = np.empty((1, NC), dtype=np.complex128, order="F")
+            _native.check(lib.kpmgb_kpm1d_current(op.handle, jadj.handle, NC, 1, NH,
+                                                  col.ctypes.data, row.ctypes.data, C.byref(opts)))
+            out[i] = row[0]
+    mu_all = np.ascontiguousarray(out)
+    if avg_output:
+        return mu_all.sum(axis=0) / NR
+    return mu_all

@@ -253,6 +253,35 @@ def kpm2d_dense_reference(H, Ja, Jb, psi_l, psi_r, NC):
     return mu
 
 
+def kpm_1d_current(H, Ja, NC: int, psi: np.ndarray) -> np.ndarray:
+    """mu[i, n] = <Ja^dagger psi_i | T_n(H) psi_i> (NR, NC) (``src/moment.jl:656-714``)."""
+    H = _csr(H)
+    Jd = _csr(Ja).conj().T.tocsr()
+    bra = Jd @ np.asarray(psi, dtype=np.complex128)
+    return kpm_1d_lr(H, NC, bra, psi)
+
+
+def chebyshev_action(H, V: np.ndarray, C: np.ndarray) -> np.ndarray:
+    """out[:, :, k] = sum_n C[n, k] T_{n-1}(H) V, coefficients verbatim
+    (``src/utils/chebyshev_action.jl:47-122``); V (NH, NR), C (NC, K)."""
+    H = _csr(H)
+    V = np.asarray(V, dtype=np.complex128)
+    C = np.asarray(C, dtype=np.complex128)
+    NH, NR = V.shape
+    NC, K = C.shape
+    out = np.zeros((NH, NR, K), dtype=np.complex128)
+    a_prev = V.copy()
+    out += a_prev[:, :, None] * C[0][None, None, :]
+    if NC == 1:
+        return out
+    a_cur = H @ a_prev
+    out += a_cur[:, :, None] * C[1][None, None, :]
+    for n in range(2, NC):
+        a_prev, a_cur = a_cur, cheb_step(H, a_prev, a_cur)
+        out += a_cur[:, :, None] * C[n][None, None, :]
+    return out
+
+
 # ------------------------------------------------------------ reconstruction
 def hn(n):
     """h_0 = 1, h_n = 2 (``src/kernels/kernels.jl:2``)."""

@@ -260,3 +260,63 @@ def test_anchored_kernel_matches_oracle(NR, lr):
                         kernel="anchored")
     for i in range(NR):
         assert relerr(got[i], ref[i]) < TOL["ff"]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+@pytest.mark.parametrize("lr", [False, True])
+def test_cuda_graph_replay_identical(prec, lr):
+    """use_graph captures the recurrence once and replays it: results are
+    bitwise those of direct launches, on the first call and on replays, and a
+    changed NC or probe count is captured afresh."""
+    rng = np.random.default_rng(17)
+    H = models.square_anderson(24, W=2.0, rng=rng)
+    op = kg.GB300Operator((H / 5.1).tocsc())
+    for NC, NR in ((128, 12), (128, 12), (64, 12), (64, 7)):
+        psi = ko.random_phase_vectors(rng, 576, NR)
+        kw = dict(psi_in_l=psi, psi_in_r=psi[:, ::-1].copy()) if lr else dict(psi_in=psi)
+        ref = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, **kw)
+        n0 = kg.kernel_launch_count()
+        g1 = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, use_graph=True, **kw)
+        n1 = kg.kernel_launch_count()
+        g2 = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, use_graph=True, **kw)
+        n2 = kg.kernel_launch_count()
+        assert np.array_equal(g1, ref) and np.array_equal(g2, ref)
+        assert n2 - n1 == n1 - n0 > 0
+
+
+def test_cuda_graph_device_api_stream():
+    import torch
+    rng = np.random.default_rng(3)
+    H = models.square_anderson(16, W=1.0, rng=rng)
+    op = kg.GB300Operator((H / 4.6).tocsc())
+    NC, NR = 96, 8
+    psi = ko.random_phase_vectors(rng, 256, NR)
+    psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    s = torch.cuda.Stream()
+    outs = []
+    mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
+    for use_graph in (False, True, True):
+        mu_t.zero_()
+        kg.kpm_1d_device(op, NC, psi_t, mu_t, precision="ff", stream=s, use_graph=use_graph)
+        kg.sync(op, s)
+        outs.append(mu_t.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+@pytest.mark.parametrize("NR", [5, 12, 40, 64])
+def test_autotuned_kernel_matches_oracle(prec, NR):
+    rng = np.random.default_rng(NR)
+    H = models.square_anderson(20, W=2.0, rng=rng)
+    H = (H / 5.1).tocsc()
+    op = kg.GB300Operator(H)
+    psi = ko.random_phase_vectors(rng, 400, NR)
+    ref = ko.kpm_1d_doubling(H, 64, psi)
+    a = kg.kpm_1d(op, 64, NR, psi_in=psi, avg_output=False, precision=prec, kernel="tune")
+    b = kg.kpm_1d(op, 64, NR, psi_in=psi, avg_output=False, precision=prec, kernel="tune",
+                  use_graph=True)
+    assert relerr(a, ref) < TOL[prec]
+    assert np.array_equal(a, b)
+    lr = kg.kpm_1d(op, 33, NR, psi_in_l=psi, psi_in_r=psi, avg_output=False, precision=prec,
+                   kernel="tune")
+    assert relerr(lr, ko.kpm_1d_lr(H, 33, psi, psi)) < TOL[prec]
