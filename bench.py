@@ -55,6 +55,12 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5", "action"],
+                   help="c2 (default): the headline kpm_1d line; the others print one JSON "
+                        "line each for the secondary configurations")
+    p.add_argument("--haldane-L", type=int, default=256, help="c3: Haldane cells per side")
+    p.add_argument("--contraction", default="both", choices=["both", "split", "fp64"],
+                   help="c3: which kpm_2d contraction(s) to time")
     return p.parse_args()
 
 
@@ -200,6 +206,189 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------ secondary workloads
+def _events(stream):
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _time_device(fn, stream, warmup, steps, sync):
+    """Average ms of fn() over `steps` calls on `stream` (CUDA events), after warm-up."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    sync()
+    torch.cuda.synchronize()
+    e0, e1 = _events(stream)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sync()
+    return e0.elapsed_time(e1) / steps
+
+
+def _time_host(fn, warmup, steps):
+    for _ in range(warmup):
+        fn()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        fn()
+    return (time.perf_counter() - t0) * 1e3 / steps
+
+
+def workload_c1(args):
+    """2D square Anderson L=64 (NH=4096, 5 nnz/row), W=2, NC=1024, NR=12: the
+    L2-resident configuration the CPU port runs in full."""
+    import torch
+    import kpm_gb300 as kg
+    from kpm_gb300 import models, rescale
+    from oracle import cpu_port
+    H = models.square_anderson(64, W=2.0, rng=np.random.default_rng(42))
+    h = rescale(H)
+    NH, NR, NC = 4096, 12, 1024
+    psi = kg.random_phase_vectors(np.random.default_rng(42), NH, NR)
+    op = kg.GB300Operator(h.H)
+    s = torch.cuda.Stream()
+    psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
+    vs = NR * NC // 2
+    out = {"workload": "c1: kpm_1d, 2D square Anderson L=64 (NH=4096), W=2, NC=1024, NR=12",
+           "metric": METRIC, "unit": UNIT}
+    for prec in ("fp64", "ff"):
+        for graph in (False, True):
+            ms = _time_device(lambda: kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec,
+                                                       stream=s, use_graph=graph),
+                              s, args.warmup, max(args.steps, 10), lambda: kg.sync(op, s))
+            out[f"{prec}{'_graph' if graph else ''}"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+    ms_h = _time_host(lambda: kg.kpm_1d(op, NC, NR, psi_in=psi, use_graph=True), 2, 10)
+    out["e2e_fp64_graph"] = {"ms_per_call": ms_h, "value": vs / (ms_h / 1e3)}
+    nt = cpu_port.max_threads()
+    t0 = time.perf_counter()
+    cpu_port.kpm1d_cpu(h.H, NC, psi, nthreads=nt)
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": vs / dt, "unit": UNIT, "cores": nt, "kind": "port",
+                           "sample": "the full c1 call (512 steps)"}
+    return out
+
+
+def workload_c3(args):
+    """kpm_2d on the Haldane model 256x256 cells (NH=131072), NC=512, NR=16, then
+    sigma_xy at 201 Fermi energies in [-3, 3]."""
+    import torch
+    import kpm_gb300 as kg
+    from kpm_gb300 import models, rescale
+    Lh = args.haldane_L
+    H, Jx, Jy, area = models.haldane(Lh, Lh, t=1.0, t2=0.1)
+    h = rescale(H, center=True)
+    NH, NR, NC = H.shape[0], 16, 512
+    psi = kg.random_phase_vectors(np.random.default_rng(42), NH, NR)
+    ops = [kg.GB300Operator(M) for M in (h.H, Jx, Jy)]
+    s = torch.cuda.Stream()
+    psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    F = 8.0 * NC * NC * NH * NR
+    out = {"workload": f"c3: kpm_2d, Haldane {Lh}x{Lh}x2 (NH={NH}), t2=0.1i, NC=512, NR=16; "
+                       "sigma_xy at 201 Ef",
+           "flop_per_call_complex_fp64_equivalent": F}
+    mus = {}
+    forms = {"split": [("ff", "split"), ("fp64", "split")], "fp64": [("fp64", "fp64")]}
+    which = (forms["split"] + forms["fp64"]) if args.contraction == "both" else forms[args.contraction]
+    for prec, contraction in which:
+        key = f"{prec}_recurrence_{contraction}_contraction"
+        mu_t = torch.zeros((NC, NC), dtype=torch.complex128, device="cuda")
+        steps = 1 if contraction == "fp64" else max(args.steps, 1)
+        ms = _time_device(lambda: kg.kpm_2d_device(ops[0], ops[1], ops[2], NC, psi_t, psi_t, mu_t,
+                                                   precision=prec, contraction=contraction,
+                                                   stream=s),
+                          s, 1, steps, lambda: kg.sync(ops[0], s))
+        mus[key] = mu_t.cpu().numpy().T.copy()
+        out[key] = {"ms_per_call": ms, "TFLOP/s": F / (ms / 1e3) / 1e12}
+    ref_key = "fp64_recurrence_fp64_contraction"
+    if ref_key in mus:
+        b = mus[ref_key]
+        for k, a in mus.items():
+            if k != ref_key:
+                out[f"{k}_rel_err_vs_fp64"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    Efs = np.linspace(-3, 3, 201)
+    t0 = time.perf_counter()
+    last = f"{which[-1][0]}_recurrence_{which[-1][1]}_contraction"
+    sig = kg.kubo_bastin_cond(mus[last], h.a, Efs, b=h.b, NH=NH, area=area)
+    out["kubo_bastin_201_Ef_ms"] = (time.perf_counter() - t0) * 1e3
+    out["sigma_xy_at_Ef0"] = float(sig[100])
+    return out
+
+
+def workload_c4(args):
+    """256 realisations of the 2D Anderson model, L ~ U{24..96}, W ~ U[1, 8],
+    NC=512, NR=8: one persistent ensemble launch against per-member calls."""
+    import kpm_gb300 as kg
+    from kpm_gb300 import models
+    rng = np.random.default_rng(42)
+    Hs, psis = [], []
+    for _ in range(256):
+        L = int(rng.integers(24, 97))
+        W = float(rng.uniform(1.0, 8.0))
+        Hs.append((models.square_anderson(L, W=W, rng=rng) / (4.0 + W / 2 + 0.1)).tocsc())
+        psis.append(kg.random_phase_vectors(rng, L * L, 8))
+    NC, NR = 512, 8
+    vs = 256 * NR * NC // 2
+    out = {"workload": "c4: 256 x kpm_1d, 2D Anderson L~U{24..96}, W~U[1,8], NC=512, NR=8",
+           "metric": METRIC, "unit": UNIT, "mean_NH": float(np.mean([H.shape[0] for H in Hs]))}
+    for prec in ("fp64", "ff"):
+        ms = _time_host(lambda: kg.kpm_1d_ensemble(Hs, NC, psis, precision=prec), 1,
+                        max(args.steps, 3))
+        out[f"ensemble_{prec}"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+    ops = [kg.GB300Operator(H) for H in Hs]
+    def loop():
+        for op, p in zip(ops, psis):
+            kg.kpm_1d(op, NC, NR, psi_in=p, use_graph=True)
+    ms = _time_host(loop, 1, max(args.steps, 3))
+    out["per_member_calls_fp64_graph"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+    return out
+
+
+def workload_c5(args):
+    """Adjoint gradient: graphene 128x128 (NH=32768), onsite N(0, 0.1^2),
+    NC=1024, NR=16; forward kpm_1d vs kpmgb_kpm1d_grad."""
+    import kpm_gb300 as kg
+    from kpm_gb300 import models
+    rng = np.random.default_rng(42)
+    NH = 2 * 128 * 128
+    H = (models.graphene(128, 128, onsite=0.1 * rng.standard_normal(NH)) / 3.4).tocsc()
+    NC, NR = 1024, 16
+    psi = kg.random_phase_vectors(rng, NH, NR)
+    g = rng.standard_normal(NC)
+    op = kg.GB300Operator(H)
+    out = {"workload": "c5: gradient of sum_m g_m mu_m, graphene 128x128 (NH=32768), NC=1024, NR=16"}
+    tf = _time_host(lambda: kg.kpm_1d(op, NC, NR, psi_in=psi), 1, max(args.steps, 3))
+    out["forward_ms"] = tf
+    for C in (0, 64):
+        tg = _time_host(lambda: kg.kpm_1d_grad(op, NC, psi, g, checkpoint_every=C), 1,
+                        max(args.steps, 3))
+        out[f"grad_checkpoint_{C or 'auto'}_ms"] = tg
+        out[f"grad_over_forward_{C or 'auto'}"] = tg / tf
+    return out
+
+
+def workload_action(args):
+    """chebyshev_action: 256x256 periodic square (NH=65536), NC=1024, NR=8, K=2
+    (the reference benchmark's configuration), stability guard off."""
+    import kpm_gb300 as kg
+    from kpm_gb300 import models
+    H = (models.square_anderson(256, W=0.0) / 4.2).tocsc()
+    V = kg.random_phase_vectors(np.random.default_rng(42), 65536, 8)
+    n = np.arange(1024)
+    C = np.stack([np.where(n == 0, 1.0, 2.0) * np.cos(n * np.pi / 2) * np.exp(-n / 300),
+                  np.where(n == 0, 1.0, 2.0) * np.cos(n * 1.3) * np.exp(-n / 300)], axis=1)
+    op = kg.GB300Operator(H)
+    ms = _time_host(lambda: kg.chebyshev_action(op, V, C, check_every=0), 1, max(args.steps, 3))
+    NH, NR, NC, K = 65536, 8, 1024, 2
+    return {"workload": "chebyshev_action, square 256x256 (NH=65536), NC=1024, NR=8, K=2",
+            "ms_per_call_e2e": ms, "vector_steps_per_s": NR * (NC - 1) / (ms / 1e3),
+            "h2d_bytes": NH * NR * 16 + NC * K * 16, "d2h_bytes": NH * NR * K * 16}
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -207,6 +396,16 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload != "c2":
+        import torch
+        torch.cuda.set_device(local)
+        fn = {"c1": workload_c1, "c3": workload_c3, "c4": workload_c4, "c5": workload_c5,
+              "action": workload_action}[args.workload]
+        res = fn(args)
+        res["version"] = __import__("kpm_gb300").version()
+        if rank == 0:
+            print(json.dumps(res), flush=True)
         return
     import torch
     import torch.distributed as dist

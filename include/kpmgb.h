@@ -184,6 +184,16 @@ int kpmgb_kpm1d_current(kpmgb_operator H, kpmgb_operator Jadj, int64_t NC,
                         int64_t NR, int64_t NH, const double* psi,
                         double* mu_all, const kpmgb_kpm1d_options* opts);
 
+/* kpm_3d!: mu[n, m, n1] = kpm_2d(H, Jc, Jb; psi_l, T_{n1-1}(H) Ja psi_r)[n, m]
+ * (src/moment.jl:1105-1228), i.e. mu[n,m,p] = (1/NR) sum_i
+ * <psi_l| T_m Jb T_n Jc T_p Ja |psi_r> for identity-like probes.  mu: host
+ * NC x NC x NC column-major complex.  opts as kpmgb_kpm2d (blocking,
+ * precision and contraction of every slice).  Blocking call. */
+int kpmgb_kpm3d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
+                kpmgb_operator Jc, int64_t NC, int64_t NR, int64_t NH,
+                const double* psi_l, const double* psi_r, double* mu,
+                const kpmgb_kpm2d_options* opts);
+
 /* chebyshev_action!: out[:, :, k] = sum_{n=1}^{NC} C[n, k] T_{n-1}(H) V
  * (src/utils/chebyshev_action.jl:47-122), coefficients used verbatim (no h_n,
  * no damping).  V: column-major NH x NR complex; C: column-major NC x K

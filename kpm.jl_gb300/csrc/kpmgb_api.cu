@@ -949,3 +949,71 @@ extern "C" int kpmgb_kpm1d_current(kpmgb_operator h, kpmgb_operator jadj, int64_
   KPMGB_CUDA(cudaMemcpyAsync(mu_all, ws.mu.ptr, (size_t)NR * NC * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
 }
+
+// ------------------------------------------------------------------ kpm_3d
+// kpm_3d!(H, Ja, Jb, Jc, NC, NR, NH, mu, psi_in_l, psi_in_r)
+// (src/moment.jl:1105-1228): mu[:, :, n1] = kpm_2d(H, Jc, Jb) with the right
+// probes T_{n1-1}(H) Ja psi_r.  The outer chain runs in FP64 row-major slots;
+// each slice is one kpm_2d on the device.
+extern "C" int kpmgb_kpm3d(kpmgb_operator h, kpmgb_operator ja, kpmgb_operator jb,
+                           kpmgb_operator jc, int64_t NC, int64_t NR, int64_t NH,
+                           const double* psi_l, const double* psi_r, double* mu,
+                           const kpmgb_kpm2d_options* opts) {
+  clear_error();
+  if (!h || !ja || !jb || !jc) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  if (!psi_l || !psi_r || !mu) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
+  if (NC < 2) return fail(KPMGB_ERR_ARGUMENT, "NC must be at least 2 (got %lld)", (long long)NC);
+  if (NR < 1) return fail(KPMGB_ERR_ARGUMENT, "NR must be positive");
+  Operator* op = as_op(h);
+  Operator* A = as_op(ja);
+  if (NH != op->csr.n || NH != A->csr.n || NH != as_op(jb)->csr.n || NH != as_op(jc)->csr.n)
+    return fail(KPMGB_ERR_ARGUMENT, "`psi_in_r` has size (%lld, %lld) but expecting %lld, %lld",
+                (long long)NH, (long long)NR, (long long)op->csr.n, (long long)NR);
+  Guard g(op);
+  cudaStream_t s = op->stream;
+  Workspace& ws = op->ws;
+  const size_t blk = (size_t)NH * NR * 16;
+  KPMGB_TRY(ws.psi_in.ensure(3 * blk));
+  KPMGB_TRY(ws.slots.ensure(4 * blk));
+  KPMGB_TRY(ws.mu.ensure((size_t)NC * NC * 16));
+  char* in = ws.psi_in.as<char>();
+  char* sl = ws.slots.as<char>();
+  auto ring = [&](int64_t n1) { return sl + (1 + (n1 - 1) % 3) * blk; };
+  KPMGB_CUDA(cudaMemcpyAsync(in, psi_l, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_CUDA(cudaMemcpyAsync(in + blk, psi_r, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(launch_load_block(in + blk, sl, NH, (int)NR, KPMGB_PREC_FP64, nullptr, false, s));
+  StepArgs a;
+  a.NH = NH;
+  a.NR = (int)NR;
+  for (int64_t n1 = 1; n1 <= NC; ++n1) {
+    if (n1 == 1) {  // Ja psi_r
+      a.H = &A->csr;
+      a.x = sl;
+      a.z = nullptr;
+      a.y = ring(1);
+      a.alpha = 1.0;
+      a.beta = 0.0;
+    } else if (n1 == 2) {  // H Ja psi_r
+      a.H = &op->csr;
+      a.x = ring(1);
+      a.y = ring(2);
+    } else {  // 2 H v_{n1-1} - v_{n1-2}, in place over v_{n1-2}
+      a.H = &op->csr;
+      a.x = ring(n1 - 1);
+      a.z = ring(n1 - 2);
+      a.y = ring(n1);
+      a.alpha = 2.0;
+      a.beta = -1.0;
+    }
+    KPMGB_TRY(launch_step(a, KPMGB_PREC_FP64, s));
+    KPMGB_TRY(launch_rowmajor_to_colmajor(reinterpret_cast<const double2*>(ring(n1)),
+                                          reinterpret_cast<double2*>(in + 2 * blk), NH, (int)NR, 1,
+                                          s));
+    KPMGB_TRY(run_kpm2d(op, as_op(jc), as_op(jb), NC, NR, NH, in, in + 2 * blk,
+                        ws.mu.as<double2>(), opts, s));
+    KPMGB_CUDA(cudaMemcpyAsync(mu + (size_t)(n1 - 1) * NC * NC * 2, ws.mu.ptr,
+                               (size_t)NC * NC * 16, cudaMemcpyDeviceToHost, s));
+    KPMGB_TRY(check_status(op, s));
+  }
+  return KPMGB_OK;
+}

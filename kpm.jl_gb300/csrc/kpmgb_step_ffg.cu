@@ -12,8 +12,8 @@
 // step that produced each vector (this kernel writes the maxima of its output
 // y).  The accumulators therefore start at a fixed anchor per column, every
 // product costs one rounding-exact anchored update (4 FP32 operations + 2 for
-// the low-order cross terms), the operator row is streamed without chunking,
-// and the dots cost half of the TwoSum form.  A looser anchor only costs
+// the low-order cross terms), chunks of a row need no per-chunk anchor or
+// merge, and the dots cost half of the TwoSum form.  A looser anchor only costs
 // precision in the last bits (about log2 of max/typical magnitude), never
 // correctness: the anchor invariant holds for every input.
 #include <cuda_runtime.h>
@@ -79,8 +79,13 @@ __device__ __forceinline__ void gnorm2(float (&A)[2], float (&C)[2], float4 a) {
 
 }  // namespace
 
+#ifndef KPMGB_FFG_CHUNK
+#define KPMGB_FFG_CHUNK 8
+#endif
+
 template <int LPR, int CPL, bool REALH, int DOT>
 __global__ void __launch_bounds__(kThreads, KPMGB_FF_MIN_BLOCKS) k_step_ffg(KParams p) {
+  constexpr int CH = KPMGB_FFG_CHUNK;
   constexpr int ND = NDots<DOT>::value;
   static_assert(ND > 0, "the maxima-anchored kernel serves the moment steps");
   constexpr int GROUPS = kThreads / LPR;
@@ -148,16 +153,36 @@ __global__ void __launch_bounds__(kThreads, KPMGB_FF_MIN_BLOCKS) k_step_ffg(KPar
       Ar[c] = Ai[c] = sig_y[c];
       Cr[c] = Ci[c] = 0.f;
     }
-#pragma unroll 8
-    for (int k = k0; k < k1; ++k) {
-      const int j = __ldg(p.col + k);
-      const HV h = __ldg(val + k);
-      const float4* xr = x + (int64_t)j * p.ld + p.c0;
+    // Chunks of CH nonzeros: all indices, values and gathers of a chunk are
+    // issued before any arithmetic (memory-level parallelism).  Unused slots
+    // carry exact zeros, which leave the anchored accumulators unchanged.
+    for (int kc = k0; kc < k1; kc += CH) {
+      const int cnt = min(CH, k1 - kc);
+      int jj[CH];
+      HV hv[CH];
+#pragma unroll
+      for (int u = 0; u < CH; ++u) {
+        if (u < cnt) {
+          jj[u] = __ldg(p.col + kc + u);
+          hv[u] = __ldg(val + kc + u);
+        } else {
+          jj[u] = 0;
+          hzero(hv[u]);
+        }
+      }
+      float4 xv[CPL][CH];
 #pragma unroll
       for (int c = 0; c < CPL; ++c) {
         const int cc = lg + c * LPR;
-        if (cc < p.ncols) gmac<REALH>(Ar[c], Cr[c], Ai[c], Ci[c], h, __ldg(xr + cc));
+#pragma unroll
+        for (int u = 0; u < CH; ++u)
+          xv[c][u] = (u < cnt && cc < p.ncols) ? __ldg(x + (int64_t)jj[u] * p.ld + p.c0 + cc)
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
       }
+#pragma unroll
+      for (int c = 0; c < CPL; ++c)
+#pragma unroll
+        for (int u = 0; u < CH; ++u) gmac<REALH>(Ar[c], Cr[c], Ai[c], Ci[c], hv[u], xv[c][u]);
     }
     const int64_t base = r * p.ld + p.c0;
 #pragma unroll

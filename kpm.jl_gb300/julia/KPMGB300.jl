@@ -143,4 +143,67 @@ function KPM.kpm_2d!(H::GB300CSR, Jα, Jβ, NC::Int64, NR::Int64, NH::Int64, μ,
     return nothing
 end
 
+# kpm_1d_current! (src/moment.jl:656-714): the adjoint of Jα is uploaded as its
+# own handle and the bra J†ψ is formed on the device.
+function KPM.kpm_1d_current!(H::GB300CSR, Jα, NC::Int64, NR::Int64, NH::Int64, mu_all, psi_in;
+                             precision::Symbol = :fp64, kwargs...)
+    Jadj = Jα isa GB300CSR ? Jα : GB300CSR(sparse(Jα'))
+    out = Matrix{ComplexF64}(undef, NR, NC)
+    opts = Ref(Kpm1dOptions(_prec(precision), 0, 0, 0))
+    _check(ccall((:kpmgb_kpm1d_current, libkpmgb), Cint,
+                 (Ptr{Cvoid}, Ptr{Cvoid}, Int64, Int64, Int64, Ptr{ComplexF64}, Ptr{ComplexF64},
+                  Ref{Kpm1dOptions}),
+                 H.handle, Jadj.handle, NC, NR, NH, Matrix{ComplexF64}(psi_in), out, opts))
+    mu_all .= out
+    return nothing
+end
+
+# chebyshev_action! (src/utils/chebyshev_action.jl:47-122)
+function KPM.chebyshev_action!(out::AbstractArray{<:Complex,3}, Hn::GB300CSR, V::AbstractMatrix,
+                               C::AbstractMatrix; check_every::Integer = 16, kwargs...)
+    NH, NR = size(V)
+    NC, K = size(C)
+    res = Array{ComplexF64,3}(undef, NH, NR, K)
+    _check(ccall((:kpmgb_chebyshev_action, libkpmgb), Cint,
+                 (Ptr{Cvoid}, Int64, Int64, Ptr{ComplexF64}, Int64, Int64, Ptr{ComplexF64}, Int64,
+                  Ptr{ComplexF64}),
+                 Hn.handle, NH, NR, Matrix{ComplexF64}(V), NC, K, Matrix{ComplexF64}(C),
+                 Int64(check_every), res))
+    out .= res
+    return nothing
+end
+
+# kubo_bastin_cond (src/applications/conductivity.jl:101-157) for a vector of
+# Fermi energies in one device pass.
+function kubo_bastin_cond_gpu(mu2D, a::Real, Efs::AbstractVector; b::Real = 0.0, NH::Integer,
+                              area::Real, beta::Real = Inf, kernel = KPM.JacksonKernel,
+                              NC::Int64 = size(mu2D, 1), quad_N::Int64 = 8 * NC,
+                              edge_cutoff::Real = 1e-3)
+    NC = min(NC, size(mu2D, 1), size(mu2D, 2))
+    g = Float64[kernel(n, NC) for n = 0:(NC-1)]
+    σ = Vector{Float64}(undef, length(Efs))
+    _check(ccall((:kpmgb_kubo_bastin, libkpmgb), Cint,
+                 (Ptr{ComplexF64}, Int64, Int64, Float64, Float64, Ptr{Float64}, Int64, Int64,
+                  Float64, Float64, Ptr{Float64}, Int64, Float64, Ptr{Float64}),
+                 Matrix{ComplexF64}(mu2D), size(mu2D, 1), NC, a, b, Vector{Float64}(Efs),
+                 length(Efs), NH, area, beta, g, quad_N, edge_cutoff, σ))
+    return σ
+end
+
+# dL/dH on the sparsity pattern of H for L = sum_m g[m] mu_m (doubling moments);
+# no reference counterpart.  Returns a SparseMatrixCSC with H's pattern.
+function kpm_1d_grad(H::SparseMatrixCSC, NC::Int64, psi_in::AbstractMatrix, g::AbstractVector;
+                     checkpoint_every::Int64 = 0)
+    Hc = SparseMatrixCSC{ComplexF64,Int64}(H)
+    op = GB300CSR(Hc)
+    NH, NR = size(psi_in)
+    out = Vector{ComplexF64}(undef, nnz(Hc))
+    _check(ccall((:kpmgb_kpm1d_grad, libkpmgb), Cint,
+                 (Ptr{Cvoid}, Int64, Int64, Int64, Ptr{ComplexF64}, Ptr{Float64}, Int64,
+                  Ptr{ComplexF64}),
+                 op.handle, NC, NR, NH, Matrix{ComplexF64}(psi_in), Vector{Float64}(g),
+                 checkpoint_every, out))
+    return SparseMatrixCSC(size(Hc, 1), size(Hc, 2), copy(Hc.colptr), copy(Hc.rowval), out)
+end
+
 end # module

@@ -516,3 +516,39 @@ def kpm_1d_current(H, Ja, NC: int, NR: int, NH: int | None = None, *, psi_in=Non
     if avg_output:
         return mu_all.sum(axis=0) / NR
     return mu_all
+
+
+def kpm_3d(H, Ja, Jb, Jc, NC: int, NR: int, NH: int, *, arr_size="auto", right_block="auto",
+           verbose: int = 0, psi_in_l=None, psi_in_r=None, psi_in=None, precision="fp64",
+           contraction="fp64", rng=None):
+    """Three-operator moments mu[n, m, p] (NC, NC, NC) (``src/moment.jl:1105-1280``).
+
+    ``mu[:, :, p] = kpm_2d(H, Jc, Jb; psi_l, T_p(H) Ja psi_r)``.  Probe rules
+    follow the reference: ``psi_in`` wins over ``psi_in_l``/``psi_in_r``; one
+    of the pair alone is used for both; none draws random phases.
+    """
+    import warnings
+    NC, NR, NH = int(NC), int(NR), int(NH)
+    if psi_in is not None:
+        if psi_in_l is not None or psi_in_r is not None:
+            warnings.warn("`psi_in_l`, `psi_in_r` and `psi_in` are simultaneously set. "
+                          "Taking `psi_in` and discarding the others")
+        psi_in_l = psi_in_r = psi_in
+    elif psi_in_l is not None or psi_in_r is not None:
+        if psi_in_l is None or psi_in_r is None:
+            warnings.warn("only one of `psi_in_l` and `psi_in_r` is set. Setting them as the same.")
+            psi_in_l = psi_in_r = psi_in_l if psi_in_l is not None else psi_in_r
+    else:
+        from .frontend import random_phase_vectors
+        rng = np.random.default_rng() if rng is None else rng
+        psi_in_l = psi_in_r = random_phase_vectors(rng, NH, NR)
+    pl = _colmajor(psi_in_l, NH, NR, "psi_in_l")
+    pr = _colmajor(psi_in_r, NH, NR, "psi_in_r")
+    ops = [as_operator(M) for M in (H, Ja, Jb, Jc)]
+    opts = _opts2d(arr_size, right_block, "auto", "NONE", False, precision, contraction)
+    mu = np.zeros((NC, NC, NC), dtype=np.complex128, order="F")
+    lib = _native.load()
+    _native.check(lib.kpmgb_kpm3d(ops[0].handle, ops[1].handle, ops[2].handle, ops[3].handle, NC,
+                                  NR, NH, pl.ctypes.data, pr.ctypes.data, mu.ctypes.data,
+                                  C.byref(opts)))
+    return mu

@@ -256,9 +256,28 @@ def kpm2d_dense_reference(H, Ja, Jb, psi_l, psi_r, NC):
 def kpm_1d_current(H, Ja, NC: int, psi: np.ndarray) -> np.ndarray:
     """mu[i, n] = <Ja^dagger psi_i | T_n(H) psi_i> (NR, NC) (``src/moment.jl:656-714``)."""
     H = _csr(H)
-    Jd = _csr(Ja).conj().T.tocsr()
+    Jd = sp.csr_matrix(_csr(Ja)).conj().T.tocsr()
     bra = Jd @ np.asarray(psi, dtype=np.complex128)
     return kpm_1d_lr(H, NC, bra, psi)
+
+
+def kpm_3d(H, Ja, Jb, Jc, NC: int, psi_l: np.ndarray, psi_r: np.ndarray) -> np.ndarray:
+    """mu[:, :, p] = kpm_2d(H, Jc, Jb; psi_l, T_p(H) Ja psi_r) (``src/moment.jl:1105-1228``)."""
+    H = _csr(H)
+    v_prev = _csr(Ja) @ np.asarray(psi_r, dtype=np.complex128)
+    mu = np.zeros((NC, NC, NC), dtype=np.complex128)
+    v_cur = None
+    for p in range(NC):
+        if p == 0:
+            v = v_prev
+        elif p == 1:
+            v_cur = H @ v_prev
+            v = v_cur
+        else:
+            v_prev, v_cur = v_cur, cheb_step(H, v_prev, v_cur)
+            v = v_cur
+        mu[:, :, p] = kpm_2d(H, Jc, Jb, NC, psi_l, v, NC, min(NC, 16))
+    return mu
 
 
 def chebyshev_action(H, V: np.ndarray, C: np.ndarray) -> np.ndarray:

@@ -250,3 +250,50 @@ def test_c_port_matches_oracle():
     ref = ko.kpm_1d_doubling(Hn, 128, psi)
     got = cpu_port.kpm1d_cpu(Hn, 128, psi, nthreads=2)
     assert relerr(got, ref) < 1e-12
+
+
+def test_oracle_kpm3d_trace_formula():
+    """test/cpge_test.jl:319-338: mu[n,m,p] = Tr[T_m Jb T_n Jc T_p Ja] / D with
+    identity probes."""
+    from helpers import rand_herm
+    rng = np.random.default_rng(9)
+    D, NC = 10, 5
+    H = rand_herm(rng, D)
+    J = [rand_herm(rng, D, scale=1.0) for _ in range(3)]
+    T = ko.chebyshev_matrices(H, NC)
+    ref = np.array([[[np.trace(T[m] @ J[1] @ T[n] @ J[2] @ T[p] @ J[0]) / D
+                      for p in range(NC)] for m in range(NC)] for n in range(NC)])
+    psi = np.eye(D, dtype=complex)
+    got = ko.kpm_3d(H, J[0], J[1], J[2], NC, psi, psi)
+    assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+def test_oracle_chebyshev_action_ed():
+    """test/chebyshev_action_test.jl:43-60: the action equals the spectral sum."""
+    rng = np.random.default_rng(151)
+    NH, NC, NR, K = 30, 14, 2, 3
+    A = rng.standard_normal((NH, NH)) + 1j * rng.standard_normal((NH, NH))
+    Hd = (A + A.conj().T) / 2
+    Hd /= np.abs(np.linalg.eigvalsh(Hd)).max() / 0.95
+    V = rng.standard_normal((NH, NR)) + 1j * rng.standard_normal((NH, NR))
+    C = rng.standard_normal((NC, K)) + 1j * rng.standard_normal((NC, K))
+    out = ko.chebyshev_action(Hd, V, C)
+    lam, U = np.linalg.eigh(Hd)
+    th = np.arccos(np.clip(lam, -1, 1))
+    for k in range(K):
+        f = np.array([np.sum(C[:, k] * np.cos(np.arange(NC) * t)) for t in th])
+        assert np.abs(out[:, :, k] - U @ (f[:, None] * (U.conj().T @ V))).max() < 1e-8
+
+
+def test_oracle_kpm1d_current_trace():
+    """test/optical_cond_test.jl:278-287: kpm_1d_current with identity probes is
+    Tr[J T_n] / D."""
+    from helpers import rand_herm
+    rng = np.random.default_rng(2)
+    D, NC = 14, 10
+    H = rand_herm(rng, D)
+    J = rand_herm(rng, D, scale=1.0)
+    T = ko.chebyshev_matrices(H, NC)
+    ref = np.array([np.trace(J @ T[n]) / D for n in range(NC)])
+    mu = ko.kpm_1d_current(H, J, NC, np.eye(D, dtype=complex)).sum(axis=0) / D
+    assert np.linalg.norm(mu - ref) <= 1e-12 * np.linalg.norm(ref)
