@@ -380,9 +380,12 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
   if (opt.workspace_bytes >= 0) {
     budget = (size_t)opt.workspace_bytes;
   } else {
+    // half of the free memory plus what this operator already holds for
+    // kpm_2d (reused, not allocated again)
     size_t fr = 0, tot = 0;
     KPMGB_CUDA(cudaMemGetInfo(&fr, &tot));
-    budget = fr / 2;
+    const size_t held = ws.left.bytes + ws.right.bytes + ws.ring.bytes + ws.gemm.bytes;
+    budget = (fr + held) / 2;
   }
   int64_t KR = opt.right_block > 0 ? opt.right_block : 0;
   int64_t KL = opt.arr_size > 0 ? opt.arr_size : 0;
@@ -514,6 +517,7 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
       c.status = ws.sync.as<unsigned>() + 1;
       c.scratch = ws.gemm.ptr;
       c.scratch_bytes = ws.gemm.bytes;
+      c.reuse_l = n1 > 0;  // same left block as the previous contraction of this rep
       KPMGB_TRY(launch_contract(c, precision, opt.contraction, s));
     }
     if (rep < reps - 1) {

@@ -244,11 +244,26 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
   }
 }
 
-// Zero the padding rows of a plane array (rows nrows..rows_pad-1).
-__global__ void k_zero(uint8_t* p, size_t bytes) {
-  for (size_t i = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) * 16; i < bytes;
-       i += (size_t)gridDim.x * blockDim.x * 16)
-    *reinterpret_cast<uint4*>(p + i) = make_uint4(0, 0, 0, 0);
+// Zero the padding rows nrows..rows_pad-1 of a plane array (every k-tile and
+// digit plane), leaving the rows k_slice writes untouched.
+template <int ROWS>
+__global__ void k_zero_rows(uint8_t* planes, int nrows, int rows_pad, int64_t ktiles) {
+  constexpr uint32_t TILE = ROWS == TC_N ? B_TILE : A_TILE;
+  const int64_t per_row = ktiles * (TC_KT / 8) * TC_SLICES;
+  const int64_t total = (int64_t)(rows_pad - nrows) * per_row;
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int row = nrows + (int)(idx / per_row);
+    int64_t q = idx % per_row;
+    const int i = (int)(q % TC_SLICES);
+    q /= TC_SLICES;
+    const int64_t kt = q / (TC_KT / 8);
+    const int kin = (int)(q % (TC_KT / 8)) * 8;
+    const int tile = row / ROWS, r = row % ROWS;
+    uint8_t* tbase = planes + ((size_t)(tile * ktiles + kt) * TC_SLICES) * TILE;
+    *reinterpret_cast<uint4*>(tbase + (size_t)i * TILE + tile_off<ROWS>(r, kin)) =
+        make_uint4(0, 0, 0, 0);
+  }
 }
 
 // --------------------------------------------------------------- GEMM
@@ -491,50 +506,69 @@ size_t contract_split_scratch_bytes(int64_t K, int nr, int nl) {
   const TcPlan pl = plan_for(K, nr, nl);
   const size_t part_bound = (size_t)(2 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N *
                             sizeof(double);
-  return pl.a_bytes + pl.b_bytes + pl.exp_bytes + std::max(pl.part_bytes, part_bound) + 1024;
+  return pl.a_bytes + pl.b_bytes + 2 * pl.exp_bytes + std::max(pl.part_bytes, part_bound) + 1024;
 }
 
 int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) {
   const TcPlan pl = plan_for(a.K, a.nr, a.nl);
   const size_t part_bound =
       (size_t)(2 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N * sizeof(double);
-  const size_t need = pl.a_bytes + pl.b_bytes + pl.exp_bytes +
+  const size_t need = pl.a_bytes + pl.b_bytes + 2 * pl.exp_bytes +
                       std::max(pl.part_bytes, part_bound) + 1024;
   if (need > a.scratch_bytes) return fail(KPMGB_ERR_ALLOC, "split contraction scratch too small");
   if (!a.status) return fail(KPMGB_ERR_ARGUMENT, "split contraction needs a status word");
+  // Layout: the L (B) planes and exponents first, at offsets that depend only
+  // on (K, nl), so a caller contracting several right blocks against the same
+  // left block (a.reuse_l) skips re-slicing L; then the R (A) planes.
   uint8_t* base = static_cast<uint8_t*>(a.scratch);
   base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(base) + 1023) & ~uintptr_t(1023));
-  uint8_t* A = base;
-  uint8_t* B = A + pl.a_bytes;
-  int* expA = reinterpret_cast<int*>(B + pl.b_bytes);
-  int* expB = expA + a.nr;
+  uint8_t* B = base;
+  int* expB = reinterpret_cast<int*>(B + pl.b_bytes);
+  uint8_t* A = reinterpret_cast<uint8_t*>(expB) + pl.exp_bytes;
+  int* expA = reinterpret_cast<int*>(A + pl.a_bytes);
   double* part = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(expA) + pl.exp_bytes);
   const bool ff = precision == KPMGB_PREC_FF;
-  // exponents
-  if (ff) {
-    k_vec_exp<true><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
-    k_vec_exp<true><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
-  } else {
-    k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
-    k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
-  }
-  KPMGB_LAUNCHED();
-  // digit planes (padding rows zeroed first)
   const int rowsA = pl.mtiles * TC_M, rowsB = pl.ntiles * TC_N;
-  if (rowsA > a.nr || rowsB > 2 * a.nl) {
-    k_zero<<<2048, 256, 0, s>>>(A, pl.a_bytes + pl.b_bytes);
-    KPMGB_LAUNCHED();
-  }
   const int64_t groupsA = (int64_t)a.nr * pl.ktiles * (TC_KT / 8);
   const int64_t groupsB = (int64_t)a.nl * pl.ktiles * (TC_KT / 8);
   const int gA = (int)std::min<int64_t>((groupsA + 255) / 256, 65535 * 16);
   const int gB = (int)std::min<int64_t>((groupsB + 255) / 256, 65535 * 16);
+  auto zero_grid = [&](int64_t rows) {
+    const int64_t n = rows * pl.ktiles * (TC_KT / 8) * TC_SLICES;
+    return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 65535 * 16));
+  };
+  if (!a.reuse_l) {
+    if (ff) {
+      k_vec_exp<true><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
+    } else {
+      k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
+    }
+    KPMGB_LAUNCHED();
+    if (rowsB > 2 * a.nl) {
+      k_zero_rows<TC_N><<<zero_grid(rowsB - 2 * a.nl), 256, 0, s>>>(B, 2 * a.nl, rowsB, pl.ktiles);
+      KPMGB_LAUNCHED();
+    }
+    if (ff) {
+      k_slice<true, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
+    } else {
+      k_slice<false, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
+    }
+    KPMGB_LAUNCHED();
+  }
+  if (ff) {
+    k_vec_exp<true><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
+  } else {
+    k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
+  }
+  KPMGB_LAUNCHED();
+  if (rowsA > a.nr) {
+    k_zero_rows<TC_M><<<zero_grid(rowsA - a.nr), 256, 0, s>>>(A, a.nr, rowsA, pl.ktiles);
+    KPMGB_LAUNCHED();
+  }
   if (ff) {
     k_slice<true, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A);
-    k_slice<true, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
   } else {
     k_slice<false, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A);
-    k_slice<false, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
   }
   KPMGB_LAUNCHED();
   // GEMM

@@ -224,6 +224,8 @@ struct ContractArgs {
   unsigned* status = nullptr;  // device status word (bounded-wait expiry)
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
+  bool reuse_l = false;   // L (and scratch) unchanged since the previous call:
+                          // the split form keeps its L digit planes
 };
 int launch_contract(const ContractArgs& a, int precision, int contraction,
                     cudaStream_t s);

@@ -30,6 +30,12 @@ namespace step {
 #ifndef KPMGB_FF_MIN_BLOCKS
 #define KPMGB_FF_MIN_BLOCKS 2
 #endif
+#ifndef KPMGB_FF_PREFETCH
+#define KPMGB_FF_PREFETCH 0
+#endif
+#ifndef KPMGB_FF_SMEM_ACC
+#define KPMGB_FF_SMEM_ACC 0
+#endif
 #ifndef KPMGB_FF_MIN_BLOCKS_NARROW_REAL
 #define KPMGB_FF_MIN_BLOCKS_NARROW_REAL 3
 #endif
@@ -359,6 +365,11 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
   const float alpha = (float)p.alpha;
   const int beta_mode = p.beta == 0.0 ? 0 : (p.beta > 0.0 ? 1 : -1);
 
+  // FP64 dot accumulators: in registers, or (KPMGB_FF_SMEM_ACC, up to two
+  // columns per lane) in a thread-private shared-memory slot, which frees
+  // 16 registers in the row loop
+  constexpr bool kSmemAcc = KPMGB_FF_SMEM_ACC && ND > 0 && CPL <= 2;
+  __shared__ double2 sacc[kSmemAcc ? kThreads : 1][NDA * CPL];
   double2 d[NDA][CPL];
   float dS[NDA][CPL][2], dC[NDA][CPL][2];
 #pragma unroll
@@ -366,15 +377,40 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
 #pragma unroll
     for (int c = 0; c < CPL; ++c) {
       d[k][c] = make_double2(0.0, 0.0);
+      if constexpr (kSmemAcc) sacc[threadIdx.x][k * CPL + c] = make_double2(0.0, 0.0);
       dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
     }
   int rows_since_flush = 0;
 
   const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+#if KPMGB_FF_PREFETCH
+  // row bounds of the next row of this lane group are loaded one row ahead,
+  // taking the row-pointer load off the dependent chain of every row
+  int nk0 = 0, nk1 = 0;
+  {
+    const int64_t r0 = (int64_t)blockIdx.x * GROUPS + g;
+    if (blockIdx.x < ntiles && r0 < p.NH) {
+      nk0 = __ldg(p.rowptr + r0);
+      nk1 = __ldg(p.rowptr + r0 + 1);
+    }
+  }
+#endif
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int64_t r = t * GROUPS + g;
+#if KPMGB_FF_PREFETCH
+    const int k0 = nk0, k1 = nk1;
+    {
+      const int64_t rn = r + (int64_t)gridDim.x * GROUPS;
+      if (t + gridDim.x < ntiles && rn < p.NH) {
+        nk0 = __ldg(p.rowptr + rn);
+        nk1 = __ldg(p.rowptr + rn + 1);
+      }
+    }
+    if (r >= p.NH) continue;
+#else
     if (r >= p.NH) continue;
     const int k0 = __ldg(p.rowptr + r), k1 = __ldg(p.rowptr + r + 1);
+#endif
     float Sr[CPL], Cr[CPL], Si[CPL], Ci[CPL];
 #pragma unroll
     for (int c = 0; c < CPL; ++c) Sr[c] = Cr[c] = Si[c] = Ci[c] = 0.f;
@@ -466,8 +502,15 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
         for (int k = 0; k < ND; ++k)
 #pragma unroll
           for (int c = 0; c < CPL; ++c) {
-            d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
-            d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
+            if constexpr (kSmemAcc) {
+              double2 v = sacc[threadIdx.x][k * CPL + c];
+              v.x += ff::join(dS[k][c][0], dC[k][c][0]);
+              v.y += ff::join(dS[k][c][1], dC[k][c][1]);
+              sacc[threadIdx.x][k * CPL + c] = v;
+            } else {
+              d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
+              d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
+            }
             dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
           }
       }
@@ -478,6 +521,7 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
     for (int k = 0; k < ND; ++k)
 #pragma unroll
       for (int c = 0; c < CPL; ++c) {
+        if constexpr (kSmemAcc) d[k][c] = sacc[threadIdx.x][k * CPL + c];
         d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
         d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
       }
