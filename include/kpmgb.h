@@ -87,8 +87,11 @@ typedef struct kpmgb_kpm1d_options {
                               the register-gather shapes (and the TMA-fed
                               kernel where it applies) once per (NR,
                               precision, path) on this operator and reuse the
-                              fastest.  Automatic selection (0) is the
-                              register-gather kernel with the default shape. */
+                              fastest; 5: software-pipelined float-float
+                              kernel (cp.async neighbour staging, 17..64
+                              columns, at most 8 nonzeros per row).
+                              Automatic selection (0) is the register-gather
+                              kernel with the default shape.                  */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <vector>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <mutex>
 #include <unordered_map>
@@ -102,6 +103,55 @@ int blocks_per_sm(KernelFn fn) {
   return per_sm;
 }
 
+// Step kernels launch with programmatic stream serialization (see pdl_enter)
+// on created streams; KPMGB_PDL=0 in the environment turns it off.
+int launch_step_kernel(KernelFn fn, int G, cudaStream_t s, const KParams& p,
+                       int threads = kThreads, size_t smem = 0) {
+  static const bool on = [] {
+    const char* e = std::getenv("KPMGB_PDL");
+    return !(e && e[0] == '0');
+  }();
+  if (!on || s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) {
+    fn<<<G, threads, smem, s>>>(p);
+    KPMGB_LAUNCHED();
+    return KPMGB_OK;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)G);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  KPMGB_CUDA(cudaLaunchKernelEx(&cfg, fn, p));
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+int pipe_grid(const PipeGeom& g, int64_t NH) {
+  static std::mutex m;
+  static std::unordered_map<const void*, int> cache;
+  int per_sm = 1;
+  {
+    std::lock_guard<std::mutex> lk(m);
+    auto it = cache.find((const void*)g.fn);
+    if (it != cache.end()) {
+      per_sm = it->second;
+    } else {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.fn, g.threads, g.smem) !=
+          cudaSuccess)
+        per_sm = 1;
+      per_sm = std::max(per_sm, 1);
+      cache.emplace((const void*)g.fn, per_sm);
+    }
+  }
+  const int64_t blocks = (NH + g.rows_per_block - 1) / g.rows_per_block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)per_sm * num_sms()));
+}
+
 int grid_for(KernelFn fn, int64_t NH, int lpr) {
   const int per_sm = blocks_per_sm(fn);
   const int64_t groups = kThreads / lpr;
@@ -134,6 +184,12 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
     if (precision == KPMGB_PREC_FF && ncols >= 32) {
       const int64_t G = std::max<int64_t>(1, std::min<int64_t>(num_sms(), (NH + 3) / 4));
       worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
+    }
+    if (precision == KPMGB_PREC_FF) {
+      for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
+        const PipeGeom g = select_kernel_ffp(ncols, dot, H.is_real != 0, H.max_row_nnz);
+        if (g.fn) worst = std::max(worst, (size_t)pipe_grid(g, NH) * 2 * ncols * sizeof(double2));
+      }
     }
   }
   return worst;
@@ -185,8 +241,15 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
       const Shape sh = pick_shape(p.ncols);
       KernelFn fn = select_kernel_ffg(sh, a.dot, H.is_real != 0);
       const int G = grid_for(fn, a.NH, sh.lpr);
-      fn<<<G, kThreads, 0, s>>>(p);
-      KPMGB_LAUNCHED();
+      KPMGB_TRY(launch_step_kernel(fn, G, s, p));
+      continue;
+    }
+    if (precision == KPMGB_PREC_FF && a.variant == 5) {
+      const PipeGeom g = select_kernel_ffp(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz);
+      if (!g.fn)
+        return fail(KPMGB_ERR_ARGUMENT, "the pipelined kernel serves float-float steps with "
+                                        "17..64 columns and at most 8 nonzeros per row");
+      KPMGB_TRY(launch_step_kernel(g.fn, pipe_grid(g, a.NH), s, p, g.threads, g.smem));
       continue;
     }
     // The TMA-fed kernel serves float-float steps with at least one warp of
@@ -215,8 +278,7 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     const Shape sh = shape_for(a, p.ncols);
     KernelFn fn = select_kernel(sh, precision, a.dot, H.is_real != 0);
     const int G = grid_for(fn, a.NH, sh.lpr);
-    fn<<<G, kThreads, 0, s>>>(p);
-    KPMGB_LAUNCHED();
+    KPMGB_TRY(launch_step_kernel(fn, G, s, p));
   }
   return KPMGB_OK;
 }
@@ -232,6 +294,9 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
   for (const Shape& c : candidate_shapes(a0.NR)) cands.push_back({1, c.lpr * 10 + c.cpl});
   if (precision == KPMGB_PREC_FF && a0.NR >= 32 && tma_chmax(a0.H->max_row_nnz) > 0)
     cands.push_back({2, 0});
+  if (precision == KPMGB_PREC_FF &&
+      select_kernel_ffp(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz).fn)
+    cands.push_back({5, 0});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   KPMGB_CUDA(cudaEventCreate(&e0));
   cudaError_t ce = cudaEventCreate(&e1);

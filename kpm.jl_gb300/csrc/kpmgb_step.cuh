@@ -51,6 +51,15 @@ struct FFTune {
                            : KPMGB_FF_CHUNK_CPL1);
 };
 
+// Programmatic dependent launch: a step kernel waits for the previous kernel
+// of the stream (whose outputs are its inputs) to complete and flush, and at
+// once allows the next one to begin launching, so launch latency overlaps the
+// tail of the running step.  Without the launch attribute both are no-ops.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kMaxCols = 128;  // columns per launch (larger NR runs in batches)
@@ -222,6 +231,7 @@ __device__ __forceinline__ void cdot(double2& acc, double2 a, double2 b) {
 
 template <int LPR, int CPL, bool REALH, int DOT>
 __global__ void __launch_bounds__(kThreads) k_step_f64(KParams p) {
+  pdl_enter();
   constexpr int ND = NDots<DOT>::value;
   constexpr int GROUPS = kThreads / LPR;
   using HV = typename F64Val<REALH>::T;
@@ -351,6 +361,7 @@ constexpr int kFlushRows = 16;  // per-lane float accumulators fold into FP64 th
 
 template <int LPR, int CPL, bool REALH, int DOT, int CH>
 __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_step_ff(KParams p) {
+  pdl_enter();
   constexpr int ND = NDots<DOT>::value;
   constexpr int NDA = ND > 0 ? ND : 1;
   constexpr int GROUPS = kThreads / LPR;
@@ -580,6 +591,16 @@ KernelFn select_kernel_ffg(Shape s, int dot, bool real);
 
 struct TmaGeom;
 int tma_chmax(int max_row_nnz);
+
+// Software-pipelined float-float kernel (kpmgb_step_ffp.cu): 17..64 columns,
+// rows of at most 8 nonzeros; fn == nullptr when it does not serve the shape.
+struct PipeGeom {
+  KernelFn fn;
+  int threads;
+  size_t smem;
+  int rows_per_block;
+};
+PipeGeom select_kernel_ffp(int ncols, int dot, bool real, int max_row_nnz);
 
 }  // namespace step
 }  // namespace kpmgb

@@ -85,6 +85,7 @@ __device__ __forceinline__ void gnorm2(float (&A)[2], float (&C)[2], float4 a) {
 
 template <int LPR, int CPL, bool REALH, int DOT>
 __global__ void __launch_bounds__(kThreads, KPMGB_FF_MIN_BLOCKS) k_step_ffg(KParams p) {
+  pdl_enter();
   constexpr int CH = KPMGB_FFG_CHUNK;
   constexpr int ND = NDots<DOT>::value;
   static_assert(ND > 0, "the maxima-anchored kernel serves the moment steps");

@@ -320,3 +320,41 @@ def test_autotuned_kernel_matches_oracle(prec, NR):
     lr = kg.kpm_1d(op, 33, NR, psi_in_l=psi, psi_in_r=psi, avg_output=False, precision=prec,
                    kernel="tune")
     assert relerr(lr, ko.kpm_1d_lr(H, 33, psi, psi)) < TOL[prec]
+
+
+def _peierls_square(L, rng):
+    """Complex Hermitian square lattice (5 nonzeros per row)."""
+    H = models.square_anderson(L, W=1.5, rng=rng).tocoo()
+    ph = np.exp(1j * 0.37 * (H.row - H.col))
+    return sp.csc_matrix((H.data * ph, (H.row, H.col)), shape=H.shape) / 4.9
+
+
+@pytest.mark.parametrize("NR", [17, 32, 33, 40, 64])
+@pytest.mark.parametrize("lr", [False, True])
+@pytest.mark.parametrize("complex_h", [False, True])
+def test_pipelined_kernel_matches_oracle(NR, lr, complex_h):
+    rng = np.random.default_rng(NR + 7)
+    if complex_h:
+        H = _peierls_square(20, rng)
+    else:
+        H = (models.cubic_anderson(8, W=4.0, rng=rng) / 8.2).tocsc()
+    NH = H.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    if lr:
+        psr = ko.random_phase_vectors(rng, NH, NR)
+        got = kg.kpm_1d(H, 41, NR, psi_in_l=psi, psi_in_r=psr, avg_output=False,
+                        precision="ff", kernel="pipelined")
+        ref = ko.kpm_1d_lr(H, 41, psi, psr)
+    else:
+        got = kg.kpm_1d(H, 96, NR, psi_in=psi, avg_output=False, precision="ff",
+                        kernel="pipelined")
+        ref = ko.kpm_1d_doubling(H, 96, psi)
+    assert relerr(got, ref) < TOL["ff"]
+
+
+def test_pipelined_kernel_rejects_unserved_shapes():
+    rng = np.random.default_rng(1)
+    H = (models.cubic_anderson(6, W=1.0, rng=rng) / 7.0).tocsc()
+    psi = ko.random_phase_vectors(rng, 216, 8)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(H, 16, 8, psi_in=psi, precision="ff", kernel="pipelined")
