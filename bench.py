@@ -257,11 +257,13 @@ def workload_c1(args):
     out = {"workload": "c1: kpm_1d, 2D square Anderson L=64 (NH=4096), W=2, NC=1024, NR=12",
            "metric": METRIC, "unit": UNIT}
     for prec in ("fp64", "ff"):
-        for graph in (False, True):
+        for mode in ("launches", "graph", "single"):
             ms = _time_device(lambda: kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec,
-                                                       stream=s, use_graph=graph),
+                                                       stream=s, use_graph=mode == "graph",
+                                                       kernel="single" if mode == "single"
+                                                       else "auto"),
                               s, args.warmup, max(args.steps, 10), lambda: kg.sync(op, s))
-            out[f"{prec}{'_graph' if graph else ''}"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+            out[f"{prec}_{mode}"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
     ms_h = _time_host(lambda: kg.kpm_1d(op, NC, NR, psi_in=psi, use_graph=True), 2, 10)
     out["e2e_fp64_graph"] = {"ms_per_call": ms_h, "value": vs / (ms_h / 1e3)}
     nt = cpu_port.max_threads()

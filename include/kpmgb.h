@@ -89,9 +89,11 @@ typedef struct kpmgb_kpm1d_options {
                               precision, path) on this operator and reuse the
                               fastest; 5: software-pipelined float-float
                               kernel (cp.async neighbour staging, 17..64
-                              columns, at most 8 nonzeros per row).
-                              Automatic selection (0) is the register-gather
-                              kernel with the default shape.                  */
+                              columns, at most 8 nonzeros per row); 6: the
+                              whole recurrence in one cooperative launch with
+                              a grid barrier per step (small operators,
+                              NR <= 256).  Automatic selection (0) is the
+                              register-gather kernel with the default shape. */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {

@@ -198,6 +198,15 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
     KPMGB_TRY(launch_colmax(sl[0], NH, (int)NR, ring(0), s));
     if (lr) KPMGB_TRY(launch_colmax(ws.bra.ptr, NH, (int)NR, bmax, s));
   }
+  // kernel_variant 6: the whole recurrence in one cooperative launch
+  if (o && o->kernel_variant == 6) {
+    KPMGB_TRY(ws.partials.ensure(std::max(ws.partials.bytes, small_partials_bytes((int)NR))));
+    KPMGB_CUDA(cudaMemsetAsync(ws.sync.as<unsigned>() + 2, 0, 2 * sizeof(unsigned), s));
+    return launch_kpm1d_small(op->csr, NH, (int)NR, NC, lr, precision, sl[0], sl[1],
+                              lr ? ws.bra.ptr : nullptr, mu, mom_scale,
+                              (!lr && o->stability_check) ? 2.25 : 0.0, ws.partials.ptr,
+                              ws.partials.bytes, ws.sync.as<unsigned>(), s);
+  }
   // kernel_variant 4: time the candidate kernels once per (NR, precision,
   // path) on this operator with the first recurrence step, then reuse.
   int chosen_variant = o ? o->kernel_variant : 0, chosen_shape = 0;

@@ -358,3 +358,34 @@ def test_pipelined_kernel_rejects_unserved_shapes():
     psi = ko.random_phase_vectors(rng, 216, 8)
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d(H, 16, 8, psi_in=psi, precision="ff", kernel="pipelined")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+@pytest.mark.parametrize("NR", [1, 5, 12, 64, 200, 256])
+@pytest.mark.parametrize("lr", [False, True])
+def test_single_launch_kernel_matches_oracle(prec, NR, lr):
+    """kernel variant 6: the whole recurrence in one cooperative launch"""
+    rng = np.random.default_rng(3 * NR + lr)
+    H = _peierls_square(16, rng) if lr else (models.square_anderson(16, W=2.0, rng=rng) / 5.1).tocsc()
+    psi = ko.random_phase_vectors(rng, 256, NR)
+    if lr:
+        psr = ko.random_phase_vectors(rng, 256, NR)
+        got = kg.kpm_1d(H, 37, NR, psi_in_l=psi, psi_in_r=psr, avg_output=False, precision=prec,
+                        kernel="single")
+        ref = ko.kpm_1d_lr(H, 37, psi, psr)
+    else:
+        got = kg.kpm_1d(H, 128, NR, psi_in=psi, avg_output=False, precision=prec, kernel="single")
+        ref = ko.kpm_1d_doubling(H, 128, psi)
+    assert relerr(got, ref) < TOL[prec]
+
+
+def test_single_launch_kernel_growth_and_limits():
+    rng = np.random.default_rng(2)
+    H = (models.square_anderson(12, W=0.0, rng=rng) / 3.0).tocsc()   # spectrum beyond [-1, 1]
+    psi = ko.random_phase_vectors(rng, 144, 4)
+    with pytest.raises(kg.KPMNumericalError):
+        kg.kpm_1d(H, 64, 4, psi_in=psi, kernel="single", stability_check=True)
+    ok = (models.square_anderson(12, W=0.0, rng=rng) / 4.4).tocsc()
+    kg.kpm_1d(ok, 64, 4, psi_in=psi, kernel="single", stability_check=True)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(ok, 16, 257, psi_in=ko.random_phase_vectors(rng, 144, 257), kernel="single")
