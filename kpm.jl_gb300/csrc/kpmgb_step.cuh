@@ -357,7 +357,11 @@ __device__ __forceinline__ void ffnorm2(float (&S)[2], float (&C)[2], float4 a) 
   ff::dacc(S[0], C[0], a.z, a.w, a.z, a.w);
 }
 
-constexpr int kFlushRows = 16;  // per-lane float accumulators fold into FP64 this often
+#ifndef KPMGB_FF_FLUSH_ROWS
+#define KPMGB_FF_FLUSH_ROWS 16
+#endif
+// per-lane float-float dot accumulators fold into FP64 every this many rows
+constexpr int kFlushRows = KPMGB_FF_FLUSH_ROWS;
 
 template <int LPR, int CPL, bool REALH, int DOT, int CH>
 __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_step_ff(KParams p) {
