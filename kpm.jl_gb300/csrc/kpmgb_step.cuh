@@ -49,6 +49,11 @@ struct FFTune {
       CPL >= 3 ? 4
                : (CPL == 2 ? (REALH ? KPMGB_FF_CHUNK_CPL2_REAL : KPMGB_FF_CHUNK_CPL2)
                            : KPMGB_FF_CHUNK_CPL1);
+  // a row's last chunk with its exact length: measured on GB300 a gain for
+  // complex operators (Haldane, 10 nonzeros: chunks 8 + 2 instead of 8 + 8,
+  // c3 kpm_2d 352 -> 335 ms) and a loss for the real 3-block kernel (3D
+  // Anderson, chunks 4 + 3: 33% -> 29% of HBM), so it applies to complex H
+  static constexpr bool exact_tail = !REALH;
 };
 
 // Programmatic dependent launch: a step kernel waits for the previous kernel
@@ -363,6 +368,83 @@ __device__ __forceinline__ void ffnorm2(float (&S)[2], float (&C)[2], float4 a) 
 // per-lane float-float dot accumulators fold into FP64 every this many rows
 constexpr int kFlushRows = KPMGB_FF_FLUSH_ROWS;
 
+#ifndef KPMGB_FF_EXACT_TAIL
+#define KPMGB_FF_EXACT_TAIL 1
+#endif
+
+// One chunk of exactly N nonzeros of a row for the CPL columns of this lane:
+// gathers, the chunk anchor (|partial sums| <= R*M, accumulator started at
+// 1.5 * 2^E with 2^E = 4P, P <= R*M (1 + tiny) < 2P, so every partial sum
+// stays inside one binade), anchored products, and the TwoSum merge into the
+// row sums.  A row's last chunk runs with its exact length (no padded slots).
+template <int N, int LPR, int CPL, bool REALH>
+__device__ __forceinline__ void ff_chunk(const KParams& p,
+                                         const typename FFVal<REALH>::T* __restrict__ val,
+                                         const float4* __restrict__ x, int kc, int lg, bool first,
+                                         float (&Sr)[CPL], float (&Cr)[CPL], float (&Si)[CPL],
+                                         float (&Ci)[CPL]) {
+  using HV = typename FFVal<REALH>::T;
+  int jj[N];
+  HV hv[N];
+  float R = 0.f;
+#pragma unroll
+  for (int u = 0; u < N; ++u) {
+    jj[u] = __ldg(p.col + kc + u);
+    hv[u] = __ldg(val + kc + u);
+    R = __fadd_rn(R, habs(hv[u]));
+  }
+  float4 xv[CPL][N];
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) {
+    const int cc = lg + c * LPR;
+#pragma unroll
+    for (int u = 0; u < N; ++u)
+      xv[c][u] = cc < p.ncols ? __ldg(x + (int64_t)jj[u] * p.ld + p.c0 + cc)
+                              : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) {
+    float M = 0.f;
+#pragma unroll
+    for (int u = 0; u < N; ++u) M = fmaxf(M, fmaxf(fabsf(xv[c][u].x), fabsf(xv[c][u].z)));
+    const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+    const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+    float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+    for (int u = 0; u < N; ++u) ffmac(Ar, cr, Ai, ci, hv[u], xv[c][u]);
+    const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+    if (first) {
+      Sr[c] = sr;
+      Cr[c] = cr;
+      Si[c] = si;
+      Ci[c] = ci;
+    } else {
+      float s, e;
+      ff::two_sum(Sr[c], sr, s, e);
+      Sr[c] = s;
+      Cr[c] = __fadd_rn(Cr[c], __fadd_rn(cr, e));
+      ff::two_sum(Si[c], si, s, e);
+      Si[c] = s;
+      Ci[c] = __fadd_rn(Ci[c], __fadd_rn(ci, e));
+    }
+  }
+}
+
+// ff_chunk with a run-time length 1..N (uniform within a lane group).
+template <int N, int LPR, int CPL, bool REALH>
+__device__ __forceinline__ void ff_chunk_n(int cnt, const KParams& p,
+                                           const typename FFVal<REALH>::T* __restrict__ val,
+                                           const float4* __restrict__ x, int kc, int lg,
+                                           bool first, float (&Sr)[CPL], float (&Cr)[CPL],
+                                           float (&Si)[CPL], float (&Ci)[CPL]) {
+  if constexpr (N >= 1) {
+    if (cnt == N)
+      ff_chunk<N, LPR, CPL, REALH>(p, val, x, kc, lg, first, Sr, Cr, Si, Ci);
+    else
+      ff_chunk_n<N - 1, LPR, CPL, REALH>(cnt, p, val, x, kc, lg, first, Sr, Cr, Si, Ci);
+  }
+}
+
 template <int LPR, int CPL, bool REALH, int DOT, int CH>
 __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_step_ff(KParams p) {
   pdl_enter();
@@ -429,61 +511,68 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
     float Sr[CPL], Cr[CPL], Si[CPL], Ci[CPL];
 #pragma unroll
     for (int c = 0; c < CPL; ++c) Sr[c] = Cr[c] = Si[c] = Ci[c] = 0.f;
-    for (int kc = k0; kc < k1; kc += CH) {
-      const int cnt = min(CH, k1 - kc);
-      int jj[CH];
-      HV hv[CH];
-      float R = 0.f;
-#pragma unroll
-      for (int u = 0; u < CH; ++u) {
-        if (u < cnt) {
-          jj[u] = __ldg(p.col + kc + u);
-          hv[u] = __ldg(val + kc + u);
-        } else {
-          jj[u] = 0;
-          hzero(hv[u]);
-        }
-        R = __fadd_rn(R, habs(hv[u]));
+    if constexpr (KPMGB_FF_EXACT_TAIL && FFTune<CPL, REALH>::exact_tail) {
+      for (int kc = k0; kc < k1; kc += CH) {
+        const int cnt = min(CH, k1 - kc);
+        ff_chunk_n<CH, LPR, CPL, REALH>(cnt, p, val, x, kc, lg, kc == k0, Sr, Cr, Si, Ci);
       }
-      float4 xv[CPL][CH];
-#pragma unroll
-      for (int c = 0; c < CPL; ++c) {
-        const int cc = lg + c * LPR;
+    } else {
+      for (int kc = k0; kc < k1; kc += CH) {
+        const int cnt = min(CH, k1 - kc);
+        int jj[CH];
+        HV hv[CH];
+        float R = 0.f;
 #pragma unroll
         for (int u = 0; u < CH; ++u) {
-          if (u < cnt && cc < p.ncols)
-            xv[c][u] = __ldg(x + (int64_t)jj[u] * p.ld + p.c0 + cc);
-          else
-            xv[c][u] = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (u < cnt) {
+            jj[u] = __ldg(p.col + kc + u);
+            hv[u] = __ldg(val + kc + u);
+          } else {
+            jj[u] = 0;
+            hzero(hv[u]);
+          }
+          R = __fadd_rn(R, habs(hv[u]));
         }
-      }
+        float4 xv[CPL][CH];
 #pragma unroll
-      for (int c = 0; c < CPL; ++c) {
-        float M = 0.f;
+        for (int c = 0; c < CPL; ++c) {
+          const int cc = lg + c * LPR;
 #pragma unroll
-        for (int u = 0; u < CH; ++u) M = fmaxf(M, fmaxf(fabsf(xv[c][u].x), fabsf(xv[c][u].z)));
-        // |partial sums| <= R*M (1 + tiny); anchor at 1.5 * 2^E with 2^E = 4P,
-        // P <= bound < 2P, so every partial sum stays inside the binade.
-        const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
-        const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
-        float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+          for (int u = 0; u < CH; ++u) {
+            if (u < cnt && cc < p.ncols)
+              xv[c][u] = __ldg(x + (int64_t)jj[u] * p.ld + p.c0 + cc);
+            else
+              xv[c][u] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
 #pragma unroll
-        for (int u = 0; u < CH; ++u)
-          if (u < cnt) ffmac(Ar, cr, Ai, ci, hv[u], xv[c][u]);
-        const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
-        if (kc == k0) {
-          Sr[c] = sr;
-          Cr[c] = cr;
-          Si[c] = si;
-          Ci[c] = ci;
-        } else {
-          float s, e;
-          ff::two_sum(Sr[c], sr, s, e);
-          Sr[c] = s;
-          Cr[c] = __fadd_rn(Cr[c], __fadd_rn(cr, e));
-          ff::two_sum(Si[c], si, s, e);
-          Si[c] = s;
-          Ci[c] = __fadd_rn(Ci[c], __fadd_rn(ci, e));
+        for (int c = 0; c < CPL; ++c) {
+          float M = 0.f;
+#pragma unroll
+          for (int u = 0; u < CH; ++u) M = fmaxf(M, fmaxf(fabsf(xv[c][u].x), fabsf(xv[c][u].z)));
+          // |partial sums| <= R*M (1 + tiny); anchor at 1.5 * 2^E with 2^E = 4P,
+          // P <= bound < 2P, so every partial sum stays inside the binade.
+          const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+          const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+          float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+          for (int u = 0; u < CH; ++u)
+            if (u < cnt) ffmac(Ar, cr, Ai, ci, hv[u], xv[c][u]);
+          const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+          if (kc == k0) {
+            Sr[c] = sr;
+            Cr[c] = cr;
+            Si[c] = si;
+            Ci[c] = ci;
+          } else {
+            float s, e;
+            ff::two_sum(Sr[c], sr, s, e);
+            Sr[c] = s;
+            Cr[c] = __fadd_rn(Cr[c], __fadd_rn(cr, e));
+            ff::two_sum(Si[c], si, s, e);
+            Si[c] = s;
+            Ci[c] = __fadd_rn(Ci[c], __fadd_rn(ci, e));
+          }
         }
       }
     }
