@@ -175,7 +175,7 @@ int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
  * member i (seg[0] = 0, seg[nseg] = NH) and H must not couple members.  psi:
  * host NH x NR column-major (member i's probes are its rows); mu_all: host,
  * member i's NR x NC column-major moments at offset i*NR*NC complex values.
- * 1 <= NR <= 32.  Blocking call. */
+ * Probe columns run in batches of 32 (one launch per batch).  Blocking call. */
 int kpmgb_kpm1d_ensemble(kpmgb_operator H, int32_t nseg, const int64_t* seg,
                          int64_t NC, int64_t NR, const double* psi,
                          double* mu_all, const kpmgb_kpm1d_options* opts);
@@ -245,8 +245,9 @@ int kpmgb_dos(const double* mu, int64_t NC, double a, double b,
  * checkpoint_every <= 0 picks the spacing: every vector stays resident
  * (a single forward pass) when that fits in half of the free device memory,
  * else the spacing shrinks towards sqrt(NC/2).
- * FP64, 1 <= NR <= 32, NC even >= 4.  No reference counterpart (the
- * reference differentiates through ForwardDiff duals).  Blocking call. */
+ * FP64, probe columns processed in batches of 32, NC even >= 4.  No
+ * reference counterpart (the reference differentiates through ForwardDiff
+ * duals).  Blocking call. */
 int kpmgb_kpm1d_grad(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,
                      const double* psi, const double* g,
                      int64_t checkpoint_every, double* grad);

@@ -153,12 +153,15 @@ int adjoint_forward_step(const DeviceCSR& H, int64_t NH, int NR, const void* x, 
   return launch_step(a, KPMGB_PREC_FP64, s);
 }
 
-// Gradient driver.  psi_rowmajor: FP64 row-major probes; g[0..NC) host
-// weights; C: checkpoint spacing.  Writes conj(G) per stored entry in the
-// caller's CSC order.
+// Gradient driver for one batch of at most 32 probe columns.
+// psi_rowmajor: FP64 row-major probes; g[0..NC) host weights; C: checkpoint
+// spacing; inv: 1 / total probe count.  The first batch clears the CSR-order
+// accumulator, the last writes conj(G) per stored entry in the caller's CSC
+// order.
 int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, int64_t NH,
                    const double2* psi_rowmajor, const double* g, int64_t C, double2* d_grad_csr,
-                   double2* d_grad_csc, DevBuf& work, cudaStream_t s) {
+                   double2* d_grad_csc, DevBuf& work, cudaStream_t s, double inv, bool first,
+                   bool last) {
   const int64_t N = NC / 2;
   const size_t blk = (size_t)NH * NR * sizeof(double2);
   auto need_for = [&](int64_t c) { return (2 * ((N + c - 1) / c) + (c + 2) + 3) * blk; };
@@ -213,8 +216,8 @@ int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, in
   auto Gw = [&](int64_t m) { return (m >= 0 && m < NC) ? g[m] : 0.0; };
   double c1 = Gw(1);
   for (int64_t m = 1; m <= N - 1; ++m) c1 -= Gw(2 * m + 1);
-  const double inv = 1.0 / NR;
-  KPMGB_CUDA(cudaMemsetAsync(d_grad_csr, 0, (size_t)H.nnz * sizeof(double2), s));
+  // inv: 1 / (total probe count); column batches accumulate into d_grad_csr
+  if (first) KPMGB_CUDA(cudaMemsetAsync(d_grad_csr, 0, (size_t)H.nnz * sizeof(double2), s));
   auto base_params = [&]() {
     AdjParams p{};
     p.rowptr = H.rowptr;
@@ -264,6 +267,7 @@ int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, in
     KPMGB_TRY(launch_adj(q, s));
   }
   const int blocks = (int)std::min<int64_t>((H.nnz + 255) / 256, 4096);
+  if (!last) return KPMGB_OK;
   k_scatter_grad<<<std::max(blocks, 1), 256, 0, s>>>(d_grad_csr, d_perm, H.nnz, d_grad_csc);
   KPMGB_LAUNCHED();
   return KPMGB_OK;

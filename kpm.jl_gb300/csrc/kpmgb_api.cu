@@ -782,7 +782,7 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
   if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   if (nseg < 1 || !seg || !psi || !mu_all) return fail(KPMGB_ERR_ARGUMENT, "invalid ensemble arguments");
   if (NC < 2 || NC % 2 != 0) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be even.");
-  if (NR < 1 || NR > 32) return fail(KPMGB_ERR_ARGUMENT, "the ensemble path supports 1 <= NR <= 32");
+  if (NR < 1) return fail(KPMGB_ERR_ARGUMENT, "NR must be positive");
   const int precision = opts ? opts->precision : KPMGB_PREC_FP64;
   KPMGB_TRY(check_precision(precision));
   Operator* op = as_op(h);
@@ -802,11 +802,15 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
   Guard g(op);
   cudaStream_t s = op->stream;
   Workspace& ws = op->ws;
-  const size_t slot = (size_t)NH * NR * 16;
+  // probe columns in batches of at most 32 (one lane per column in the
+  // ensemble kernel); the moments of each column are independent
+  constexpr int64_t kBatch = 32;
+  const int64_t nb_max = std::min<int64_t>(NR, kBatch);
+  const size_t slot = (size_t)NH * nb_max * 16;
   KPMGB_TRY(ws.psi_in.ensure(slot));
   KPMGB_TRY(ws.slots.ensure(2 * slot));
-  KPMGB_TRY(ws.mu.ensure((size_t)nseg * NC * NR * 16));
-  KPMGB_TRY(ws.scales.ensure((size_t)(3 * NR + 2) * sizeof(double)));
+  KPMGB_TRY(ws.mu.ensure((size_t)nseg * NC * nb_max * 16));
+  KPMGB_TRY(ws.scales.ensure((size_t)(3 * nb_max + 2) * sizeof(double)));
   // segment table + order + work counter in the partials buffer (small)
   const size_t meta = (size_t)(nseg + 1) * sizeof(int64_t) + (size_t)nseg * sizeof(int) + 64;
   KPMGB_TRY(ws.partials.ensure(std::max(meta, ws.partials.bytes)));
@@ -819,22 +823,27 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
                              cudaMemcpyHostToDevice, s));
   KPMGB_CUDA(cudaMemcpyAsync(d_order, order.data(), (size_t)nseg * sizeof(int),
                              cudaMemcpyHostToDevice, s));
-  KPMGB_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned), s));
-  KPMGB_CUDA(cudaMemcpyAsync(ws.psi_in.ptr, psi, slot, cudaMemcpyHostToDevice, s));
   char* slots = ws.slots.as<char>();
   double* sc = ws.scales.as<double>();
   const bool ff = precision == KPMGB_PREC_FF;
-  KPMGB_TRY(launch_load_block(ws.psi_in.ptr, slots, NH, (int)NR, precision, sc, false, s));
-  const double* scale = nullptr;
-  if (ff) {
-    KPMGB_TRY(launch_scale_product(sc, sc, sc + 2 * NR, (int)NR, s));
-    scale = sc + 2 * NR;
+  for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
+    const int nb = (int)std::min<int64_t>(kBatch, NR - c0);
+    const size_t bb = (size_t)NH * nb * 16;
+    KPMGB_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned), s));
+    KPMGB_CUDA(cudaMemcpyAsync(ws.psi_in.ptr, psi + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
+    KPMGB_TRY(launch_load_block(ws.psi_in.ptr, slots, NH, nb, precision, sc, false, s));
+    const double* scale = nullptr;
+    if (ff) {
+      KPMGB_TRY(launch_scale_product(sc, sc, sc + 2 * nb, nb, s));
+      scale = sc + 2 * nb;
+    }
+    KPMGB_TRY(launch_ensemble(op->csr, d_seg, d_order, nseg, nb, NC, slots, slots + bb,
+                              ws.mu.as<double2>(), scale, next, ws.sync.as<unsigned>() + 1,
+                              precision, s));
+    // [nseg][NC][nb] -> columns c0 .. c0+nb of the caller's [nseg][NC][NR]
+    KPMGB_CUDA(cudaMemcpy2DAsync(mu_all + 2 * c0, (size_t)NR * 16, ws.mu.ptr, (size_t)nb * 16,
+                                 (size_t)nb * 16, (size_t)nseg * NC, cudaMemcpyDeviceToHost, s));
   }
-  KPMGB_TRY(launch_ensemble(op->csr, d_seg, d_order, nseg, (int)NR, NC, slots, slots + slot,
-                            ws.mu.as<double2>(), scale, next, ws.sync.as<unsigned>() + 1,
-                            precision, s));
-  KPMGB_CUDA(cudaMemcpyAsync(mu_all, ws.mu.ptr, (size_t)nseg * NC * NR * 16,
-                             cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
 }
 
@@ -842,7 +851,8 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
 namespace kpmgb {
 int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, int64_t NH,
                    const double2* psi_rowmajor, const double* g, int64_t C, double2* d_grad_csr,
-                   double2* d_grad_csc, DevBuf& work, cudaStream_t s);
+                   double2* d_grad_csc, DevBuf& work, cudaStream_t s, double inv, bool first,
+                   bool last);
 }
 
 extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH,
@@ -851,7 +861,7 @@ extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_
   clear_error();
   if (!h || !psi || !g || !grad) return fail(KPMGB_ERR_ARGUMENT, "null argument");
   if (NC < 4 || NC % 2 != 0) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be even and >= 4.");
-  if (NR < 1 || NR > 32) return fail(KPMGB_ERR_ARGUMENT, "the gradient path supports 1 <= NR <= 32");
+  if (NR < 1) return fail(KPMGB_ERR_ARGUMENT, "NR must be positive");
   Operator* op = as_op(h);
   if (NH != op->csr.n) return fail(KPMGB_ERR_ARGUMENT, "psi has %lld rows; the operator has %lld",
                                    (long long)NH, (long long)op->csr.n);
@@ -859,18 +869,27 @@ extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_
   Guard gd(op);
   cudaStream_t s = op->stream;
   Workspace& ws = op->ws;
-  const size_t blk = (size_t)NH * NR * 16;
+  // probe columns in batches of at most 32 (one lane per column in the
+  // adjoint kernel); the gradient is a sum over columns
+  constexpr int64_t kBatch = 32;
+  const int64_t nb_max = std::min<int64_t>(NR, kBatch);
+  const size_t blk = (size_t)NH * nb_max * 16;
   KPMGB_TRY(ws.psi_in.ensure(2 * blk));
   KPMGB_TRY(ws.gemm.ensure(std::max(ws.gemm.bytes, (size_t)2 * op->csr.nnz * 16)));
   KPMGB_TRY(ensure_sync(op, s));
   char* in = ws.psi_in.as<char>();
-  KPMGB_CUDA(cudaMemcpyAsync(in, psi, blk, cudaMemcpyHostToDevice, s));
-  KPMGB_TRY(launch_load_block(in, in + blk, NH, (int)NR, KPMGB_PREC_FP64, nullptr, false, s));
   double2* gcsr = ws.gemm.as<double2>();
   double2* gcsc = gcsr + op->csr.nnz;
-  KPMGB_TRY(run_kpm1d_grad(op->csr, op->csr.perm, NC, (int)NR, NH,
-                           reinterpret_cast<const double2*>(in + blk), g,
-                           checkpoint_every, gcsr, gcsc, ws.split, s));
+  for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
+    const int64_t nb = std::min<int64_t>(kBatch, NR - c0);
+    const size_t bb = (size_t)NH * nb * 16;
+    KPMGB_CUDA(cudaMemcpyAsync(in, psi + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
+    KPMGB_TRY(launch_load_block(in, in + blk, NH, (int)nb, KPMGB_PREC_FP64, nullptr, false, s));
+    KPMGB_TRY(run_kpm1d_grad(op->csr, op->csr.perm, NC, (int)nb, NH,
+                             reinterpret_cast<const double2*>(in + blk), g, checkpoint_every,
+                             gcsr, gcsc, ws.split, s, 1.0 / (double)NR, c0 == 0,
+                             c0 + kBatch >= NR));
+  }
   KPMGB_CUDA(cudaMemcpyAsync(grad, gcsc, (size_t)op->csr.nnz * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
 }

@@ -204,8 +204,11 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
   const int64_t total = (int64_t)nvec * groups;
   for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
-    const int v = (int)(idx / groups);
-    const int64_t g = idx - (int64_t)v * groups;
+    // vector fastest: consecutive threads write consecutive 16-byte rows of
+    // one 8-row core matrix (128 contiguous bytes); each thread reads 64
+    // contiguous bytes of its own vector
+    const int64_t g = idx / nvec;
+    const int v = (int)(idx - g * nvec);
     const int64_t kp0 = g * 8;  // first real K' element
     const int e = exps[v];
     float d[8][TC_SLICES];

@@ -152,6 +152,17 @@ int pipe_grid(const PipeGeom& g, int64_t NH) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)per_sm * num_sms()));
 }
 
+// Columns per step launch: kMaxCols, or fewer through KPMGB_COLS_PER_LAUNCH
+// (a tuning knob: narrower launches give each lane group shorter rows).
+int cols_per_launch() {
+  static const int w = [] {
+    const char* e = std::getenv("KPMGB_COLS_PER_LAUNCH");
+    const int v = e ? std::atoi(e) : kMaxCols;
+    return v >= 1 && v <= kMaxCols ? v : kMaxCols;
+  }();
+  return w;
+}
+
 int grid_for(KernelFn fn, int64_t NH, int lpr) {
   const int per_sm = blocks_per_sm(fn);
   const int64_t groups = kThreads / lpr;
@@ -163,8 +174,9 @@ int grid_for(KernelFn fn, int64_t NH, int lpr) {
 
 size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision) {
   size_t worst = 0;
-  for (int c0 = 0; c0 < NR; c0 += kMaxCols) {
-    const int ncols = std::min(kMaxCols, NR - c0);
+  const int W = cols_per_launch();
+  for (int c0 = 0; c0 < NR; c0 += W) {
+    const int ncols = std::min(W, NR - c0);
     const Shape s = pick_shape(ncols);
     for (const Shape& c : candidate_shapes(ncols))
       for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
@@ -206,7 +218,8 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
                   "float-float recurrence supports alpha = +-2^k and beta in {-1, 0, 1}");
     if (!H.val_ff) return fail(KPMGB_ERR_ARGUMENT, "operator has no float-float values");
   }
-  for (int c0 = 0; c0 < a.NR; c0 += kMaxCols) {
+  const int W = cols_per_launch();
+  for (int c0 = 0; c0 < a.NR; c0 += W) {
     KParams p;
     p.rowptr = H.rowptr;
     p.col = H.col;
@@ -215,7 +228,7 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     p.NH = a.NH;
     p.ld = a.NR;
     p.c0 = c0;
-    p.ncols = std::min(kMaxCols, a.NR - c0);
+    p.ncols = std::min(W, a.NR - c0);
     p.x = a.x;
     p.z = a.z;
     p.y = a.y;

@@ -337,7 +337,8 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     """Doubling moments of many independent members in one persistent launch.
 
     ``Hs``: list of (rescaled) sparse operators of any sizes; ``psis``: list of
-    probe blocks (NH_i, NR) with a common NR <= 32.  Equivalent to
+    probe blocks (NH_i, NR) with a common NR (run in batches of 32 columns).
+    Equivalent to
     ``[kpm_1d(H_i, NC, NR, psi_in=psi_i) for ...]`` (``src/moment.jl:339-492``
     per member).  Returns a list of length-NC real averages, or of (NR, NC)
     matrices with ``avg_output=False``.

@@ -49,3 +49,17 @@ def test_ensemble_validation(built_lib):
         kg.kpm_1d_ensemble(Hs, 63, psis)
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d_ensemble(Hs, 64, [psis[0], psis[1][:, :4]])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_ensemble_column_batches(built_lib, prec):
+    """NR = 40 runs as column batches of 32 + 8."""
+    rng = np.random.default_rng(31)
+    Hs, psis = [], []
+    for _ in range(5):
+        L = int(rng.integers(5, 12))
+        Hs.append((models.square_anderson(L, W=2.0, rng=rng) / 5.1).tocsc())
+        psis.append(ko.random_phase_vectors(rng, L * L, 40))
+    got = kg.kpm_1d_ensemble(Hs, 64, psis, precision=prec, avg_output=False)
+    for H, psi, m in zip(Hs, psis, got):
+        assert relerr(m, ko.kpm_1d_doubling(H, 64, psi)) < TOL[prec]

@@ -134,5 +134,17 @@ def test_grad_argument_errors(built_lib):
         kg.kpm_1d_grad(H, 15, psi, np.zeros(15))
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d_grad(H, 16, psi, np.zeros(12))
-    with pytest.raises(kg.KPMArgumentError):
-        kg.kpm_1d_grad(H, 16, np.ones((16, 33), dtype=np.complex128), np.zeros(16))
+
+
+def test_grad_column_batches():
+    """NR = 40 runs as batches of 32 + 8 columns; the gradient is the
+    probe-count-weighted sum of the per-batch gradients."""
+    rng = np.random.default_rng(12)
+    H = (models.square_anderson(10, W=2.0, rng=rng) / 5.1).tocsc()
+    psi = ko.random_phase_vectors(rng, 100, 40)
+    g = rng.standard_normal(48)
+    full = kg.kpm_1d_grad(H, 48, psi, g).toarray()
+    a = kg.kpm_1d_grad(H, 48, psi[:, :32], g).toarray()
+    b = kg.kpm_1d_grad(H, 48, psi[:, 32:], g).toarray()
+    ref = (32 * a + 8 * b) / 40
+    assert np.abs(full - ref).max() <= 1e-13 * np.abs(ref).max()
