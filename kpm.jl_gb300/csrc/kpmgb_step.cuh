@@ -39,16 +39,25 @@ namespace step {
 #ifndef KPMGB_FF_MIN_BLOCKS_NARROW_REAL
 #define KPMGB_FF_MIN_BLOCKS_NARROW_REAL 3
 #endif
+// complex operators with one column per lane (NR <= 32): 3 blocks/SM with
+// chunks of 4 (Haldane 256x256, NR=16: c3 kpm_2d 244 -> 211 ms)
+#ifndef KPMGB_FF_MIN_BLOCKS_CPL1_COMPLEX
+#define KPMGB_FF_MIN_BLOCKS_CPL1_COMPLEX 3
+#endif
+#ifndef KPMGB_FF_CHUNK_CPL1_COMPLEX
+#define KPMGB_FF_CHUNK_CPL1_COMPLEX 4
+#endif
 
 template <int CPL, bool REALH>
 struct FFTune {
   static constexpr bool narrow_real = REALH && CPL <= 2;
   static constexpr int min_blocks =
-      narrow_real ? KPMGB_FF_MIN_BLOCKS_NARROW_REAL : KPMGB_FF_MIN_BLOCKS;
+      narrow_real ? KPMGB_FF_MIN_BLOCKS_NARROW_REAL
+                  : (CPL == 1 ? KPMGB_FF_MIN_BLOCKS_CPL1_COMPLEX : KPMGB_FF_MIN_BLOCKS);
   static constexpr int chunk =
       CPL >= 3 ? 4
                : (CPL == 2 ? (REALH ? KPMGB_FF_CHUNK_CPL2_REAL : KPMGB_FF_CHUNK_CPL2)
-                           : KPMGB_FF_CHUNK_CPL1);
+                           : (REALH ? KPMGB_FF_CHUNK_CPL1 : KPMGB_FF_CHUNK_CPL1_COMPLEX));
   // a row's last chunk with its exact length: measured on GB300 a gain for
   // complex operators (Haldane, 10 nonzeros: chunks 8 + 2 instead of 8 + 8,
   // c3 kpm_2d 352 -> 335 ms) and a loss for the real 3-block kernel (3D

@@ -145,10 +145,6 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_step_ff_tma(KParams p) {
         }
         if (!mbar_wait(empty, (q & 1) ^ 1)) {
           atomicOr(&p.sync[1], (unsigned)STATUS_TIMEOUT);
-#ifdef KPMGB_TMA_DEBUG
-          printf("tma timeout: producer empty block %d w %d s %d q %d r %lld\n", blockIdx.x, w, s,
-                 q, (long long)r);
-#endif
           ok = false;
           break;
         }
@@ -178,9 +174,6 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_step_ff_tma(KParams p) {
       // drain: the copies of the last issued stage must land before exit
       if (last_q >= 0 && !mbar_wait(full, last_q & 1)) {
         atomicOr(&p.sync[1], (unsigned)STATUS_TIMEOUT);
-#ifdef KPMGB_TMA_DEBUG
-        printf("tma timeout: producer drain block %d w %d s %d q %d\n", blockIdx.x, w, s, last_q);
-#endif
       }
     }
   } else {
@@ -204,11 +197,6 @@ __global__ void __launch_bounds__((NCW + 1) * 32, 1) k_step_ff_tma(KParams p) {
       unsigned char* st = smem + (size_t)(w * S + s) * stage_bytes;
       if (!mbar_wait(smem_addr(&bars[w * S + s]), q & 1)) {
         atomicOr(&p.sync[1], (unsigned)STATUS_TIMEOUT);
-#ifdef KPMGB_TMA_DEBUG
-        if (lane == 0)
-          printf("tma timeout: consumer full block %d w %d s %d q %u r %lld ncols %d\n", blockIdx.x,
-                 w, s, q, (long long)r, p.ncols);
-#endif
         break;
       }
       const int nnz = *reinterpret_cast<const int*>(st + Stage::meta_offset(rowbytes));
