@@ -489,8 +489,25 @@ TcPlan plan_for(int64_t K, int nr, int nl) {
   pl.ntiles = (2 * nl + TC_N - 1) / TC_N;
   pl.ktiles = (2 * K + TC_KT - 1) / TC_KT;
   const int64_t tiles = (int64_t)pl.mtiles * pl.ntiles;
-  int64_t want = std::max<int64_t>(1, (2 * (int64_t)sm_count() + tiles - 1) / tiles);
-  want = std::min<int64_t>(want, std::max<int64_t>(1, pl.ktiles / (4 * TC_CHUNK)));
+  const int64_t S = sm_count();  // one CTA per SM (shared memory)
+  const int64_t kmax = std::max<int64_t>(1, pl.ktiles / (4 * TC_CHUNK));
+  int64_t want = std::max<int64_t>(1, (2 * S + tiles - 1) / tiles);
+  want = std::min<int64_t>(want, kmax);
+  // K splits: the count in [want, 4 want] (at most 8 S + tiles CTAs) whose
+  // grid fills its last wave best, i.e. the least waves per unit of work
+  // ceil(n tiles / S) / n; e.g. 64 tiles on 152 SMs: 19 splits (8 full
+  // waves) instead of 5 (2.1 waves run as 3)
+  int64_t best = want;
+  double best_cost = 1e300;
+  for (int64_t n = want; n <= std::min<int64_t>(4 * want, kmax); ++n) {
+    if (n * tiles > 8 * S + tiles) break;
+    const double cost = (double)((n * tiles + S - 1) / S) / (double)n;
+    if (cost < best_cost * (1.0 - 1e-9)) {
+      best_cost = cost;
+      best = n;
+    }
+  }
+  want = best;
   pl.kt_per_split = (pl.ktiles + want - 1) / want;
   pl.kt_per_split = (pl.kt_per_split + TC_CHUNK - 1) / TC_CHUNK * TC_CHUNK;
   pl.nsplit = (int)((pl.ktiles + pl.kt_per_split - 1) / pl.kt_per_split);
@@ -505,9 +522,9 @@ TcPlan plan_for(int64_t K, int nr, int nl) {
 
 size_t contract_split_scratch_bytes(int64_t K, int nr, int nl) {
   // the largest plan over sub-blocks nr' <= nr, nl' <= nl is the full block's
-  // (plane sizes grow with nr, nl; partials stay within 2*SMs tiles of work)
+  // (plane sizes grow with nr, nl; partials stay within 8*SMs + tiles tiles of work)
   const TcPlan pl = plan_for(K, nr, nl);
-  const size_t part_bound = (size_t)(2 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N *
+  const size_t part_bound = (size_t)(8 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N *
                             sizeof(double);
   return pl.a_bytes + pl.b_bytes + 2 * pl.exp_bytes + std::max(pl.part_bytes, part_bound) + 1024;
 }
@@ -515,7 +532,7 @@ size_t contract_split_scratch_bytes(int64_t K, int nr, int nl) {
 int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) {
   const TcPlan pl = plan_for(a.K, a.nr, a.nl);
   const size_t part_bound =
-      (size_t)(2 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N * sizeof(double);
+      (size_t)(8 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N * sizeof(double);
   const size_t need = pl.a_bytes + pl.b_bytes + 2 * pl.exp_bytes +
                       std::max(pl.part_bytes, part_bound) + 1024;
   if (need > a.scratch_bytes) return fail(KPMGB_ERR_ALLOC, "split contraction scratch too small");
