@@ -333,38 +333,62 @@ def sync(op: GB300Operator, stream=None) -> None:
     _native.check(_native.load().kpmgb_operator_sync(op.handle, _stream_ptr(stream)))
 
 
+class EnsembleOperator:
+    """The members of an ensemble stacked once as a block-diagonal operator
+    resident on the device, with its segment table; reusable across
+    :func:`kpm_1d_ensemble` calls."""
+
+    def __init__(self, Hs):
+        import scipy.sparse as sp
+        if not Hs:
+            raise KPMArgumentError("Hs must be a non-empty list")
+        self.sizes = [int(H.shape[0]) for H in Hs]
+        Hb = sp.block_diag([sp.csc_matrix(H, dtype=np.complex128) for H in Hs], format="csc")
+        self.op = GB300Operator(Hb)
+        self.seg = np.zeros(len(Hs) + 1, dtype=np.int64)
+        self.seg[1:] = np.cumsum(self.sizes)
+
+    def __len__(self):
+        return len(self.sizes)
+
+
 def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: bool = True):
     """Doubling moments of many independent members in one persistent launch.
 
-    ``Hs``: list of (rescaled) sparse operators of any sizes; ``psis``: list of
-    probe blocks (NH_i, NR) with a common NR (run in batches of 32 columns).
+    ``Hs``: list of (rescaled) sparse operators of any sizes, or an
+    :class:`EnsembleOperator` built from them; ``psis``: list of probe blocks
+    (NH_i, NR) with a common NR (run in batches of 32 columns).
     Equivalent to
     ``[kpm_1d(H_i, NC, NR, psi_in=psi_i) for ...]`` (``src/moment.jl:339-492``
     per member).  Returns a list of length-NC real averages, or of (NR, NC)
     matrices with ``avg_output=False``.
     """
-    import scipy.sparse as sp
-    if len(Hs) != len(psis) or not Hs:
-        raise KPMArgumentError("Hs and psis must be non-empty lists of equal length")
+    ens = Hs if isinstance(Hs, EnsembleOperator) else None
+    if ens is None:
+        if not Hs or len(Hs) != len(psis):
+            raise KPMArgumentError("Hs and psis must be non-empty lists of equal length")
+        sizes = [H.shape[0] for H in Hs]
+    else:
+        sizes = ens.sizes
+        if len(psis) != len(sizes):
+            raise KPMArgumentError("one probe block per ensemble member")
     NR = int(np.asarray(psis[0]).shape[1])
-    sizes = [H.shape[0] for H in Hs]
-    for H, p in zip(Hs, psis):
-        if np.asarray(p).shape != (H.shape[0], NR):
+    for n, p in zip(sizes, psis):
+        if np.asarray(p).shape != (n, NR):
             raise KPMArgumentError("every probe block must be (NH_i, NR) with a common NR")
     if NC % 2 != 0:
         raise KPMArgumentError("Invalid NC: NC should be even.")
-    Hb = sp.block_diag([sp.csc_matrix(H, dtype=np.complex128) for H in Hs], format="csc")
-    op = GB300Operator(Hb)
-    seg = np.zeros(len(Hs) + 1, dtype=np.int64)
-    seg[1:] = np.cumsum(sizes)
+    if ens is None:
+        ens = EnsembleOperator(Hs)
+    op, seg = ens.op, ens.seg
     psi = np.asfortranarray(np.vstack([np.asarray(p, dtype=np.complex128) for p in psis]))
-    out = np.empty((len(Hs), NC, NR), dtype=np.complex128)
+    out = np.empty((len(sizes), NC, NR), dtype=np.complex128)
     opts = _opts1d(precision, False)
     lib = _native.load()
-    rc = lib.kpmgb_kpm1d_ensemble(op.handle, len(Hs), seg.ctypes.data, NC, NR, psi.ctypes.data,
+    rc = lib.kpmgb_kpm1d_ensemble(op.handle, len(sizes), seg.ctypes.data, NC, NR, psi.ctypes.data,
                                   out.ctypes.data, C.byref(opts))
     _native.check(rc)
-    res = [np.ascontiguousarray(out[i].T) for i in range(len(Hs))]
+    res = [np.ascontiguousarray(out[i].T) for i in range(len(sizes))]
     if avg_output:
         return [m.sum(axis=0).real / NR for m in res]
     return res

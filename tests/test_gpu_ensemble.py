@@ -63,3 +63,16 @@ def test_ensemble_column_batches(built_lib, prec):
     got = kg.kpm_1d_ensemble(Hs, 64, psis, precision=prec, avg_output=False)
     for H, psi, m in zip(Hs, psis, got):
         assert relerr(m, ko.kpm_1d_doubling(H, 64, psi)) < TOL[prec]
+
+
+def test_ensemble_operator_reuse(built_lib):
+    rng = np.random.default_rng(44)
+    Hs, psis = _members(rng, 9, 6, 14)
+    ens = kg.EnsembleOperator(Hs)
+    a = kg.kpm_1d_ensemble(Hs, 48, psis, avg_output=False)
+    b = kg.kpm_1d_ensemble(ens, 48, psis, avg_output=False)
+    c = kg.kpm_1d_ensemble(ens, 48, psis, avg_output=False)
+    for x, y, z in zip(a, b, c):
+        assert np.array_equal(x, y) and np.array_equal(y, z)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_ensemble(ens, 48, psis[:-1])
