@@ -92,8 +92,10 @@ typedef struct kpmgb_kpm1d_options {
                               columns, at most 8 nonzeros per row); 6: the
                               whole recurrence in one cooperative launch with
                               a grid barrier per step (small operators,
-                              NR <= 256).  Automatic selection (0) is the
-                              register-gather kernel with the default shape. */
+                              NR <= 256); 7: float-float on packed FP32x2
+                              pairs (real operators, 17..64 columns).
+                              Automatic selection (0) is the register-gather
+                              kernel with the default shape.                  */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {

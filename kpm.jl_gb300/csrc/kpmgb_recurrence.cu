@@ -201,6 +201,8 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
       for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
         const PipeGeom g = select_kernel_ffp(ncols, dot, H.is_real != 0, H.max_row_nnz);
         if (g.fn) worst = std::max(worst, (size_t)pipe_grid(g, NH) * 2 * ncols * sizeof(double2));
+        if (KernelFn fx = select_kernel_ffx(ncols, dot, H.is_real != 0))
+          worst = std::max(worst, (size_t)grid_for(fx, NH, 32) * 2 * ncols * sizeof(double2));
       }
     }
   }
@@ -257,6 +259,14 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
       KPMGB_TRY(launch_step_kernel(fn, G, s, p));
       continue;
     }
+    if (precision == KPMGB_PREC_FF && a.variant == 7) {
+      KernelFn fx = select_kernel_ffx(p.ncols, a.dot, H.is_real != 0);
+      if (!fx)
+        return fail(KPMGB_ERR_ARGUMENT, "the packed float-float kernel serves real operators "
+                                        "with 17..64 columns");
+      KPMGB_TRY(launch_step_kernel(fx, grid_for(fx, a.NH, 32), s, p));
+      continue;
+    }
     if (precision == KPMGB_PREC_FF && a.variant == 5) {
       const PipeGeom g = select_kernel_ffp(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz);
       if (!g.fn)
@@ -310,6 +320,8 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
   if (precision == KPMGB_PREC_FF &&
       select_kernel_ffp(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz).fn)
     cands.push_back({5, 0});
+  if (precision == KPMGB_PREC_FF && select_kernel_ffx(a0.NR, a0.dot, a0.H->is_real != 0))
+    cands.push_back({7, 0});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   KPMGB_CUDA(cudaEventCreate(&e0));
   cudaError_t ce = cudaEventCreate(&e1);

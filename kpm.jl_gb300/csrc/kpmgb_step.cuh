@@ -704,5 +704,9 @@ struct PipeGeom {
 };
 PipeGeom select_kernel_ffp(int ncols, int dot, bool real, int max_row_nnz);
 
+// Packed-FP32x2 float-float kernel for real operators (kpmgb_step_ffx.cu):
+// 17..64 columns; nullptr when it does not serve the shape.
+KernelFn select_kernel_ffx(int ncols, int dot, bool real);
+
 }  // namespace step
 }  // namespace kpmgb

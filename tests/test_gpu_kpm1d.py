@@ -389,3 +389,34 @@ def test_single_launch_kernel_growth_and_limits():
     kg.kpm_1d(ok, 64, 4, psi_in=psi, kernel="single", stability_check=True)
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d(ok, 16, 257, psi_in=ko.random_phase_vectors(rng, 144, 257), kernel="single")
+
+
+@pytest.mark.parametrize("NR", [17, 32, 33, 64])
+@pytest.mark.parametrize("lr", [False, True])
+def test_packed_kernel_matches_oracle(NR, lr):
+    """kernel variant 7: packed FP32x2 float-float arithmetic (real operators)"""
+    rng = np.random.default_rng(NR + 11 * lr)
+    H = (models.cubic_anderson(8, W=4.0, rng=rng) / 8.2).tocsc()
+    NH = H.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    if lr:
+        psr = ko.random_phase_vectors(rng, NH, NR)
+        got = kg.kpm_1d(H, 41, NR, psi_in_l=psi, psi_in_r=psr, avg_output=False,
+                        precision="ff", kernel="packed")
+        ref = ko.kpm_1d_lr(H, 41, psi, psr)
+        gat = kg.kpm_1d(H, 41, NR, psi_in_l=psi, psi_in_r=psr, avg_output=False,
+                        precision="ff", kernel="gather")
+    else:
+        got = kg.kpm_1d(H, 96, NR, psi_in=psi, avg_output=False, precision="ff", kernel="packed")
+        ref = ko.kpm_1d_doubling(H, 96, psi)
+        gat = kg.kpm_1d(H, 96, NR, psi_in=psi, avg_output=False, precision="ff", kernel="gather")
+    assert relerr(got, ref) < TOL["ff"]
+    assert relerr(got, gat) < 1e-12
+
+
+def test_packed_kernel_rejects_complex_operators():
+    rng = np.random.default_rng(3)
+    H = _peierls_square(8, rng)
+    psi = ko.random_phase_vectors(rng, 64, 32)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(H, 16, 32, psi_in=psi, precision="ff", kernel="packed")
