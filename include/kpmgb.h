@@ -93,7 +93,9 @@ typedef struct kpmgb_kpm1d_options {
                               whole recurrence in one cooperative launch with
                               a grid barrier per step (small operators,
                               NR <= 256); 7: float-float on packed FP32x2
-                              pairs (real operators, 17..64 columns).
+                              pairs (real operators, 17..64 columns); 8:
+                              warp tiles with batched operator-index loads
+                              (17..64 columns, at most 8 nonzeros per row).
                               Automatic selection (0) is the register-gather
                               kernel with the default shape.                  */
 } kpmgb_kpm1d_options;

@@ -203,6 +203,8 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
         if (g.fn) worst = std::max(worst, (size_t)pipe_grid(g, NH) * 2 * ncols * sizeof(double2));
         if (KernelFn fx = select_kernel_ffx(ncols, dot, H.is_real != 0))
           worst = std::max(worst, (size_t)grid_for(fx, NH, 32) * 2 * ncols * sizeof(double2));
+        if (KernelFn fb = select_kernel_ffb(ncols, dot, H.is_real != 0, H.max_row_nnz))
+          worst = std::max(worst, (size_t)grid_for(fb, NH, 32) * 2 * ncols * sizeof(double2));
       }
     }
   }
@@ -257,6 +259,14 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
       KernelFn fn = select_kernel_ffg(sh, a.dot, H.is_real != 0);
       const int G = grid_for(fn, a.NH, sh.lpr);
       KPMGB_TRY(launch_step_kernel(fn, G, s, p));
+      continue;
+    }
+    if (precision == KPMGB_PREC_FF && a.variant == 8) {
+      KernelFn fb = select_kernel_ffb(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz);
+      if (!fb)
+        return fail(KPMGB_ERR_ARGUMENT, "the batched-index kernel serves float-float steps with "
+                                        "17..64 columns and at most 8 nonzeros per row");
+      KPMGB_TRY(launch_step_kernel(fb, grid_for(fb, a.NH, 32), s, p));
       continue;
     }
     if (precision == KPMGB_PREC_FF && a.variant == 7) {
@@ -322,6 +332,9 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
     cands.push_back({5, 0});
   if (precision == KPMGB_PREC_FF && select_kernel_ffx(a0.NR, a0.dot, a0.H->is_real != 0))
     cands.push_back({7, 0});
+  if (precision == KPMGB_PREC_FF &&
+      select_kernel_ffb(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz))
+    cands.push_back({8, 0});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   KPMGB_CUDA(cudaEventCreate(&e0));
   cudaError_t ce = cudaEventCreate(&e1);

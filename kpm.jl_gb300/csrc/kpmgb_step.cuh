@@ -708,5 +708,9 @@ PipeGeom select_kernel_ffp(int ncols, int dot, bool real, int max_row_nnz);
 // 17..64 columns; nullptr when it does not serve the shape.
 KernelFn select_kernel_ffx(int ncols, int dot, bool real);
 
+// Float-float kernel with batched operator-index loads per warp tile
+// (kpmgb_step_ffb.cu): 17..64 columns, rows of at most 8 nonzeros.
+KernelFn select_kernel_ffb(int ncols, int dot, bool real, int max_row_nnz);
+
 }  // namespace step
 }  // namespace kpmgb

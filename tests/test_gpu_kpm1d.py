@@ -420,3 +420,29 @@ def test_packed_kernel_rejects_complex_operators():
     psi = ko.random_phase_vectors(rng, 64, 32)
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d(H, 16, 32, psi_in=psi, precision="ff", kernel="packed")
+
+
+@pytest.mark.parametrize("NR", [17, 32, 33, 64])
+@pytest.mark.parametrize("lr", [False, True])
+@pytest.mark.parametrize("complex_h", [False, True])
+def test_batched_index_kernel_matches_oracle(NR, lr, complex_h):
+    """kernel variant 8: warp tiles with batched operator-index loads; y is
+    bitwise that of the register-gather kernel"""
+    rng = np.random.default_rng(NR + 5 * lr + 17 * complex_h)
+    if complex_h:
+        H = _peierls_square(19, rng)          # 361 rows: a partial last tile
+    else:
+        H = (models.cubic_anderson(7, W=4.0, rng=rng) / 8.2).tocsc()
+    NH = H.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    if lr:
+        psr = ko.random_phase_vectors(rng, NH, NR)
+        kw = dict(psi_in_l=psi, psi_in_r=psr)
+        NC, ref = 41, ko.kpm_1d_lr(H, 41, psi, psr)
+    else:
+        kw = dict(psi_in=psi)
+        NC, ref = 96, ko.kpm_1d_doubling(H, 96, psi)
+    got = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="batched", **kw)
+    gat = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="gather", **kw)
+    assert relerr(got, ref) < TOL["ff"]
+    assert relerr(got, gat) < 1e-13
