@@ -55,12 +55,16 @@ def parse():
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", default="c2", choices=["c2", "c1", "c3", "c4", "c5", "action"],
-                   help="c2 (default): the headline kpm_1d line; the others print one JSON "
-                        "line each for the secondary configurations")
-    p.add_argument("--haldane-L", type=int, default=256, help="c3: Haldane cells per side")
+    p.add_argument("--workload", default="dos",
+                   choices=["dos", "dos-small", "cond", "ensemble", "grad", "action"],
+                   help="dos (default): the headline kpm_1d line on the 3D Anderson model; "
+                        "the others print one JSON line each: dos-small (2D Anderson L=64), "
+                        "cond (kpm_2d + Kubo-Bastin on the Haldane model), ensemble (256 "
+                        "realisations), grad (adjoint gradient on graphene), action "
+                        "(chebyshev_action)")
+    p.add_argument("--haldane-L", type=int, default=256, help="cond: Haldane cells per side")
     p.add_argument("--contraction", default="both", choices=["both", "split", "fp64"],
-                   help="c3: which kpm_2d contraction(s) to time")
+                   help="cond: which kpm_2d contraction(s) to time")
     return p.parse_args()
 
 
@@ -238,7 +242,7 @@ def _time_host(fn, warmup, steps):
     return (time.perf_counter() - t0) * 1e3 / steps
 
 
-def workload_c1(args):
+def workload_dos_small(args):
     """2D square Anderson L=64 (NH=4096, 5 nnz/row), W=2, NC=1024, NR=12: the
     L2-resident configuration the CPU port runs in full."""
     import torch
@@ -254,7 +258,7 @@ def workload_c1(args):
     psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
     mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
     vs = NR * NC // 2
-    out = {"workload": "c1: kpm_1d, 2D square Anderson L=64 (NH=4096), W=2, NC=1024, NR=12",
+    out = {"workload": "kpm_1d, 2D square Anderson L=64 (NH=4096), W=2, NC=1024, NR=12",
            "metric": METRIC, "unit": UNIT}
     for prec in ("fp64", "ff"):
         for mode in ("launches", "graph", "single"):
@@ -271,11 +275,11 @@ def workload_c1(args):
     cpu_port.kpm1d_cpu(h.H, NC, psi, nthreads=nt)
     dt = time.perf_counter() - t0
     out["cpu_baseline"] = {"value": vs / dt, "unit": UNIT, "cores": nt, "kind": "port",
-                           "sample": "the full c1 call (512 steps)"}
+                           "sample": "the whole call (512 steps)"}
     return out
 
 
-def workload_c3(args):
+def workload_cond(args):
     """kpm_2d on the Haldane model 256x256 cells (NH=131072), NC=512, NR=16, then
     sigma_xy at 201 Fermi energies in [-3, 3]."""
     import torch
@@ -290,7 +294,7 @@ def workload_c3(args):
     s = torch.cuda.Stream()
     psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
     F = 8.0 * NC * NC * NH * NR
-    out = {"workload": f"c3: kpm_2d, Haldane {Lh}x{Lh}x2 (NH={NH}), t2=0.1i, NC=512, NR=16; "
+    out = {"workload": f"kpm_2d, Haldane {Lh}x{Lh}x2 (NH={NH}), t2=0.1i, NC=512, NR=16; "
                        "sigma_xy at 201 Ef",
            "flop_per_call_complex_fp64_equivalent": F}
     mus = {}
@@ -321,7 +325,7 @@ def workload_c3(args):
     return out
 
 
-def workload_c4(args):
+def workload_ensemble(args):
     """256 realisations of the 2D Anderson model, L ~ U{24..96}, W ~ U[1, 8],
     NC=512, NR=8: one persistent ensemble launch against per-member calls."""
     import kpm_gb300 as kg
@@ -335,7 +339,7 @@ def workload_c4(args):
         psis.append(kg.random_phase_vectors(rng, L * L, 8))
     NC, NR = 512, 8
     vs = 256 * NR * NC // 2
-    out = {"workload": "c4: 256 x kpm_1d, 2D Anderson L~U{24..96}, W~U[1,8], NC=512, NR=8",
+    out = {"workload": "256 x kpm_1d, 2D Anderson L~U{24..96}, W~U[1,8], NC=512, NR=8",
            "metric": METRIC, "unit": UNIT, "mean_NH": float(np.mean([H.shape[0] for H in Hs]))}
     t0 = time.perf_counter()
     ens = kg.EnsembleOperator(Hs)
@@ -353,7 +357,7 @@ def workload_c4(args):
     return out
 
 
-def workload_c5(args):
+def workload_grad(args):
     """Adjoint gradient: graphene 128x128 (NH=32768), onsite N(0, 0.1^2),
     NC=1024, NR=16; forward kpm_1d vs kpmgb_kpm1d_grad."""
     import kpm_gb300 as kg
@@ -365,7 +369,7 @@ def workload_c5(args):
     psi = kg.random_phase_vectors(rng, NH, NR)
     g = rng.standard_normal(NC)
     op = kg.GB300Operator(H)
-    out = {"workload": "c5: gradient of sum_m g_m mu_m, graphene 128x128 (NH=32768), NC=1024, NR=16"}
+    out = {"workload": "gradient of sum_m g_m mu_m, graphene 128x128 (NH=32768), NC=1024, NR=16"}
     tf = _time_host(lambda: kg.kpm_1d(op, NC, NR, psi_in=psi), 1, max(args.steps, 3))
     out["forward_ms"] = tf
     for C in (0, 64):
@@ -402,10 +406,11 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
         return
-    if args.workload != "c2":
+    if args.workload != "dos":
         import torch
         torch.cuda.set_device(local)
-        fn = {"c1": workload_c1, "c3": workload_c3, "c4": workload_c4, "c5": workload_c5,
+        fn = {"dos-small": workload_dos_small, "cond": workload_cond,
+              "ensemble": workload_ensemble, "grad": workload_grad,
               "action": workload_action}[args.workload]
         res = fn(args)
         res["version"] = __import__("kpm_gb300").version()

@@ -24,8 +24,9 @@
 namespace kpmgb {
 namespace {
 
-// 1024 threads: four times the rows in flight per member than 256 (c4, 256
-// members of mean NH 4136, NR=8: 346 -> 231 ms FP64, 311 -> 208 ms FF)
+// 1024 threads: four times the rows in flight per member than 256 (256 2D
+// Anderson realisations of mean NH 4136, NC=512, NR=8: 346 -> 231 ms FP64,
+// 311 -> 208 ms float-float)
 #ifndef KPMGB_ENS_THREADS
 #define KPMGB_ENS_THREADS 1024
 #endif

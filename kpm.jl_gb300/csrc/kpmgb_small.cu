@@ -1,5 +1,5 @@
 // Whole kpm_1d recurrence in one cooperative launch, for small operators
-// (kernel variant 6; SURVEY c1-sized problems: NH*NR up to a few hundred
+// (kernel variant 6; problems such as a 64x64 lattice with 12 probes: NH*NR up to a few hundred
 // thousand elements, where one step is a few microseconds of work and the
 // per-step launch, ramp and last-block reduction dominate).
 //

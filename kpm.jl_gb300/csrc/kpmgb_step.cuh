@@ -40,7 +40,7 @@ namespace step {
 #define KPMGB_FF_MIN_BLOCKS_NARROW_REAL 3
 #endif
 // complex operators with one column per lane (NR <= 32): 3 blocks/SM with
-// chunks of 4 (Haldane 256x256, NR=16: c3 kpm_2d 244 -> 211 ms)
+// chunks of 4 (Haldane 256x256 cells, NR=16, NC=512: kpm_2d 244 -> 211 ms)
 #ifndef KPMGB_FF_MIN_BLOCKS_CPL1_COMPLEX
 #define KPMGB_FF_MIN_BLOCKS_CPL1_COMPLEX 3
 #endif
@@ -60,7 +60,7 @@ struct FFTune {
                            : (REALH ? KPMGB_FF_CHUNK_CPL1 : KPMGB_FF_CHUNK_CPL1_COMPLEX));
   // a row's last chunk with its exact length: measured on GB300 a gain for
   // complex operators (Haldane, 10 nonzeros: chunks 8 + 2 instead of 8 + 8,
-  // c3 kpm_2d 352 -> 335 ms) and a loss for the real 3-block kernel (3D
+  // kpm_2d at NC=512 352 -> 335 ms) and a loss for the real 3-block kernel (3D
   // Anderson, chunks 4 + 3: 33% -> 29% of HBM), so it applies to complex H
   static constexpr bool exact_tail = !REALH;
 };
