@@ -173,6 +173,37 @@ function KPM.chebyshev_action!(out::AbstractArray{<:Complex,3}, Hn::GB300CSR, V:
     return nothing
 end
 
+# kpm_3d! (src/moment.jl:1105-1228): mu[:, :, p] = kpm_2d(H, Jγ, Jβ; ψl, T_p(H) Jα ψr)
+function KPM.kpm_3d!(H::GB300CSR, Jα, Jβ, Jγ, NC::Int64, NR::Int64, NH::Int64, μ, psi_in_l,
+                     psi_in_r; arr_size = :auto, right_block = :auto, precision::Symbol = :fp64,
+                     contraction::Symbol = :fp64, kwargs...)
+    opts = Ref(Kpm2dOptions(_blk(arr_size), _blk(right_block), Int64(-1), _parity(:NONE),
+                            Int32(0), _prec(precision), _contract(contraction)))
+    out = Array{ComplexF64,3}(undef, NC, NC, NC)
+    A, B, Cg = _op(Jα), _op(Jβ), _op(Jγ)
+    _check(ccall((:kpmgb_kpm3d, libkpmgb), Cint,
+                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int64, Int64, Int64,
+                  Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}, Ref{Kpm2dOptions}),
+                 H.handle, A.handle, B.handle, Cg.handle, NC, NR, NH,
+                 Matrix{ComplexF64}(psi_in_l), Matrix{ComplexF64}(psi_in_r), out, opts))
+    μ .= out
+    return nothing
+end
+
+# DOS reconstruction on the device (src/applications/dos.jl:76-161, dE_order = 0)
+function dos_gpu(μ::AbstractVector, a::Real, E_grid::AbstractVector; b::Real = 0.0,
+                 kernel = KPM.JacksonKernel, NC::Int64 = length(μ))
+    NC = min(NC, length(μ))
+    g = Float64[kernel(n, NC) for n = 0:(NC-1)]
+    ρ = Vector{Float64}(undef, length(E_grid))
+    _check(ccall((:kpmgb_dos, libkpmgb), Cint,
+                 (Ptr{Float64}, Int64, Float64, Float64, Ptr{Float64}, Ptr{Float64}, Int64,
+                  Ptr{Float64}),
+                 Vector{Float64}(real.(μ[1:NC])), NC, a, b, g, Vector{Float64}(E_grid),
+                 length(E_grid), ρ))
+    return ρ
+end
+
 # kubo_bastin_cond (src/applications/conductivity.jl:101-157) for a vector of
 # Fermi energies in one device pass.
 function kubo_bastin_cond_gpu(mu2D, a::Real, Efs::AbstractVector; b::Real = 0.0, NH::Integer,
