@@ -159,7 +159,10 @@ int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
  * mu_all/mu are device addresses with the same layouts.  Work is enqueued on
  * `stream` (a cudaStream_t; 0 is CUDA's legacy default stream) and the call
  * returns without waiting; kpmgb_operator_sync waits and reports a deferred
- * numerical failure. */
+ * numerical failure.  An operator's workspace (recurrence slots, partial
+ * sums, status word) is reused by every call on it: enqueue the calls of one
+ * handle on one stream (or order the streams), and do not destroy a handle
+ * while work on it is pending or another thread uses it. */
 int kpmgb_kpm1d_device(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,
                        const void* psi, void* mu_all,
                        const kpmgb_kpm1d_options* opts, void* stream);
