@@ -259,6 +259,13 @@ int kpmgb_kpm1d_grad(kpmgb_operator H, int64_t NC, int64_t NR, int64_t NH,
                      const double* psi, const double* g,
                      int64_t checkpoint_every, double* grad);
 
+/* Self-test of the bounded-wait error path (no reference counterpart): runs
+ * the single-launch kernel on H with a grid barrier that waits for one
+ * arrival more than the grid has, so every wait gives up after a short spin,
+ * records the timeout status and returns.  Returns KPMGB_ERR_TIMEOUT when the
+ * path works; the device context stays usable for further calls. */
+int kpmgb_selftest_wait_expiry(kpmgb_operator H);
+
 /* kpm_1d doubling moments (FP64) for callers that cannot let the library
  * allocate device memory: a host runtime that owns all device memory through
  * its own pool and budget, or a loop that must not take the device-wide

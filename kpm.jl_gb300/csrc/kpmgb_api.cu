@@ -1049,3 +1049,31 @@ extern "C" int kpmgb_kpm3d(kpmgb_operator h, kpmgb_operator ja, kpmgb_operator j
   }
   return KPMGB_OK;
 }
+
+// ------------------------------------------------------------- self-test
+// Drives the bounded-wait error path of the single-launch kernel: a grid
+// barrier that expects one arrival more than the grid has (a flag nothing
+// sets) gives up after a short spin, every block records TIMEOUT and leaves,
+// and the host maps the status to KPMGB_ERR_TIMEOUT.  The context stays
+// usable.  Returns KPMGB_ERR_TIMEOUT when the path works.
+extern "C" int kpmgb_selftest_wait_expiry(kpmgb_operator h) {
+  clear_error();
+  if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  Operator* op = as_op(h);
+  Guard g(op);
+  cudaStream_t s = op->stream;
+  Workspace& ws = op->ws;
+  const int64_t NH = op->csr.n, NR = 1, NC = 4;
+  const size_t slot = (size_t)NH * NR * 16;
+  KPMGB_TRY(ws.slots.ensure(2 * slot));
+  KPMGB_TRY(ws.mu.ensure((size_t)NR * NC * 16));
+  KPMGB_TRY(ws.partials.ensure(std::max(ws.partials.bytes, small_partials_bytes((int)NR))));
+  KPMGB_TRY(ensure_sync(op, s));
+  KPMGB_CUDA(cudaMemsetAsync(ws.slots.ptr, 0, 2 * slot, s));
+  KPMGB_CUDA(cudaMemsetAsync(ws.sync.as<unsigned>() + 2, 0, 2 * sizeof(unsigned), s));
+  KPMGB_TRY(launch_kpm1d_small(op->csr, NH, (int)NR, NC, false, KPMGB_PREC_FP64,
+                               ws.slots.ptr, ws.slots.as<char>() + slot, nullptr,
+                               ws.mu.as<double2>(), nullptr, 0.0, ws.partials.ptr,
+                               ws.partials.bytes, ws.sync.as<unsigned>(), s, 1u, 4096));
+  return check_status(op, s);
+}

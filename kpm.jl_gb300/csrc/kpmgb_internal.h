@@ -191,10 +191,13 @@ int launch_load_block(const void* psi_colmajor, void* slot, int64_t NH, int NR,
 
 // Whole kpm_1d recurrence in one cooperative launch (kpmgb_small.cu); sync[2]
 // must be zero.  small_partials_bytes: the partials it needs for NR columns.
+// extra_arrivals / spin_limit: 0 / 0 in production; the wait-expiry
+// self-test passes 1 (an arrival that never comes) and a short limit.
 int launch_kpm1d_small(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, bool lr, int precision,
                        void* slot0, void* slot1, const void* bra, double2* mu,
                        const double* mom_scale, double growth_limit, void* partials,
-                       size_t partials_bytes, unsigned* sync, cudaStream_t s);
+                       size_t partials_bytes, unsigned* sync, cudaStream_t s,
+                       unsigned extra_arrivals = 0, long long spin_limit = 0);
 size_t small_partials_bytes(int NR);
 
 // Row-major NH x NR FP64 blocks (K of them, consecutive) -> column-major.

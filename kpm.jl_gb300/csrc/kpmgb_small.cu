@@ -53,6 +53,8 @@ struct SmallParams {
   double2* partials;     // [2][G][2][NR]
   unsigned* bar;         // [0] arrivals, [1] generation
   unsigned* status;
+  unsigned extra_arrivals;  // 0; the self-test sets 1, an arrival that never comes
+  long long spin_limit;     // polls before a barrier wait gives up
 };
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
@@ -62,21 +64,22 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
 }
 
 // Returns false when the wait expired or another block reported an expiry.
-__device__ bool grid_barrier(unsigned* bar, unsigned* status) {
+__device__ bool grid_barrier(unsigned* bar, unsigned* status, unsigned extra,
+                             long long spin_limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned gen = ld_acquire(bar + 1);
     __threadfence();
     int ok = 1;
-    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+    if (atomicAdd(bar, 1u) == gridDim.x - 1 + extra) {
       atomicExch(bar, 0u);
       __threadfence();
       atomicAdd(bar + 1, 1u);
     } else {
       long long it = 0;
       while (ld_acquire(bar + 1) == gen) {
-        if (++it > kSpinLimit) {
+        if (++it > spin_limit) {
           atomicOr(status, (unsigned)STATUS_TIMEOUT);
           ok = 0;
           break;
@@ -261,7 +264,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_kpm1d_small(SmallParams p) {
       part[(size_t)blockIdx.x * 2 * NR + e] = s;
     }
     __threadfence();
-    if (!grid_barrier(p.bar, p.status)) return;
+    if (!grid_barrier(p.bar, p.status, p.extra_arrivals, p.spin_limit)) return;
     if (blockIdx.x == 0) {
       const int nd = dot == DOT_LR1 ? 1 : 2;
       for (int e = threadIdx.x; e < nd * NR; e += kSmallThreads) {
@@ -304,7 +307,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_kpm1d_small(SmallParams p) {
 int launch_kpm1d_small(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, bool lr, int precision,
                        void* slot0, void* slot1, const void* bra, double2* mu,
                        const double* mom_scale, double growth_limit, void* partials,
-                       size_t partials_bytes, unsigned* sync, cudaStream_t s) {
+                       size_t partials_bytes, unsigned* sync, cudaStream_t s,
+                       unsigned extra_arrivals, long long spin_limit) {
   if (NR < 1 || NR > kSmallThreads)
     return fail(KPMGB_ERR_ARGUMENT, "the single-launch kernel serves 1 <= NR <= 256");
   int dev = 0, coop = 0;
@@ -345,6 +349,8 @@ int launch_kpm1d_small(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, bool 
   p.partials = static_cast<double2*>(partials);
   p.bar = sync + 2;  // [2] arrivals, [3] generation (zeroed by the caller)
   p.status = sync + 1;
+  p.extra_arrivals = extra_arrivals;
+  p.spin_limit = spin_limit > 0 ? spin_limit : kSpinLimit;
   void* args[] = {&p};
   KPMGB_CUDA(cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kSmallThreads), args, 0, s));
   KPMGB_LAUNCHED();

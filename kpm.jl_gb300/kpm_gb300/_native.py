@@ -40,6 +40,7 @@ EXPORTED_SYMBOLS = (
     "kpmgb_chebyshev_action",
     "kpmgb_kpm1d_current",
     "kpmgb_kpm3d",
+    "kpmgb_selftest_wait_expiry",
 )
 
 
@@ -96,6 +97,7 @@ def _declare(lib):
     lib.kpmgb_kubo_bastin.argtypes = [vp, i64, i64, f64, f64, vp, i64, i64, f64, f64, vp, i64,
                                       f64, vp]
     lib.kpmgb_kpm1d_current.argtypes = [vp, vp, i64, i64, i64, vp, vp, C.POINTER(Kpm1dOptions)]
+    lib.kpmgb_selftest_wait_expiry.argtypes = [vp]
     lib.kpmgb_kpm3d.argtypes = [vp, vp, vp, vp, i64, i64, i64, vp, vp, vp, C.POINTER(Kpm2dOptions)]
     lib.kpmgb_chebyshev_action.argtypes = [vp, i64, i64, vp, i64, i64, vp, i64, vp]
     lib.kpmgb_dos.argtypes = [vp, i64, f64, f64, vp, vp, i64, vp]
