@@ -56,7 +56,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--workload", default="dos",
-                   choices=["dos", "dos-small", "cond", "ensemble", "grad", "action"],
+                   choices=["dos", "dos-small", "cond", "ensemble", "grad", "action", "dsigma"],
                    help="dos (default): the headline kpm_1d line on the 3D Anderson model; "
                         "the others print one JSON line each: dos-small (2D Anderson L=64), "
                         "cond (kpm_2d + Kubo-Bastin on the Haldane model), ensemble (256 "
@@ -325,6 +325,42 @@ def workload_cond(args):
     return out
 
 
+def workload_dsigma(args):
+    """dsigma_xy/dt2 at Ef=0 of the Haldane model, 64x64 cells (NH=8192), t2=0.2,
+    NC=256, NR=8, fixed rescaling: host-API kpm_2d + reconstruction (forward)
+    against kpm_2d_derivative (forward mode over the 2NH block operators) +
+    reconstruction, both end to end from host arrays."""
+    import kpm_gb300 as kg
+    from kpm_gb300 import models, rescale
+    L, t2, NC, NR = 64, 0.2, 256, 8
+    H, Jx, Jy, area = models.haldane(L, L, t2=t2)
+    H0, Jx0, Jy0, _ = models.haldane(L, L, t2=0.0)
+    H1, Jx1, Jy1, _ = models.haldane(L, L, t2=1.0)
+    h = rescale(H, center=True)
+    NH = H.shape[0]
+    dH, dJx, dJy = (H1 - H0) / h.a, Jx1 - Jx0, Jy1 - Jy0
+    psi = kg.random_phase_vectors(np.random.default_rng(42), NH, NR)
+    out = {"workload": "dsigma_xy/dt2 at Ef=0, Haldane 64x64x2 (NH=8192), t2=0.2, NC=256, NR=8"}
+    steps = max(args.steps, 3)
+    for contraction in ("fp64", "split"):
+        res = {}
+
+        def fwd():
+            mu = kg.kpm_2d(h.H, Jx, Jy, NC, NR, NH, psi_in=psi, contraction=contraction)
+            res["sigma"] = kg.kubo_bastin_cond(mu, h.a, 0.0, b=h.b, NH=NH, area=area)
+
+        def der():
+            dmu = kg.kpm_2d_derivative(h.H, dH, Jx, dJx, Jy, dJy, NC, NR, NH, psi_in=psi,
+                                       contraction=contraction)
+            res["dsigma"] = kg.kubo_bastin_cond(dmu, h.a, 0.0, b=h.b, NH=NH, area=area)
+        tf = _time_host(fwd, 1, steps)
+        td = _time_host(der, 1, steps)
+        out[f"{contraction}_contraction"] = {
+            "forward_ms": tf, "derivative_ms": td, "derivative_over_forward": td / tf,
+            "sigma_xy": res["sigma"], "dsigma_xy_dt2": res["dsigma"]}
+    return out
+
+
 def workload_ensemble(args):
     """256 realisations of the 2D Anderson model, L ~ U{24..96}, W ~ U[1, 8],
     NC=512, NR=8: one persistent ensemble launch against per-member calls."""
@@ -411,7 +447,7 @@ def main():
         torch.cuda.set_device(local)
         fn = {"dos-small": workload_dos_small, "cond": workload_cond,
               "ensemble": workload_ensemble, "grad": workload_grad,
-              "action": workload_action}[args.workload]
+              "action": workload_action, "dsigma": workload_dsigma}[args.workload]
         res = fn(args)
         res["version"] = __import__("kpm_gb300").version()
         if rank == 0:

@@ -9,16 +9,19 @@
 // 2^-e (e: exponent of the row's largest entry) and written as five signed
 // 8-bit digits d_0..d_4 (|d| <= 128), stored pre-scaled as BF16 planes
 // p_i = d_i 2^(-8i) (exact), so that
-//     v = 2^(e-7) * sum_i p_i          (truncation < 2^-40 of the row max)
+//     v = 2^(e-7) * sum_i p_i          (rounding <= 2^-39 of the row max)
 // and every plane product carries its own weight.  The 15 plane pairs with
-// i + j <= 4 feed three TMEM accumulators (128 x 64 FP32 each): level 0
-// (p_0 q_0, integers), level 1 (p_0 q_1 + p_1 q_0, multiples of 2^-8) and
-// levels >= 2 together.  Over a chunk of 256 K' elements the first two stay
-// below 2^22 and 2^15 and are therefore exact in the tensor core's FP32
-// accumulation; the third holds contributions below 2^-16 of the first, so
-// its FP32 rounding is below 2^-39 of the result.  After each chunk the
-// epilogue warps fold the three accumulators into one int64 per output in
-// units of 2^-16 (exact for levels 0-1) and the chunk accumulators are reused.
+// i + j <= 4 feed four TMEM accumulators (128 x 64 FP32 each): level 0
+// (p_0 q_0, integers), level 1 (p_0 q_1 + p_1 q_0, multiples of 2^-8),
+// level 2 (multiples of 2^-16) and levels 3-4 together.  Over a chunk of 256
+// K' elements the first three stay below 2^22, 2^15 and 2^8, i.e. within 24
+// significant bits of their granularity, and are therefore exact in the
+// tensor core's FP32 accumulation; the fourth stays below ~1, so its FP32
+// rounding is below 2^-24 (2^-38 of one leading digit product).  After each
+// chunk the epilogue warps fold the four accumulators into one int64 per
+// output in units of 2^-24 (exact for levels 0-3, level 4 rounded to 2^-25)
+// and the chunk accumulators are reused.  A K split holds at most 2^24 K'
+// elements, so the int64 stays below 2^62.
 //
 // Data movement: the digit planes are pre-tiled in global memory in the
 // canonical no-swizzle K-major UMMA layout, so each pipeline stage is two
@@ -42,7 +45,7 @@ constexpr int TC_M = 128;      // A rows per tile
 constexpr int TC_N = 64;       // B rows per tile
 constexpr int TC_KT = 32;      // real K' elements per k-tile
 constexpr int TC_SLICES = 5;   // digit planes per operand
-constexpr int TC_ACC = 3;      // TMEM accumulators: level 0, level 1, levels >= 2
+constexpr int TC_ACC = 4;      // TMEM accumulators: levels 0, 1, 2 and 3-4
 constexpr int TC_CHUNK = 8;    // k-tiles per exact chunk (256 K' elements)
 constexpr int TC_STAGES = 3;
 constexpr uint32_t A_TILE = TC_M * TC_KT * 2;  // 8 KiB per plane
@@ -50,7 +53,8 @@ constexpr uint32_t B_TILE = TC_N * TC_KT * 2;  // 4 KiB per plane
 constexpr uint32_t A_STAGE = A_TILE * TC_SLICES;
 constexpr uint32_t B_STAGE = B_TILE * TC_SLICES;
 constexpr uint32_t STAGE_BYTES = A_STAGE + B_STAGE;
-constexpr int TMEM_COLS = 512;  // 2 buffers x 3 accumulators x 64 columns (384 used)
+constexpr int TMEM_COLS = 512;  // 2 buffers x 4 accumulators x 64 columns
+constexpr int64_t kMaxKtPerSplit = (int64_t)1 << 19;  // 2^24 K' elements: int64 headroom
 constexpr int TMEM_BUF = TC_ACC * TC_N;
 constexpr int kSpin = 1 << 22;
 constexpr int kThreadsTC = 192;  // 6 warps
@@ -179,17 +183,22 @@ __global__ void __launch_bounds__(256) k_vec_exp(const void* vecs, int64_t K, in
   }
 }
 
-// Five signed digits of the scaled value (vh + vl) * 2^-e.
+// Five signed base-256 digits of the scaled value (vh + vl) * 2^(7-e).  The
+// value is first made an integer, N = round(vh 2^(39-e)) + round(vl 2^(39-e))
+// (|N| <= 2^39; within one unit, 2^-39 of the vector maximum), so no digit
+// loses the low half's bits to an FP32 rounding; the digits then come off N
+// from the least significant end, balanced: d_i in [-128, 127] for i >= 1 and
+// |d_0| <= 128, with (vh + vl) 2^(7-e) = sum_i d_i 256^-i to that unit.
 __device__ __forceinline__ void digits(float vh, float vl, int e, float (&d)[TC_SLICES]) {
-  const float th = ldexpf(vh, 7 - e), tl = ldexpf(vl, 7 - e);
-  d[0] = rintf(th);
-  float r = __fadd_rn(__fsub_rn(th, d[0]), tl);
+  long long n = __float2ll_rn(ldexpf(vh, 39 - e)) + __float2ll_rn(ldexpf(vl, 39 - e));
 #pragma unroll
-  for (int i = 1; i < TC_SLICES; ++i) {
-    const float t = __fmul_rn(r, 256.f);
-    d[i] = rintf(t);
-    r = __fsub_rn(t, d[i]);
+  for (int i = TC_SLICES - 1; i >= 1; --i) {
+    const int lo = (int)(n & 255);
+    const int di = lo >= 128 ? lo - 256 : lo;
+    d[i] = (float)di;
+    n = (n - di) / 256;  // exact: n - di is a multiple of 256
   }
+  d[0] = (float)n;
 }
 
 // Write the digit planes of A (R vectors) or B/B' (L vectors) in the
@@ -348,7 +357,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        bool started[TC_ACC] = {false, false, false};
+        bool started[TC_ACC] = {false, false, false, false};
         const int64_t rem = nkt - c * TC_CHUNK;
         const int64_t tiles = rem < TC_CHUNK ? rem : TC_CHUNK;
         for (int64_t t = 0; t < tiles; ++t, ++i) {
@@ -365,7 +374,7 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
             for (int ia = 0; ia < TC_SLICES; ++ia)
 #pragma unroll
               for (int ib = 0; ib < TC_SLICES - ia; ++ib) {
-                const int acc = ia + ib < 2 ? ia + ib : 2;
+                const int acc = ia + ib < 3 ? ia + ib : 3;
                 const uint64_t ad = umma_desc(a0 + ia * A_TILE + ks * (TC_M * 32));
                 const uint64_t bd = umma_desc(b0 + ib * B_TILE + ks * (TC_N * 32));
                 umma(tmem + buf * TMEM_BUF + acc * TC_N, ad, bd, started[acc] ? 1u : 0u);
@@ -395,10 +404,11 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int ac = 0; ac < TC_ACC; ++ac) {
-        // in units of 2^-16: level 0 is an integer, level 1 a multiple of
-        // 2^-8 (both exact), levels >= 2 rounded to 2^-16
-        const float unit = ac == 0 ? 1.f : (ac == 1 ? 256.f : 65536.f);
-        const int shift = ac == 0 ? 16 : (ac == 1 ? 8 : 0);
+        // in units of 2^-24: level 0 is an integer, level 1 a multiple of
+        // 2^-8, level 2 of 2^-16 (all exact), levels 3-4 (|.| < ~1.01, so
+        // below 2^25 units) rounded to 2^-24
+        const float unit = ac == 0 ? 1.f : (ac == 1 ? 256.f : (ac == 2 ? 65536.f : 16777216.f));
+        const int shift = 24 - 8 * ac;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           uint32_t v[32];
@@ -418,14 +428,14 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
     if (!ok) atomicOr(p.status, (unsigned)STATUS_TIMEOUT);
     const int a = mt * TC_M + row;
     if (a < p.nr) {
-      // value = acc * 2^-16 * 2^(eA - 7) * 2^(eB - 7)
+      // value = acc * 2^-24 * 2^(eA - 7) * 2^(eB - 7)
       const int ea = p.expA[a];
 #pragma unroll
       for (int j = 0; j < TC_N; ++j) {
         const int col = nt * TC_N + j;
         if (col < p.ncols) {
           const int eb = p.expB[col % p.nl];
-          const double vv = ldexp((double)acc[j], ea + eb - 30);
+          const double vv = ldexp((double)acc[j], ea + eb - 38);
           p.part[((size_t)sp * p.nr + a) * p.ncols + col] = vv;
         }
       }
@@ -507,9 +517,10 @@ TcPlan plan_for(int64_t K, int nr, int nl) {
       best = n;
     }
   }
-  want = best;
+  want = std::max(best, (pl.ktiles + kMaxKtPerSplit - 1) / kMaxKtPerSplit);
   pl.kt_per_split = (pl.ktiles + want - 1) / want;
   pl.kt_per_split = (pl.kt_per_split + TC_CHUNK - 1) / TC_CHUNK * TC_CHUNK;
+  pl.kt_per_split = std::min(pl.kt_per_split, kMaxKtPerSplit);
   pl.nsplit = (int)((pl.ktiles + pl.kt_per_split - 1) / pl.kt_per_split);
   pl.a_bytes = (size_t)pl.mtiles * pl.ktiles * TC_SLICES * A_TILE;
   pl.b_bytes = (size_t)pl.ntiles * pl.ktiles * TC_SLICES * B_TILE;
@@ -518,21 +529,29 @@ TcPlan plan_for(int64_t K, int nr, int nl) {
   return pl;
 }
 
+// Partials of a plan, bounded over its sub-blocks: the split count times the
+// tiles stays within 8*SMs + tiles, or the minimum split count that keeps a
+// split within kMaxKtPerSplit k-tiles times the tiles.
+size_t part_bound_bytes(const TcPlan& pl) {
+  const int64_t tiles = (int64_t)pl.mtiles * pl.ntiles;
+  const int64_t nmin = (pl.ktiles + kMaxKtPerSplit - 1) / kMaxKtPerSplit;
+  return (size_t)std::max<int64_t>(8 * sm_count() + tiles, nmin * tiles) * TC_M * TC_N *
+         sizeof(double);
+}
+
 }  // namespace
 
 size_t contract_split_scratch_bytes(int64_t K, int nr, int nl) {
   // the largest plan over sub-blocks nr' <= nr, nl' <= nl is the full block's
-  // (plane sizes grow with nr, nl; partials stay within 8*SMs + tiles tiles of work)
+  // (plane sizes grow with nr, nl; partials within part_bound_bytes)
   const TcPlan pl = plan_for(K, nr, nl);
-  const size_t part_bound = (size_t)(8 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N *
-                            sizeof(double);
+  const size_t part_bound = part_bound_bytes(pl);
   return pl.a_bytes + pl.b_bytes + 2 * pl.exp_bytes + std::max(pl.part_bytes, part_bound) + 1024;
 }
 
 int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) {
   const TcPlan pl = plan_for(a.K, a.nr, a.nl);
-  const size_t part_bound =
-      (size_t)(8 * sm_count() + pl.mtiles * pl.ntiles) * TC_M * TC_N * sizeof(double);
+  const size_t part_bound = part_bound_bytes(pl);
   const size_t need = pl.a_bytes + pl.b_bytes + 2 * pl.exp_bytes +
                       std::max(pl.part_bytes, part_bound) + 1024;
   if (need > a.scratch_bytes) return fail(KPMGB_ERR_ALLOC, "split contraction scratch too small");

@@ -277,6 +277,124 @@ def kpm_2d(H, Ja, Jb, NC: int, NR: int, NH: int, *, psi_in=None, psi_in_l=None, 
     return mu
 
 
+# ------------------------------------------------- directional derivatives
+def _host_sparse(M, name):
+    import scipy.sparse as sp
+    if isinstance(M, GB300Operator):
+        raise KPMArgumentError(f"{name}: the derivative forms need host matrices, "
+                               "not device operators")
+    return sp.csr_matrix(M, dtype=np.complex128)
+
+
+def _lower_block(A, dA, n):
+    """[[A, 0], [dA, A]]: T_n of it is [[T_n(A), 0], [D T_n(A)[dA], T_n(A)]], and a
+    product of such blocks carries the product rule in its lower-left block."""
+    import scipy.sparse as sp
+    dA = sp.csr_matrix((n, n), dtype=np.complex128) if dA is None else dA
+    return sp.bmat([[A, None], [dA, A]], format="csc")
+
+
+def _inf_norm(M) -> float:
+    return float(abs(M).sum(axis=1).max()) if M is not None and M.nnz else 0.0
+
+
+def _tangent_scale(NC: int, dH, J_pairs=()) -> float:
+    """Power of two s applied to the tangent direction and undone on the result
+    (both exact).  The tangent halves of the augmented vectors grow like
+    n^2 |dH| relative to the value halves (|D T_n(H)[dH]| <= n^2 |dH| for
+    |H| <= 1); s near the geometric mean of that growth over n = 1..NC keeps
+    both halves within a factor ~NC of each other, which the per-vector
+    scaling of the float-float rows and of the split contraction's digit
+    planes needs (otherwise the small half loses ~2 log2(NC |dH|) bits)."""
+    import math
+    g = int(NC) * _inf_norm(dH)
+    for J, dJ in J_pairs:
+        nj = _inf_norm(J)
+        if nj > 0:
+            g = max(g, _inf_norm(dJ) / nj)
+    if not g > 0 or not math.isfinite(g):
+        return 1.0
+    return math.ldexp(1.0, -round(math.log2(g)))
+
+
+def kpm_1d_derivative(H, dH, NC: int, NR: int, NH: int | None = None, *, psi_in,
+                      avg_output: bool = True, precision: str = "fp64", kernel: str = "auto"):
+    """Directional derivative of ``kpm_1d`` moments along ``H + t dH`` at t = 0:
+    ``dmu_n = sum_i <psi_i| D T_n(H)[dH] |psi_i>`` (forward mode, one scalar
+    parameter; ``kpm_1d_grad`` is the reverse mode for many).
+
+    Runs the l/r recurrence of ``kpm_1d`` on the GPU over the 2NH operator
+    ``[[H, 0], [dH, H]]`` with ket ``[psi; 0]`` and bra ``[0; psi]``: the lower
+    half of ``T_n`` applied to the ket is the Frechet derivative of ``T_n(H)``
+    applied to psi.  Costs about twice a forward call.  Returns the real
+    probe average (length NC; ``dH`` Hermitian) or the complex (NR, NC) matrix
+    with ``avg_output=False``.  No reference counterpart: KPM.jl differentiates
+    ``src/moment.jl:420-556`` with ForwardDiff duals.
+    """
+    import scipy.sparse as sp
+    Hh, dHh = _host_sparse(H, "H"), _host_sparse(dH, "dH")
+    NH = Hh.shape[0] if NH is None else int(NH)
+    if Hh.shape != (NH, NH) or dHh.shape != (NH, NH):
+        raise KPMArgumentError(f"H and dH must both be ({NH}, {NH})")
+    psi = np.asarray(psi_in, dtype=np.complex128)
+    if psi.shape != (NH, int(NR)):
+        raise KPMArgumentError(f"Invalid `psi_in` with size {psi.shape}. Expecting ({NH}, {NR})")
+    z = np.zeros_like(psi)
+    sc = _tangent_scale(NC, dHh)
+    mu = kpm_1d(_lower_block(Hh, dHh * sc, NH), NC, NR, 2 * NH,
+                psi_in_l=np.vstack([z, psi]), psi_in_r=np.vstack([psi, z]),
+                avg_output=False, precision=precision, kernel=kernel) / sc
+    return mu.sum(axis=0).real / int(NR) if avg_output else mu
+
+
+def kpm_2d_derivative(H, dH, Ja, dJa, Jb, dJb, NC: int, NR: int, NH: int, *, psi_in=None,
+                      psi_in_l=None, psi_in_r=None, **kw):
+    """Directional derivative of ``kpm_2d`` moments along ``H + t dH``,
+    ``Ja + t dJa``, ``Jb + t dJb`` at t = 0 (``dJa`` / ``dJb`` may be None):
+    ``dmu[n, m] = (1/NR) sum_i d<T_m psi_l_i | Jb T_n Ja psi_r_i>``.
+
+    One GPU ``kpm_2d`` call over 2NH operators: ``[[H, 0], [dH, H]]``,
+    ``[[Ja, 0], [dJa, Ja]]`` and ``[[dJb, Jb], [Jb, 0]]`` (the lower-triangular
+    embedding of Jb with its halves swapped), probes ``[psi_l; 0]`` and
+    ``[psi_r; 0]``: the left chain carries ``[L_m; dL_m]``, the right one
+    ``[dR_n; R_n]``, so the contraction sums ``<L|dR> + <dL|R>``.  The
+    direction is pre-scaled by a power of two (``_tangent_scale``).  Every
+    ``kpm_2d`` keyword (blocking, parity, mn_sym, precision, contraction)
+    applies.  ``kubo_bastin_cond`` is linear in the moments, so at fixed
+    rescaling ``kubo_bastin_cond(dmu, ...)`` is the derivative of the
+    conductivity (e.g. dsigma_xy/dt2 of the Haldane model).  No reference
+    counterpart (``src/moment.jl:887-1088`` is differentiated with duals).
+    """
+    import scipy.sparse as sp
+    NH, NR = int(NH), int(NR)
+    Hh, dHh = _host_sparse(H, "H"), _host_sparse(dH, "dH")
+    A, B = _host_sparse(Ja, "Ja"), _host_sparse(Jb, "Jb")
+    dA = None if dJa is None else _host_sparse(dJa, "dJa")
+    dB = None if dJb is None else _host_sparse(dJb, "dJb")
+    for M, name in ((Hh, "H"), (dHh, "dH"), (A, "Ja"), (B, "Jb"), (dA, "dJa"), (dB, "dJb")):
+        if M is not None and M.shape != (NH, NH):
+            raise KPMArgumentError(f"{name} must be ({NH}, {NH}) (got {M.shape})")
+    if psi_in is not None:
+        if psi_in_l is not None or psi_in_r is not None:
+            raise KPMArgumentError("unimplemented")
+        psi_in_l = psi_in_r = psi_in
+    if psi_in_l is None or psi_in_r is None:
+        raise KPMArgumentError("kpm_2d_derivative needs explicit probes "
+                               "(`psi_in` or `psi_in_l` and `psi_in_r`)")
+    pl = np.asarray(psi_in_l, dtype=np.complex128)
+    pr = np.asarray(psi_in_r, dtype=np.complex128)
+    if pl.shape != (NH, NR) or pr.shape != (NH, NR):
+        raise KPMArgumentError(f"probes must be ({NH}, {NR})")
+    z = np.zeros((NH, NR), dtype=np.complex128)
+    sc = _tangent_scale(NC, dHh, ((A, dA), (B, dB)))
+    dA = None if dA is None else dA * sc
+    Bs = sp.csr_matrix((NH, NH), dtype=np.complex128) if dB is None else dB * sc
+    Jb_aug = sp.bmat([[Bs, B], [B, None]], format="csc")
+    mu = kpm_2d(_lower_block(Hh, dHh * sc, NH), _lower_block(A, dA, NH), Jb_aug, NC, NR, 2 * NH,
+                psi_in_l=np.vstack([pl, z]), psi_in_r=np.vstack([pr, z]), **kw)
+    return mu / sc
+
+
 # ------------------------------------------------------------ device forms
 def _stream_ptr(stream):
     if stream is None:

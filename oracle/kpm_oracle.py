@@ -421,3 +421,51 @@ def normalizeH(H, eps: float = 0.1, fixed_a: float = 0.0, center: bool = False):
                           return_eigenvectors=False)[0])
     a = 2 * emax / (2 - eps)
     return float(a), 0.0, Hs / a
+
+
+# ------------------------------------------------------ directional derivatives
+# No reference counterpart: KPM.jl obtains these by pushing ForwardDiff duals
+# through the recurrences of ``src/moment.jl:420-556`` and ``:887-1088``.  The
+# restatement below is the dual-number arithmetic written out: every
+# recurrence vector v carries its tangent dv along H + t dH, updated by the
+# product rule.
+def _tangent_chain(H, dH, v0, dv0, NC: int):
+    """Vectors T_n(H) v0 and their tangents for n = 0..NC-1 (dual recurrence of
+    ``src/chebyshev_iteration.jl:59-75``)."""
+    v = [v0, H @ v0]
+    dv = [dv0, dH @ v0 + H @ dv0]
+    for n in range(2, NC):
+        v.append(2.0 * (H @ v[n - 1]) - v[n - 2])
+        dv.append(2.0 * (dH @ v[n - 1] + H @ dv[n - 1]) - dv[n - 2])
+    return v[:NC], dv[:NC]
+
+
+def kpm_1d_tangent(H, dH, NC: int, psi: np.ndarray) -> np.ndarray:
+    """d/dt <psi_i|T_n(H + t dH)|psi_i> at t = 0, shape (NR, NC)."""
+    H, dH = _csr(H), _csr(dH)
+    psi = np.asarray(psi, dtype=np.complex128)
+    _, dv = _tangent_chain(H, dH, psi, np.zeros_like(psi), NC)
+    return np.stack([columnwise_dot(psi, d) for d in dv], axis=1)
+
+
+def kpm_2d_tangent(H, dH, Ja, dJa, Jb, dJb, NC: int, psi_l, psi_r) -> np.ndarray:
+    """d/dt of the kpm_2d moments mu[n, m] = sum_i <T_m psil_i|Jb T_n Ja psir_i>/NR
+    along (H, Ja, Jb) + t (dH, dJa, dJb) at t = 0 (orientation of
+    ``src/moment.jl:1055-1070``), shape (NC, NC)."""
+    H, dH, Ja, Jb = _csr(H), _csr(dH), _csr(Ja), _csr(Jb)
+    NH, NR = np.asarray(psi_r).shape
+    zero = sp.csr_matrix((NH, NH), dtype=np.complex128)
+    dJa = zero if dJa is None else _csr(dJa)
+    dJb = zero if dJb is None else _csr(dJb)
+    pl = np.asarray(psi_l, dtype=np.complex128)
+    pr = np.asarray(psi_r, dtype=np.complex128)
+    L, dL = _tangent_chain(H, dH, pl, np.zeros_like(pl), NC)
+    S, dS = _tangent_chain(H, dH, Ja @ pr, dJa @ pr, NC)
+    R = [Jb @ s for s in S]
+    dR = [dJb @ s + Jb @ ds for s, ds in zip(S, dS)]
+    Lm = np.stack([x.reshape(-1, order="F") for x in L], axis=1)
+    dLm = np.stack([x.reshape(-1, order="F") for x in dL], axis=1)
+    Rn = np.stack([x.reshape(-1, order="F") for x in R], axis=1)
+    dRn = np.stack([x.reshape(-1, order="F") for x in dR], axis=1)
+    # dmu[n, m] = (<dL_m|R_n> + <L_m|dR_n>) / NR
+    return (Rn.T @ dLm.conj() + dRn.T @ Lm.conj()) / NR

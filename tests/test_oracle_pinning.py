@@ -297,3 +297,42 @@ def test_oracle_kpm1d_current_trace():
     ref = np.array([np.trace(J @ T[n]) / D for n in range(NC)])
     mu = ko.kpm_1d_current(H, J, NC, np.eye(D, dtype=complex)).sum(axis=0) / D
     assert np.linalg.norm(mu - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+def test_oracle_tangent_trace_identity():
+    """Directional derivative of the traced moments: with identity probes,
+    d/dt Tr T_n(H + t dH) = n Tr[U_{n-1}(H) dH] (T_n' = n U_{n-1}), exactly."""
+    from helpers import rand_herm
+    rng = np.random.default_rng(5)
+    D, NC = 16, 20
+    H = rand_herm(rng, D)
+    dH = rand_herm(rng, D, scale=3.0)
+    U = [np.eye(D, dtype=complex), 2.0 * H]
+    for n in range(2, NC):
+        U.append(2.0 * H @ U[n - 1] - U[n - 2])
+    ref = np.array([0.0] + [n * np.trace(U[n - 1] @ dH) for n in range(1, NC)])
+    got = ko.kpm_1d_tangent(H, dH, NC, np.eye(D, dtype=complex)).sum(axis=0)
+    assert np.linalg.norm(got - ref) <= 1e-12 * np.linalg.norm(ref)
+
+
+def test_oracle_tangent_finite_difference():
+    """kpm_1d / kpm_2d tangents against central differences of the moments in
+    the Haldane t2 direction (H, Jx, Jy are affine in t2)."""
+    def model(t2):
+        H, Jx, Jy, _ = models.haldane(4, 4, t2=t2)
+        return H / 3.8, Jx, Jy
+    rng = np.random.default_rng(6)
+    (H0, Jx0, Jy0), (H1, Jx1, Jy1) = model(0.0), model(1.0)
+    t2, h, NC, NR = 0.2, 1e-5, 24, 3
+    H, Jx, Jy = model(t2)
+    NH = H.shape[0]
+    psl = ko.random_phase_vectors(rng, NH, NR)
+    psr = ko.random_phase_vectors(rng, NH, NR)
+    d2 = ko.kpm_2d_tangent(H, H1 - H0, Jx, Jx1 - Jx0, Jy, Jy1 - Jy0, NC, psl, psr)
+    fd2 = (ko.kpm2d_dense_reference(*model(t2 + h), psl, psr, NC)
+           - ko.kpm2d_dense_reference(*model(t2 - h), psl, psr, NC)) / (2 * h)
+    assert relerr(d2, fd2) < 1e-6
+    d1 = ko.kpm_1d_tangent(H, H1 - H0, NC, psr)
+    fd1 = (ko.kpm_1d_lr(model(t2 + h)[0], NC, psr, psr)
+           - ko.kpm_1d_lr(model(t2 - h)[0], NC, psr, psr)) / (2 * h)
+    assert relerr(d1, fd1) < 1e-6
