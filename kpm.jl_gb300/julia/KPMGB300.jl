@@ -237,4 +237,28 @@ function kpm_1d_grad(H::SparseMatrixCSC, NC::Int64, psi_in::AbstractMatrix, g::A
     return SparseMatrixCSC(size(Hc, 1), size(Hc, 2), copy(Hc.colptr), copy(Hc.rowval), out)
 end
 
+# Directional derivative of the kpm_2d moments along (H, Jα, Jβ) + t (dH, dJα, dJβ)
+# (forward mode; no reference counterpart): one kpm_2d over the 2NH block operators
+# [H 0; dH H], [Jα 0; dJα Jα], [dJβ Jβ; Jβ 0] with probes [ψl; 0], [ψr; 0], the
+# direction pre-scaled by a power of two that balances the two halves.
+function kpm_2d_derivative(H::SparseMatrixCSC, dH, Jα, dJα, Jβ, dJβ, NC::Int64, NR::Int64,
+                           NH::Int64, psi_in_l::AbstractMatrix, psi_in_r::AbstractMatrix;
+                           kwargs...)
+    Z = spzeros(ComplexF64, NH, NH)
+    nrm(M) = M === nothing ? 0.0 : opnorm(M, Inf)
+    g = sqrt(NC) * nrm(dH)
+    for (J, dJ) in ((Jα, dJα), (Jβ, dJβ))
+        nrm(J) > 0 && (g = max(g, nrm(dJ) / nrm(J)))
+    end
+    s = g > 0 ? exp2(-round(log2(g))) : 1.0
+    sc(M) = M === nothing ? Z : s .* SparseMatrixCSC{ComplexF64,Int64}(M)
+    Haug = GB300CSR([H Z; sc(dH) H])
+    Aaug = [Jα Z; sc(dJα) Jα]
+    Baug = [sc(dJβ) Jβ; Jβ Z]
+    z = zeros(ComplexF64, NH, NR)
+    dμ = Matrix{ComplexF64}(undef, NC, NC)
+    KPM.kpm_2d!(Haug, Aaug, Baug, NC, NR, 2NH, dμ, [psi_in_l; z], [psi_in_r; z]; kwargs...)
+    return dμ ./ s
+end
+
 end # module

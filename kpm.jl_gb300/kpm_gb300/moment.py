@@ -300,14 +300,15 @@ def _inf_norm(M) -> float:
 
 def _tangent_scale(NC: int, dH, J_pairs=()) -> float:
     """Power of two s applied to the tangent direction and undone on the result
-    (both exact).  The tangent halves of the augmented vectors grow like
-    n^2 |dH| relative to the value halves (|D T_n(H)[dH]| <= n^2 |dH| for
-    |H| <= 1); s near the geometric mean of that growth over n = 1..NC keeps
-    both halves within a factor ~NC of each other, which the per-vector
-    scaling of the float-float rows and of the split contraction's digit
-    planes needs (otherwise the small half loses ~2 log2(NC |dH|) bits)."""
+    (both exact).  The tangent halves of the augmented vectors grow relative
+    to the value halves like n |dH| for probes spread over the band interior
+    (T_n' = n U_{n-1}; the worst-case bound n^2 |dH| needs band-edge weight);
+    s near the geometric mean sqrt(NC) |dH| of that growth keeps the halves
+    within a factor ~sqrt(NC) of each other, which the per-vector scaling of
+    the float-float rows and of the split contraction's digit planes needs
+    (the smaller half loses log2 of the ratio in bits)."""
     import math
-    g = int(NC) * _inf_norm(dH)
+    g = math.sqrt(int(NC)) * _inf_norm(dH)
     for J, dJ in J_pairs:
         nj = _inf_norm(J)
         if nj > 0:
