@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--NR", type=int, default=64)
     p.add_argument("--cpu-steps", type=int, default=16,
                    help="recurrence steps in the bounded CPU-baseline sample")
+    p.add_argument("--kernel", default="auto",
+                   choices=["auto", "gather", "tune", "anchored", "pipelined", "packed", "batched",
+                            "padded"],
+                   help="float-float step kernel of the headline call")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -84,6 +88,7 @@ def config(args, scaling_note=None):
                      f"W={args.W}, centred rescaling, NC={args.NC}, NR={args.NR}"),
         "NH": NH, "NC": args.NC, "NR": args.NR, "nnz_per_row": 7,
         "precision": args.precision,
+        "step_kernel": args.kernel,
         "l2": "inputs larger than L2 (2.1 GB per recurrence slot), no flush needed",
         "step": "one kpm_1d call = NC/2 recurrence launches with fused moments",
     }
@@ -469,7 +474,8 @@ def main():
     mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
 
     def call(prec):
-        kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec, stream=stream)
+        kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec, stream=stream,
+                         kernel=args.kernel if prec == "ff" else "auto")
 
     def barrier():
         if world > 1:
@@ -523,11 +529,13 @@ def main():
         pinned.numpy()[...] = psi.T
         host_psi = pinned.numpy().T  # (NH, NR) column-major view of pinned memory
         mu_host = np.zeros((NR, NC), dtype=np.complex128)
-        kg.kpm_1d_bang(op, NC, NR, NH, mu_host, host_psi, precision=args.precision)
+        kg.kpm_1d_bang(op, NC, NR, NH, mu_host, host_psi, precision=args.precision,
+                       kernel=args.kernel if args.precision == "ff" else "auto")
         barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            kg.kpm_1d_bang(op, NC, NR, NH, mu_host, host_psi, precision=args.precision)
+            kg.kpm_1d_bang(op, NC, NR, NH, mu_host, host_psi, precision=args.precision,
+                           kernel=args.kernel if args.precision == "ff" else "auto")
         barrier()
         te = (time.perf_counter() - t0) / args.steps
         tt = torch.tensor([te], device="cuda")

@@ -95,9 +95,14 @@ typedef struct kpmgb_kpm1d_options {
                               NR <= 256); 7: float-float on packed FP32x2
                               pairs (real operators, 17..64 columns); 8:
                               warp tiles with batched operator-index loads
-                              (17..64 columns, at most 8 nonzeros per row).
-                              Automatic selection (0) is the register-gather
-                              kernel with the default shape.                  */
+                              (17..64 columns, at most 8 nonzeros per row);
+                              9: fixed-width padded rows (float-float; real
+                              operators with 33..64 columns or complex ones
+                              with 1..32; at most 16 nonzeros per row).
+                              Automatic selection (0) is the padded-row
+                              kernel for real operators where it serves the
+                              shape, else the register-gather kernel with the
+                              default shape.                                  */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {

@@ -85,6 +85,8 @@ Operator::~Operator() {
   cudaFree(csr.val);
   cudaFree(csr.val_real);
   cudaFree(csr.val_ff);
+  cudaFree(csr.ell_col);
+  cudaFree(csr.ell_val);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -636,6 +638,17 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
     k_split_values<<<blocks, 256, 0, op->stream>>>(c.val, nnz, is_real, c.val_ff, c.val_real);
     g_launches.fetch_add(1);
     CREATE_CUDA(cudaGetLastError());
+    // fixed-width padded rows for the padded-row step kernel (rows <= 16)
+    const int W = step::ell_width(max_nnz);
+    if (W > 0) {
+      CREATE_CUDA(cudaMalloc(&c.ell_col, (size_t)n * W * sizeof(int)));
+      CREATE_CUDA(cudaMalloc(&c.ell_val, (size_t)n * W * (is_real ? sizeof(float2) : sizeof(float4))));
+      if (step::launch_build_ell(c.rowptr, c.col, c.val_ff, is_real != 0, n, W, c.ell_col,
+                                 c.ell_val, op->stream) != 0)
+        CREATE_CUDA(cudaGetLastError());
+      g_launches.fetch_add(1);
+      c.ell_w = W;
+    }
     CREATE_CUDA(cudaStreamSynchronize(op->stream));
   }
 #undef CREATE_CUDA

@@ -74,6 +74,12 @@ struct DeviceCSR {
   int is_real = 0;
   int max_row_nnz = 0;
   double rmax = 0.0;  // max over rows of sum_k (|Re H_rk| + |Im H_rk|)
+  // float-float values in fixed-width padded rows (n x ell_w, ell_w = 0 when
+  // rows are longer than 16): padding slots hold 0 and repeat a column of
+  // their chunk of 4
+  int* ell_col = nullptr;
+  void* ell_val = nullptr;
+  int ell_w = 0;
   int* perm = nullptr;  // CSR position -> position in the caller's CSC arrays
 };
 
@@ -242,5 +248,14 @@ int launch_contract(const ContractArgs& a, int precision, int contraction,
                     cudaStream_t s);
 size_t contract_scratch_bytes(int64_t K, int nr, int nl, int precision, int contraction);
 int launch_mn_sym(double2* mu, int NC, cudaStream_t s);
+
+namespace step {
+// Fixed-width padded rows of the float-float values (kpmgb_step_ffe.cu):
+// width for rows of at most max_row_nnz nonzeros (0: rows too long), and the
+// device build from the CSR (0 on success).
+int ell_width(int max_row_nnz);
+int launch_build_ell(const int* rowptr, const int* col, const void* val_ff, bool real,
+                     int64_t NH, int W, int* ecol, void* eval, cudaStream_t s);
+}  // namespace step
 
 }  // namespace kpmgb

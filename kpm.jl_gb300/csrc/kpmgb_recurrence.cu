@@ -237,6 +237,8 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
           worst = std::max(worst, (size_t)grid_for(fx, NH, 32) * 2 * ncols * sizeof(double2));
         if (KernelFn fb = select_kernel_ffb(ncols, dot, H.is_real != 0, H.max_row_nnz))
           worst = std::max(worst, (size_t)grid_for(fb, NH, 32) * 2 * ncols * sizeof(double2));
+        if (KernelFn fe = select_kernel_ffe(ncols, dot, H.is_real != 0))
+          worst = std::max(worst, (size_t)grid_for(fe, NH, 32) * 2 * ncols * sizeof(double2));
       }
     }
   }
@@ -286,6 +288,26 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     p.ymax_clear = a.ymax_clear;
     p.rmax = (float)(H.rmax * (1.0 + 1e-6));
     p.anchor_slack = (float)((2.0 * H.max_row_nnz + 4.0) * 0x1p-22 + 0x1p-20);
+    p.ell_col = H.ell_col;
+    p.ell_val = H.ell_val;
+    p.ell_w = H.ell_w;
+    // Automatic selection takes the padded-row kernel for real operators
+    // (measured on GB300, 3D Anderson L=128, NR=64: 35.3% -> 42.6% of the HBM
+    // roofline against the CSR register-gather kernel); complex operators keep
+    // the CSR kernel with its exact-length last chunk (Haldane 256x256, NR=16:
+    // kpm_2d 182 ms against 275 ms with padded rows of 12).
+    const bool auto_padded = a.variant == 0 && H.ell_w > 0 && H.is_real;
+    if (precision == KPMGB_PREC_FF && (a.variant == 9 || auto_padded)) {
+      KernelFn fe = H.ell_w > 0 ? select_kernel_ffe(p.ncols, a.dot, H.is_real != 0) : nullptr;
+      if (fe || a.variant == 9) {
+        if (!fe)
+          return fail(KPMGB_ERR_ARGUMENT,
+                      "the padded-row kernel serves float-float steps of real operators with "
+                      "33..64 columns or complex ones with 1..32, rows of at most 16 nonzeros");
+        KPMGB_TRY(launch_step_kernel(fe, grid_for(fe, a.NH, 32), s, p));
+        continue;
+      }
+    }
     if (precision == KPMGB_PREC_FF && a.xmax && a.dot != DOT_NONE && a.variant == 3) {
       const Shape sh = pick_shape(p.ncols);
       KernelFn fn = select_kernel_ffg(sh, a.dot, H.is_real != 0);
@@ -367,6 +389,9 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
   if (precision == KPMGB_PREC_FF &&
       select_kernel_ffb(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz))
     cands.push_back({8, 0});
+  if (precision == KPMGB_PREC_FF && a0.H->ell_w > 0 &&
+      select_kernel_ffe(a0.NR, a0.dot, a0.H->is_real != 0))
+    cands.push_back({9, 0});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   KPMGB_CUDA(cudaEventCreate(&e0));
   cudaError_t ce = cudaEventCreate(&e1);

@@ -120,6 +120,10 @@ struct KParams {
   float* ymax_clear;     // maxima array zeroed by block 0 for the next step
   float rmax;            // max over rows of sum |H_rk| (re + im)
   float anchor_slack;    // relative slack of the H x anchor bound
+  // fixed-width padded rows (k_step_ffe): NH x ell_w columns / values
+  const int* ell_col;
+  const void* ell_val;
+  int ell_w;
 };
 
 template <int DOT>
@@ -729,6 +733,10 @@ KernelFn select_kernel_ffx(int ncols, int dot, bool real);
 // Float-float kernel with batched operator-index loads per warp tile
 // (kpmgb_step_ffb.cu): 17..64 columns, rows of at most 8 nonzeros.
 KernelFn select_kernel_ffb(int ncols, int dot, bool real, int max_row_nnz);
+
+// Float-float kernel over fixed-width padded rows (kpmgb_step_ffe.cu): real
+// operators with 33..64 columns, complex ones with 1..32; nullptr otherwise.
+KernelFn select_kernel_ffe(int ncols, int dot, bool real);
 
 }  // namespace step
 }  // namespace kpmgb

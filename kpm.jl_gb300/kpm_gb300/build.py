@@ -30,6 +30,7 @@ SOURCES = [
     "kpmgb_step_ffp.cu",
     "kpmgb_step_ffx.cu",
     "kpmgb_step_ffb.cu",
+    "kpmgb_step_ffe.cu",
     "kpmgb_small.cu",
     "kpmgb_contract.cu",
     "kpmgb_contract_tc.cu",

@@ -446,3 +446,73 @@ def test_batched_index_kernel_matches_oracle(NR, lr, complex_h):
     gat = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="gather", **kw)
     assert relerr(got, ref) < TOL["ff"]
     assert relerr(got, gat) < 1e-13
+
+
+def _ragged_herm(rng, n, max_row, complex_h):
+    """Hermitian operator with row lengths spread over 0..max_row (some rows
+    empty), scaled into the Chebyshev domain."""
+    rows, cols = [], []
+    for i in range(n):
+        k = int(rng.integers(0, max_row // 2 + 1))
+        for j in rng.choice(n, size=k, replace=False):
+            rows.append(i)
+            cols.append(int(j))
+    vals = rng.standard_normal(len(rows)) + (1j * rng.standard_normal(len(rows)) if complex_h else 0)
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    A = (A + A.conj().T).tocsc()
+    A.sum_duplicates()
+    deg = np.diff(A.indptr)
+    keep = deg <= max_row
+    A = sp.diags(keep.astype(float)) @ A @ sp.diags(keep.astype(float))
+    A = sp.csc_matrix(A)
+    A.eliminate_zeros()
+    return A / (1.05 * max(np.abs(np.linalg.eigvalsh(A.toarray())).max(), 1e-3))
+
+
+@pytest.mark.parametrize("NR", [33, 48, 64])
+@pytest.mark.parametrize("lr", [False, True])
+def test_padded_row_kernel_real_matches_oracle(NR, lr):
+    """kernel variant 9: fixed-width padded rows; the recurrence vectors are
+    bitwise those of the register-gather kernel, so the moments agree with it
+    to rounding of the (differently partitioned) sums"""
+    rng = np.random.default_rng(NR + 7 * lr)
+    H = (models.cubic_anderson(7, W=4.0, rng=rng) / 8.2).tocsc()
+    NH = H.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    if lr:
+        psr = ko.random_phase_vectors(rng, NH, NR)
+        kw = dict(psi_in_l=psi, psi_in_r=psr)
+        NC, ref = 41, ko.kpm_1d_lr(H, 41, psi, psr)
+    else:
+        kw = dict(psi_in=psi)
+        NC, ref = 96, ko.kpm_1d_doubling(H, 96, psi)
+    got = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="padded", **kw)
+    gat = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="gather", **kw)
+    assert relerr(got, ref) < TOL["ff"]
+    assert relerr(got, gat) < 1e-13
+
+
+@pytest.mark.parametrize("max_row", [3, 8, 13, 16])
+@pytest.mark.parametrize("complex_h,NR", [(False, 40), (False, 64), (True, 5), (True, 32)])
+def test_padded_row_kernel_ragged_rows(max_row, complex_h, NR):
+    """padding of short, empty and 4k+r rows for every table width 4..16"""
+    rng = np.random.default_rng(max_row * 3 + NR)
+    H = _ragged_herm(rng, 150, max_row, complex_h)
+    psi = ko.random_phase_vectors(rng, 150, NR)
+    got = kg.kpm_1d(H, 64, NR, psi_in=psi, avg_output=False, precision="ff", kernel="padded")
+    ref = ko.kpm_1d_doubling(H, 64, psi)
+    gat = kg.kpm_1d(H, 64, NR, psi_in=psi, avg_output=False, precision="ff", kernel="gather")
+    assert relerr(got, ref) < TOL["ff"]
+    assert relerr(got, gat) < 1e-13
+
+
+def test_padded_row_kernel_limits():
+    rng = np.random.default_rng(9)
+    H = (models.cubic_anderson(5, W=1.0, rng=rng) / 7.0).tocsc()
+    psi = ko.random_phase_vectors(rng, 125, 16)
+    with pytest.raises(kg.KPMArgumentError):   # real operator, 16 columns
+        kg.kpm_1d(H, 16, 16, psi_in=psi, precision="ff", kernel="padded")
+    dense = _ragged_herm(rng, 60, 40, False)   # rows longer than 16
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(dense, 16, 40, psi_in=ko.random_phase_vectors(rng, 60, 40), precision="ff",
+                  kernel="padded")
