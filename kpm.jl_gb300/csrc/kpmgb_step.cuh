@@ -389,9 +389,12 @@ __device__ __forceinline__ void ffnorm2(float (&S)[2], float (&C)[2], float4 a) 
 }
 
 #ifndef KPMGB_FF_FLUSH_ROWS
-#define KPMGB_FF_FLUSH_ROWS 16
+#define KPMGB_FF_FLUSH_ROWS 64
 #endif
 // per-lane float-float dot accumulators fold into FP64 every this many rows
+// (measured on GB300 with the padded-row kernel, 3D Anderson L=128: 64 rows
+// 42.8% of the HBM roofline against 42.0% with 16, whose FP64 conversions
+// kept the FP64 pipe 39% busy)
 constexpr int kFlushRows = KPMGB_FF_FLUSH_ROWS;
 
 #ifndef KPMGB_FF_EXACT_TAIL

@@ -52,8 +52,18 @@ __global__ void k_build_ell(const int* __restrict__ rowptr, const int* __restric
 
 }  // namespace
 
+// FP64 dot accumulators in a thread-private shared-memory slot (measured on
+// GB300, 3D Anderson L=128, NR=64: 43.5% of the HBM roofline against 42.8%
+// in registers, from the registers it frees)
+#ifndef KPMGB_FFE_SMEM_ACC
+#define KPMGB_FFE_SMEM_ACC 1
+#endif
+#ifndef KPMGB_FFE_MIN_BLOCKS
+#define KPMGB_FFE_MIN_BLOCKS (FFTune<CPL, REALH>::min_blocks)
+#endif
+
 template <int CPL, bool REALH, int DOT, bool FULL>
-__global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_step_ffe(KParams p) {
+__global__ void __launch_bounds__(kThreads, KPMGB_FFE_MIN_BLOCKS) k_step_ffe(KParams p) {
   pdl_enter();
   constexpr int LPR = 32;
   constexpr int CH = kEllChunk;
@@ -75,6 +85,10 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
   // gathers of this lane's columns start at x + c0 + lg (+ c * LPR)
   const float4* __restrict__ xl = x + p.c0 + lg;
 
+  // FP64 dot accumulators: in registers, or (KPMGB_FFE_SMEM_ACC) in a
+  // thread-private shared-memory slot touched once per flush
+  constexpr bool kSmemAcc = KPMGB_FFE_SMEM_ACC && ND > 0;
+  __shared__ double2 sacc[kSmemAcc ? kThreads : 1][kSmemAcc ? NDA * CPL : 1];
   double2 d[NDA][CPL];
   float dS[NDA][CPL][2], dC[NDA][CPL][2];
 #pragma unroll
@@ -82,6 +96,7 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
 #pragma unroll
     for (int c = 0; c < CPL; ++c) {
       d[k][c] = make_double2(0.0, 0.0);
+      if constexpr (kSmemAcc) sacc[threadIdx.x][k * CPL + c] = make_double2(0.0, 0.0);
       dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
     }
   int rows_since_flush = 0;
@@ -171,8 +186,15 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
         for (int k = 0; k < ND; ++k)
 #pragma unroll
           for (int c = 0; c < CPL; ++c) {
-            d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
-            d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
+            if constexpr (kSmemAcc) {
+              double2 v = sacc[threadIdx.x][k * CPL + c];
+              v.x += ff::join(dS[k][c][0], dC[k][c][0]);
+              v.y += ff::join(dS[k][c][1], dC[k][c][1]);
+              sacc[threadIdx.x][k * CPL + c] = v;
+            } else {
+              d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
+              d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
+            }
             dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
           }
       }
@@ -183,6 +205,7 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
     for (int k = 0; k < ND; ++k)
 #pragma unroll
       for (int c = 0; c < CPL; ++c) {
+        if constexpr (kSmemAcc) d[k][c] = sacc[threadIdx.x][k * CPL + c];
         d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
         d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
       }
