@@ -96,12 +96,11 @@ typedef struct kpmgb_kpm1d_options {
                               pairs (real operators, 17..64 columns); 8:
                               warp tiles with batched operator-index loads
                               (17..64 columns, at most 8 nonzeros per row);
-                              9: fixed-width padded rows (float-float; real
-                              operators with 33..64 columns or complex ones
-                              with 1..32; at most 16 nonzeros per row).
+                              9: fixed-width padded rows (float-float,
+                              5..64 columns, at most 16 nonzeros per row).
                               Automatic selection (0) is the padded-row
-                              kernel for real operators where it serves the
-                              shape, else the register-gather kernel with the
+                              kernel for real operators with 33..64 columns,
+                              else the register-gather kernel with the
                               default shape.                                  */
 } kpmgb_kpm1d_options;
 

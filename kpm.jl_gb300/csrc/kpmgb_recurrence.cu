@@ -195,6 +195,16 @@ int cols_per_launch() {
   return w;
 }
 
+// Automatic selection of the padded-row kernel for complex operators
+// (KPMGB_PADDED_COMPLEX=1; off by default).
+bool padded_complex() {
+  static const bool on = [] {
+    const char* e = std::getenv("KPMGB_PADDED_COMPLEX");
+    return e && std::atoi(e) != 0;
+  }();
+  return on;
+}
+
 int grid_for(KernelFn fn, int64_t NH, int lpr) {
   const int per_sm = blocks_per_sm(fn);
   const int64_t groups = kThreads / lpr;
@@ -238,7 +248,8 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
         if (KernelFn fb = select_kernel_ffb(ncols, dot, H.is_real != 0, H.max_row_nnz))
           worst = std::max(worst, (size_t)grid_for(fb, NH, 32) * 2 * ncols * sizeof(double2));
         if (KernelFn fe = select_kernel_ffe(ncols, dot, H.is_real != 0))
-          worst = std::max(worst, (size_t)grid_for(fe, NH, 32) * 2 * ncols * sizeof(double2));
+          worst = std::max(worst, (size_t)grid_for(fe, NH, ffe_lanes(ncols)) * 2 * ncols *
+                                      sizeof(double2));
       }
     }
   }
@@ -291,20 +302,23 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     p.ell_col = H.ell_col;
     p.ell_val = H.ell_val;
     p.ell_w = H.ell_w;
-    // Automatic selection takes the padded-row kernel for real operators
-    // (measured on GB300, 3D Anderson L=128, NR=64: 35.3% -> 42.6% of the HBM
-    // roofline against the CSR register-gather kernel); complex operators keep
-    // the CSR kernel with its exact-length last chunk (Haldane 256x256, NR=16:
-    // kpm_2d 182 ms against 275 ms with padded rows of 12).
-    const bool auto_padded = a.variant == 0 && H.ell_w > 0 && H.is_real;
+    // Automatic selection takes the padded-row kernel for real operators with
+    // 33..64 columns per launch (measured on GB300, 3D Anderson L=128, NR=64:
+    // 35.3% -> 43.5% of the HBM roofline against the CSR register-gather
+    // kernel).  Elsewhere the CSR kernel measured faster: complex Haldane
+    // 256x256, NR=16, kpm_2d 183 ms against 189 ms (exact-length last chunk);
+    // the L2-resident 2D Anderson L=64, NR=12, 7.4 ms against 8.3 ms per call
+    // (4 lanes x 3 columns against 16 x 1).
+    const bool auto_padded = a.variant == 0 && H.ell_w > 0 &&
+                             ((H.is_real && p.ncols > 32) || padded_complex());
     if (precision == KPMGB_PREC_FF && (a.variant == 9 || auto_padded)) {
       KernelFn fe = H.ell_w > 0 ? select_kernel_ffe(p.ncols, a.dot, H.is_real != 0) : nullptr;
       if (fe || a.variant == 9) {
         if (!fe)
           return fail(KPMGB_ERR_ARGUMENT,
-                      "the padded-row kernel serves float-float steps of real operators with "
-                      "33..64 columns or complex ones with 1..32, rows of at most 16 nonzeros");
-        KPMGB_TRY(launch_step_kernel(fe, grid_for(fe, a.NH, 32), s, p));
+                      "the padded-row kernel serves float-float steps with 5..64 columns "
+                      "and rows of at most 16 nonzeros");
+        KPMGB_TRY(launch_step_kernel(fe, grid_for(fe, a.NH, ffe_lanes(p.ncols)), s, p));
         continue;
       }
     }

@@ -737,9 +737,10 @@ KernelFn select_kernel_ffx(int ncols, int dot, bool real);
 // (kpmgb_step_ffb.cu): 17..64 columns, rows of at most 8 nonzeros.
 KernelFn select_kernel_ffb(int ncols, int dot, bool real, int max_row_nnz);
 
-// Float-float kernel over fixed-width padded rows (kpmgb_step_ffe.cu): real
-// operators with 33..64 columns, complex ones with 1..32; nullptr otherwise.
+// Float-float kernel over fixed-width padded rows (kpmgb_step_ffe.cu): 5..64
+// columns; nullptr otherwise.  ffe_lanes: lanes per row of its shape.
 KernelFn select_kernel_ffe(int ncols, int dot, bool real);
+int ffe_lanes(int ncols);
 
 }  // namespace step
 }  // namespace kpmgb

@@ -62,10 +62,9 @@ __global__ void k_build_ell(const int* __restrict__ rowptr, const int* __restric
 #define KPMGB_FFE_MIN_BLOCKS (FFTune<CPL, REALH>::min_blocks)
 #endif
 
-template <int CPL, bool REALH, int DOT, bool FULL>
+template <int LPR, int CPL, bool REALH, int DOT, bool FULL>
 __global__ void __launch_bounds__(kThreads, KPMGB_FFE_MIN_BLOCKS) k_step_ffe(KParams p) {
   pdl_enter();
-  constexpr int LPR = 32;
   constexpr int CH = kEllChunk;
   constexpr int ND = NDots<DOT>::value;
   constexpr int NDA = ND > 0 ? ND : 1;
@@ -215,27 +214,36 @@ __global__ void __launch_bounds__(kThreads, KPMGB_FFE_MIN_BLOCKS) k_step_ffe(KPa
 
 namespace {
 
-template <int CPL, bool REALH, bool FULL>
+template <int LPR, int CPL, bool REALH, bool FULL>
 KernelFn ffe_dot(int dot) {
   switch (dot) {
-    case DOT_DOUBLING: return k_step_ffe<CPL, REALH, DOT_DOUBLING, FULL>;
-    case DOT_LR2: return k_step_ffe<CPL, REALH, DOT_LR2, FULL>;
-    case DOT_LR1: return k_step_ffe<CPL, REALH, DOT_LR1, FULL>;
-    default: return k_step_ffe<CPL, REALH, DOT_NONE, FULL>;
+    case DOT_DOUBLING: return k_step_ffe<LPR, CPL, REALH, DOT_DOUBLING, FULL>;
+    case DOT_LR2: return k_step_ffe<LPR, CPL, REALH, DOT_LR2, FULL>;
+    case DOT_LR1: return k_step_ffe<LPR, CPL, REALH, DOT_LR1, FULL>;
+    default: return k_step_ffe<LPR, CPL, REALH, DOT_NONE, FULL>;
   }
+}
+
+template <bool REALH>
+KernelFn ffe_shape(int ncols, int dot) {
+  if (ncols <= 8) return ffe_dot<8, 1, REALH, false>(dot);
+  if (ncols <= 16) return ffe_dot<16, 1, REALH, false>(dot);
+  if (ncols <= 32) return ffe_dot<32, 1, REALH, false>(dot);
+  return ncols == 64 ? ffe_dot<32, 2, REALH, true>(dot) : ffe_dot<32, 2, REALH, false>(dot);
 }
 
 }  // namespace
 
-// Shapes whose k_step_ff chunk is 4: real operators with 33..64 columns (two
-// per lane) and complex operators with 1..32 columns (one per lane).
+// 5..64 columns: 8 or 16 lanes per row with one column each up to 8 and 16
+// columns, 32 lanes with one or two columns each above.  For real operators
+// with 33..64 columns and complex ones with 9..32 (chunks of 4 in k_step_ff)
+// the recurrence vectors are bitwise those of k_step_ff.
 KernelFn select_kernel_ffe(int ncols, int dot, bool real) {
-  if (real && ncols > 32 && ncols <= 64)
-    return ncols == 64 ? ffe_dot<2, true, true>(dot) : ffe_dot<2, true, false>(dot);
-  if (!real && ncols >= 1 && ncols <= 32)
-    return ncols == 32 ? ffe_dot<1, false, true>(dot) : ffe_dot<1, false, false>(dot);
-  return nullptr;
+  if (ncols < 5 || ncols > 64) return nullptr;
+  return real ? ffe_shape<true>(ncols, dot) : ffe_shape<false>(ncols, dot);
 }
+
+int ffe_lanes(int ncols) { return ncols <= 8 ? 8 : (ncols <= 16 ? 16 : 32); }
 
 int ell_width(int max_row_nnz) {
   if (max_row_nnz > 16) return 0;

@@ -493,9 +493,11 @@ def test_padded_row_kernel_real_matches_oracle(NR, lr):
 
 
 @pytest.mark.parametrize("max_row", [3, 8, 13, 16])
-@pytest.mark.parametrize("complex_h,NR", [(False, 40), (False, 64), (True, 5), (True, 32)])
+@pytest.mark.parametrize("complex_h,NR", [(False, 6), (False, 12), (False, 40), (False, 64),
+                                          (True, 5), (True, 16), (True, 32)])
 def test_padded_row_kernel_ragged_rows(max_row, complex_h, NR):
-    """padding of short, empty and 4k+r rows for every table width 4..16"""
+    """padding of short, empty and 4k+r rows for every table width 4..16, on
+    every lane shape (8, 16 and 32 lanes per row, one or two columns each)"""
     rng = np.random.default_rng(max_row * 3 + NR)
     H = _ragged_herm(rng, 150, max_row, complex_h)
     psi = ko.random_phase_vectors(rng, 150, NR)
@@ -503,15 +505,18 @@ def test_padded_row_kernel_ragged_rows(max_row, complex_h, NR):
     ref = ko.kpm_1d_doubling(H, 64, psi)
     gat = kg.kpm_1d(H, 64, NR, psi_in=psi, avg_output=False, precision="ff", kernel="gather")
     assert relerr(got, ref) < TOL["ff"]
-    assert relerr(got, gat) < 1e-13
+    # bitwise recurrence vectors where both kernels chunk by 4 (real H with 33..64
+    # columns, complex H with 9..32); chunks of 8 in k_step_ff elsewhere
+    same_chunks = (NR > 32) if not complex_h else (8 < NR <= 32)
+    assert relerr(got, gat) < (1e-13 if same_chunks else 1e-12)
 
 
 def test_padded_row_kernel_limits():
     rng = np.random.default_rng(9)
     H = (models.cubic_anderson(5, W=1.0, rng=rng) / 7.0).tocsc()
     psi = ko.random_phase_vectors(rng, 125, 16)
-    with pytest.raises(kg.KPMArgumentError):   # real operator, 16 columns
-        kg.kpm_1d(H, 16, 16, psi_in=psi, precision="ff", kernel="padded")
+    with pytest.raises(kg.KPMArgumentError):   # 4 columns
+        kg.kpm_1d(H, 16, 4, psi_in=psi[:, :4], precision="ff", kernel="padded")
     dense = _ragged_herm(rng, 60, 40, False)   # rows longer than 16
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d(dense, 16, 40, psi_in=ko.random_phase_vectors(rng, 60, 40), precision="ff",
