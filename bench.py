@@ -266,10 +266,10 @@ def workload_dos_small(args):
     out = {"workload": "kpm_1d, 2D square Anderson L=64 (NH=4096), W=2, NC=1024, NR=12",
            "metric": METRIC, "unit": UNIT}
     for prec in ("fp64", "ff"):
-        for mode in ("launches", "graph", "single"):
+        for mode in ("launches", "graph", "single", "cluster"):
             ms = _time_device(lambda: kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec,
                                                        stream=s, use_graph=mode == "graph",
-                                                       kernel="single" if mode == "single"
+                                                       kernel=mode if mode in ("single", "cluster")
                                                        else "auto"),
                               s, args.warmup, max(args.steps, 10), lambda: kg.sync(op, s))
             out[f"{prec}_{mode}"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}

@@ -97,11 +97,17 @@ typedef struct kpmgb_kpm1d_options {
                               warp tiles with batched operator-index loads
                               (17..64 columns, at most 8 nonzeros per row);
                               9: fixed-width padded rows (float-float,
-                              5..64 columns, at most 16 nonzeros per row).
-                              Automatic selection (0) is the padded-row
-                              kernel for real operators with 33..64 columns,
-                              else the register-gather kernel with the
-                              default shape.                                  */
+                              5..64 columns, at most 16 nonzeros per row);
+                              10: one thread-block cluster per probe column
+                              with the recurrence resident in distributed
+                              shared memory (one launch per call; NH up to
+                              ~100k rows).
+                              Automatic selection (0) is the cluster kernel
+                              (10) for NH <= 16384 and NH * NR <= 524288,
+                              else per-step launches of the padded-row kernel
+                              for real operators with 33..64 columns, else
+                              of the register-gather kernel with the default
+                              shape.                                          */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {

@@ -200,6 +200,27 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
     KPMGB_TRY(launch_colmax(sl[0], NH, (int)NR, ring(0), s));
     if (lr) KPMGB_TRY(launch_colmax(ws.bra.ptr, NH, (int)NR, bmax, s));
   }
+  // kernel_variant 10: one thread-block cluster per probe column, the
+  // recurrence resident in distributed shared memory.  Automatic selection
+  // takes it for small operators (measured on GB300 against per-step launches
+  // replayed from a CUDA graph: 1.1-4.3x faster for NH <= 16384 at NR <= 32,
+  // e.g. 2D Anderson L=64, NR=12, NC=1024: 3.6 ms against 6.9 ms).
+  // KPMGB_CLUSTER_AUTO=0 turns the automatic choice off.
+  static const bool cluster_auto_on = [] {
+    const char* e = std::getenv("KPMGB_CLUSTER_AUTO");
+    return !(e && std::atoi(e) == 0);
+  }();
+  const int variant = o ? o->kernel_variant : 0;
+  const bool auto_cluster =
+      variant == 0 && cluster_auto_on && NH <= 16384 && NH * NR <= 16384 * 32;
+  if (variant == 10 || auto_cluster) {
+    const int rc = launch_kpm1d_cluster(op->csr, NH, (int)NR, NC, lr, precision, sl[0],
+                                        lr ? ws.bra.ptr : nullptr, mu, mom_scale,
+                                        (!lr && o && o->stability_check) ? 2.25 : 0.0,
+                                        ws.sync.as<unsigned>() + 1, s);
+    if (variant == 10 || rc != KPMGB_ERR_ARGUMENT) return rc;
+    clear_error();  // no resident cluster of that shape: per-step launches
+  }
   // kernel_variant 6: the whole recurrence in one cooperative launch
   if (o && o->kernel_variant == 6) {
     KPMGB_TRY(ws.partials.ensure(std::max(ws.partials.bytes, small_partials_bytes((int)NR))));

@@ -249,6 +249,14 @@ int launch_contract(const ContractArgs& a, int precision, int contraction,
 size_t contract_scratch_bytes(int64_t K, int nr, int nl, int precision, int contraction);
 int launch_mn_sym(double2* mu, int NC, cudaStream_t s);
 
+// Cluster-resident recurrence (kpmgb_cluster.cu): one thread-block cluster
+// per probe column holds the column's recurrence in distributed shared memory;
+// psi / bra are the loaded row-major NH x NR blocks; moments [NC][NR].
+int launch_kpm1d_cluster(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, bool lr,
+                         int precision, const void* psi, const void* bra, double2* mu,
+                         const double* mom_scale, double growth_limit, unsigned* status,
+                         cudaStream_t s);
+
 namespace step {
 // Fixed-width padded rows of the float-float values (kpmgb_step_ffe.cu):
 // width for rows of at most max_row_nnz nonzeros (0: rows too long), and the

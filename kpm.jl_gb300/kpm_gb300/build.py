@@ -32,6 +32,7 @@ SOURCES = [
     "kpmgb_step_ffb.cu",
     "kpmgb_step_ffe.cu",
     "kpmgb_small.cu",
+    "kpmgb_cluster.cu",
     "kpmgb_contract.cu",
     "kpmgb_contract_tc.cu",
     "kpmgb_noalloc.cu",

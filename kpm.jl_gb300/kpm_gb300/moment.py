@@ -55,7 +55,7 @@ def _colmajor(psi, NH, NR, name):
     return np.asfortranarray(a, dtype=np.complex128)
 
 
-_VARIANT = {"auto": 0, "gather": 1, "tma": 2, "anchored": 3, "tune": 4, "pipelined": 5, "single": 6, "packed": 7, "batched": 8, "padded": 9}
+_VARIANT = {"auto": 0, "gather": 1, "tma": 2, "anchored": 3, "tune": 4, "pipelined": 5, "single": 6, "packed": 7, "batched": 8, "padded": 9, "cluster": 10}
 
 
 def _opts1d(precision, stability_check, kernel="auto", use_graph=False):

@@ -521,3 +521,59 @@ def test_padded_row_kernel_limits():
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d(dense, 16, 40, psi_in=ko.random_phase_vectors(rng, 60, 40), precision="ff",
                   kernel="padded")
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+@pytest.mark.parametrize("case", ["anderson16", "anderson64", "anderson_150", "peierls19",
+                                  "cubic28", "anderson_220"])
+@pytest.mark.parametrize("lr", [False, True])
+def test_cluster_kernel_matches_oracle(prec, case, lr):
+    """kernel variant 10: one thread-block cluster per probe column, the
+    recurrence in distributed shared memory (1, 8 and 16 CTAs per cluster; the
+    operator's rows cached in shared memory or read from global memory)"""
+    rng = np.random.default_rng(len(case) + 3 * lr)
+    if case == "anderson16":
+        H = (models.square_anderson(16, W=2.0, rng=rng) / 5.1).tocsc()      # 1 CTA
+    elif case == "anderson64":
+        H = (models.square_anderson(64, W=2.0, rng=rng) / 5.1).tocsc()      # 8 CTAs
+    elif case == "anderson_150":
+        H = (models.square_anderson(150, W=2.0, rng=rng) / 5.1).tocsc()     # 16 x 1407 rows
+    elif case == "anderson_220":
+        H = (models.square_anderson(220, W=2.0, rng=rng) / 5.1).tocsc()     # 16 x 3025 rows:
+        # the CTAs' rows of the operator do not fit beside the slots (uncached path)
+    elif case == "cubic28":
+        H = (models.cubic_anderson(28, W=4.0, rng=rng) / 8.2).tocsc()       # 16 x 1372 rows
+    else:
+        H = _peierls_square(19, rng)                                        # complex, 361 rows
+    NH = H.shape[0]
+    NR = 5 if case != "anderson64" else 12
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    if lr:
+        psr = ko.random_phase_vectors(rng, NH, NR)
+        got = kg.kpm_1d(H, 37, NR, psi_in_l=psi, psi_in_r=psr, avg_output=False, precision=prec,
+                        kernel="cluster")
+        ref = ko.kpm_1d_lr(H, 37, psi, psr)
+        tol = TOL[prec]
+    else:
+        got = kg.kpm_1d(H, 96, NR, psi_in=psi, avg_output=False, precision=prec, kernel="cluster")
+        ref = ko.kpm_1d_doubling(H, 96, psi)
+        # FP64 noise floor of the doubling moments on this operator: the oracle's
+        # own doubling and step-by-step paths differ by up to 2e-12 on 22500 rows
+        floor = relerr(ref, ko.kpm_1d_lr(H, 96, psi, psi))
+        tol = max(TOL[prec], 3 * floor)
+    assert relerr(got, ref) < tol
+
+
+def test_cluster_kernel_growth_and_capacity():
+    rng = np.random.default_rng(4)
+    H = (models.square_anderson(12, W=0.0, rng=rng) / 3.0).tocsc()   # spectrum beyond [-1, 1]
+    psi = ko.random_phase_vectors(rng, 144, 4)
+    with pytest.raises(kg.KPMNumericalError):
+        kg.kpm_1d(H, 64, 4, psi_in=psi, kernel="cluster", stability_check=True)
+    big = (models.cubic_anderson(50, W=1.0, rng=rng) / 7.0).tocsc()  # 125000 rows per column
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(big, 8, 2, psi_in=ko.random_phase_vectors(rng, 125000, 2), kernel="cluster")
+    # the operator and context stay usable
+    ok = (models.square_anderson(12, W=1.0, rng=rng) / 5.0).tocsc()
+    got = kg.kpm_1d(ok, 32, 4, psi_in=psi, avg_output=False, kernel="cluster")
+    assert relerr(got, ko.kpm_1d_doubling(ok, 32, psi)) < TOL["fp64"]
