@@ -60,7 +60,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--workload", default="dos",
-                   choices=["dos", "dos-small", "cond", "ensemble", "grad", "action", "dsigma"],
+                   choices=["dos", "dos-small", "cond", "ensemble", "grad", "action", "dsigma",
+                            "published"],
                    help="dos (default): the headline kpm_1d line on the 3D Anderson model; "
                         "the others print one JSON line each: dos-small (2D Anderson L=64), "
                         "cond (kpm_2d + Kubo-Bastin on the Haldane model), ensemble (256 "
@@ -366,6 +367,87 @@ def workload_dsigma(args):
     return out
 
 
+def _square_lattice(L):
+    """Periodic square lattice with hopping -1 on the four directed nearest-
+    neighbour entries of every site and no diagonal, as the reference's own
+    benchmark builds it (benchmarks/core_bench.jl:35-63); with currents."""
+    import scipy.sparse as sp
+    x, y = np.meshgrid(np.arange(L), np.arange(L), indexing="ij")
+    x, y = x.ravel(), y.ravel()
+    site = lambda a, b: (a % L) + L * (b % L)
+    rows, cols, dxs, dys = [], [], [], []
+    for ddx, ddy in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+        rows.append(site(x, y))
+        cols.append(site(x + ddx, y + ddy))
+        dxs.append(np.full(x.shape, -ddx))
+        dys.append(np.full(x.shape, -ddy))
+    r, c = np.concatenate(rows), np.concatenate(cols)
+    v = -np.ones(r.shape, dtype=np.complex128)
+    n = L * L
+    H = sp.csc_matrix((v, (r, c)), shape=(n, n))
+    Jx = sp.csc_matrix((v * np.concatenate(dxs), (r, c)), shape=(n, n))
+    Jy = sp.csc_matrix((v * np.concatenate(dys), (r, c)), shape=(n, n))
+    return H, Jx, Jy
+
+
+def workload_published(args):
+    """The reference's own benchmark suite (benchmarks/core_bench.jl), whose
+    A100 times it publishes: kpm_1d DOS on the 256x256 (NC=1024, NR=8) and
+    512x512 (NC=512, NR=4) periodic square lattices, kpm_2d on 128x128
+    (NC=64, NR=4; default blocking and arr_size=64), chebyshev_action on
+    256x256 (NC=1024, NR=8, K=2).  Timed end to end through the host API from
+    host arrays: `per_call_operator` builds the device operator inside every
+    call (as the reference converts and uploads H per call), `resident` reuses
+    it.  Default (FP64) precision, as the reference."""
+    import kpm_gb300 as kg
+    rng = np.random.default_rng(42)
+    steps = max(args.steps, 3)
+    out = {"workload": "KPM.jl benchmarks/core_bench.jl suite (periodic square lattices)",
+           "reference_a100_s": {"kpm_1d_NH65536_NC1024_NR8": 0.056766,
+                                "kpm_1d_NH262144_NC512_NR4": 0.058475,
+                                "kpm_2d_NH16384_NC64_NR4_default": 0.010318,
+                                "kpm_2d_NH16384_NC64_NR4_arr64": 0.006348},
+           "reference_a100_source": "benchmarks/results/perf-core-mike-a100.json:8-12"}
+    for L, NC, NR in ((256, 1024, 8), (512, 512, 4)):
+        H, _, _ = _square_lattice(L)
+        a, Hn = kg.normalizeH(H)
+        NH = L * L
+        psi = kg.random_phase_vectors(rng, NH, NR)
+        op = kg.GB300Operator(Hn)
+        key = f"kpm_1d_NH{NH}_NC{NC}_NR{NR}"
+        out[key] = {
+            "per_call_operator_s": _time_host(lambda: kg.kpm_1d(Hn, NC, NR, NH, psi_in=psi), 1,
+                                              steps) / 1e3,
+            "resident_s": _time_host(lambda: kg.kpm_1d(op, NC, NR, NH, psi_in=psi), 1, steps) / 1e3,
+            "resident_ff_s": _time_host(lambda: kg.kpm_1d(op, NC, NR, NH, psi_in=psi,
+                                                          precision="ff"), 1, steps) / 1e3}
+    H, Jx, Jy = _square_lattice(128)
+    a, Hn = kg.normalizeH(H)
+    NH = 128 * 128
+    psi = kg.random_phase_vectors(rng, NH, 4)
+    ops = [kg.GB300Operator(M) for M in (Hn, Jx, Jy)]
+    for tag, kw in (("default", {}), ("arr64", {"arr_size": 64})):
+        out[f"kpm_2d_NH16384_NC64_NR4_{tag}"] = {
+            "per_call_operator_s": _time_host(lambda: kg.kpm_2d(Hn, Jx, Jy, 64, 4, NH, psi_in=psi,
+                                                                **kw), 1, steps) / 1e3,
+            "resident_s": _time_host(lambda: kg.kpm_2d(*ops, 64, 4, NH, psi_in=psi, **kw), 1,
+                                     steps) / 1e3}
+    H, _, _ = _square_lattice(256)
+    a, Hn = kg.normalizeH(H)
+    V = kg.random_phase_vectors(rng, 65536, 8)
+    n = np.arange(1024)
+    C = np.stack([np.where(n == 0, 1.0, 2.0) * np.cos(n * np.pi / 2),
+                  np.where(n == 0, 1.0, 2.0) * np.cos(n * 1.3)], axis=1)
+    op = kg.GB300Operator(Hn)
+    out["chebyshev_action_NH65536_NC1024_NR8_K2"] = {
+        "resident_s": _time_host(lambda: kg.chebyshev_action(op, V, C, check_every=0), 1,
+                                 steps) / 1e3}
+    for k, ref in out["reference_a100_s"].items():
+        ours = out[k]["per_call_operator_s"]
+        out[k]["reference_a100_over_ours_per_call"] = ref / ours
+    return out
+
+
 def workload_ensemble(args):
     """256 realisations of the 2D Anderson model, L ~ U{24..96}, W ~ U[1, 8],
     NC=512, NR=8: one persistent ensemble launch against per-member calls."""
@@ -452,7 +534,8 @@ def main():
         torch.cuda.set_device(local)
         fn = {"dos-small": workload_dos_small, "cond": workload_cond,
               "ensemble": workload_ensemble, "grad": workload_grad,
-              "action": workload_action, "dsigma": workload_dsigma}[args.workload]
+              "action": workload_action, "dsigma": workload_dsigma,
+              "published": workload_published}[args.workload]
         res = fn(args)
         res["version"] = __import__("kpm_gb300").version()
         if rank == 0:

@@ -143,6 +143,7 @@ __device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CP
     return;
   } else {
     __shared__ double2 red[NW][ND][LPR * CPL];
+    __shared__ double2 tmp[THREADS];  // the last block's part sums
     __shared__ unsigned s_ticket;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -185,21 +186,30 @@ __device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CP
     __syncthreads();
     if (s_ticket != gridDim.x - 1) return;
     __threadfence();
-    // Last block: fixed-order sum over blocks.  Threads split the blocks into
-    // P interleaved parts, then the parts are added in order.
-    // reuse `red` (NW*ND*LPR*CPL entries) for the P x NE part sums
-    double2* tmp = &red[0][0][0];
-    const int P = max(1, min(THREADS / NE, (int)(sizeof(red) / sizeof(double2)) / NE));
-    __syncthreads();
+    // Last block: fixed-order sum over blocks.  All threads take part: the
+    // blocks are split into P = THREADS / NE interleaved parts, each summed
+    // with four interleaved accumulators (four loads in flight per thread),
+    // then the accumulators and the parts are added in a fixed order, so the
+    // result does not depend on which block finished last.
+    const int P = max(1, THREADS / NE);
+    const int G = (int)gridDim.x;
     for (int idx = threadIdx.x; idx < P * NE; idx += THREADS) {
       const int part = idx / NE, e = idx - part * NE;
-      double2 s = make_double2(0.0, 0.0);
-      for (int b = part; b < (int)gridDim.x; b += P) {
-        const double2 v = __ldcg(p.partials + (size_t)b * NE + e);
-        s.x += v.x;
-        s.y += v.y;
+      double2 s4[4] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0),
+                       make_double2(0.0, 0.0)};
+      for (int b = part; b < G; b += 4 * P) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int bq = b + q * P;
+          if (bq < G) {
+            const double2 v = __ldcg(p.partials + (size_t)bq * NE + e);
+            s4[q].x += v.x;
+            s4[q].y += v.y;
+          }
+        }
       }
-      tmp[part * NE + e] = s;
+      tmp[part * NE + e] = make_double2((s4[0].x + s4[1].x) + (s4[2].x + s4[3].x),
+                                        (s4[0].y + s4[1].y) + (s4[2].y + s4[3].y));
     }
     __syncthreads();
     for (int ee = threadIdx.x; ee < NE; ee += THREADS) {
