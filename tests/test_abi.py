@@ -92,3 +92,28 @@ def test_blocking_rule_matches_reference_arithmetic():
         kg.kpm_2d_blocking(NH, NR, NC, workspace_bytes=10 * one - 1)
     c = kg.kpm_2d_blocking(NH, NR, NC, workspace_bytes=10 * one, arr_size=27, right_block=9)
     assert (c["arr_size"], c["right_block"]) == (27, 9)
+
+
+def test_derivative_host_checks_and_tangent_scale(built_lib):
+    """The forward-mode derivatives validate shapes and probes on the host
+    before any device work; the tangent scale is an exact power of two near
+    sqrt(NC) |dH|_inf (or |dJ| / |J|)."""
+    import math
+    import kpm_gb300 as kg
+    from kpm_gb300 import moment
+    H = sp.identity(8, dtype=complex, format="csc") * 0.5
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_derivative(H, H[:4, :4], 8, 1, psi_in=np.ones((8, 1)))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_derivative(H, H, 8, 2, psi_in=np.ones((8, 1)))
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_2d_derivative(H, H, H, None, H, None, 8, 1, 8)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_2d_derivative(H, H, H, None, H[:4, :4], None, 8, 1, 8, psi_in=np.ones((8, 1)))
+    dH = sp.csr_matrix(H * 3.0)          # |dH|_inf = 1.5
+    s = moment._tangent_scale(256, dH)   # sqrt(256) * 1.5 = 24 -> 2^-5
+    assert s == math.ldexp(1.0, -5)
+    J = sp.csr_matrix(H)
+    s = moment._tangent_scale(4, dH * 0.0, ((J, J * 64.0),))   # |dJ| / |J| = 64
+    assert s == math.ldexp(1.0, -6)
+    assert moment._tangent_scale(16, sp.csr_matrix((8, 8))) == 1.0
