@@ -188,28 +188,37 @@ __device__ __forceinline__ void reduce_finalize(double2 (&d)[ND > 0 ? ND : 1][CP
     __threadfence();
     // Last block: fixed-order sum over blocks.  All threads take part: the
     // blocks are split into P = THREADS / NE interleaved parts, each summed
-    // with four interleaved accumulators (four loads in flight per thread),
-    // then the accumulators and the parts are added in a fixed order, so the
-    // result does not depend on which block finished last.
+    // with kAcc interleaved accumulators (kAcc loads in flight per thread:
+    // the partials come from L2, and one block reads them all), then the
+    // accumulators and the parts are added in a fixed order, so the result
+    // does not depend on which block finished last.
+    constexpr int kAcc = 8;
     const int P = max(1, THREADS / NE);
     const int G = (int)gridDim.x;
     for (int idx = threadIdx.x; idx < P * NE; idx += THREADS) {
       const int part = idx / NE, e = idx - part * NE;
-      double2 s4[4] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0),
-                       make_double2(0.0, 0.0)};
-      for (int b = part; b < G; b += 4 * P) {
+      double2 sa[kAcc];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+      for (int q = 0; q < kAcc; ++q) sa[q] = make_double2(0.0, 0.0);
+      for (int b = part; b < G; b += kAcc * P) {
+#pragma unroll
+        for (int q = 0; q < kAcc; ++q) {
           const int bq = b + q * P;
           if (bq < G) {
             const double2 v = __ldcg(p.partials + (size_t)bq * NE + e);
-            s4[q].x += v.x;
-            s4[q].y += v.y;
+            sa[q].x += v.x;
+            sa[q].y += v.y;
           }
         }
       }
-      tmp[part * NE + e] = make_double2((s4[0].x + s4[1].x) + (s4[2].x + s4[3].x),
-                                        (s4[0].y + s4[1].y) + (s4[2].y + s4[3].y));
+#pragma unroll
+      for (int w = kAcc / 2; w > 0; w >>= 1)
+#pragma unroll
+        for (int q = 0; q < w; ++q) {
+          sa[q].x += sa[q + w].x;
+          sa[q].y += sa[q + w].y;
+        }
+      tmp[part * NE + e] = sa[0];
     }
     __syncthreads();
     for (int ee = threadIdx.x; ee < NE; ee += THREADS) {
