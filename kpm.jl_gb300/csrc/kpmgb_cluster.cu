@@ -412,8 +412,17 @@ int launch_kpm1d_cluster(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, boo
   if (cache) smem += cache_bytes;
   const void* fn = ff ? (real ? cluster_fn<true, true>(cache) : cluster_fn<true, false>(cache))
                       : (real ? cluster_fn<false, true>(cache) : cluster_fn<false, false>(cache));
-  KPMGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  if (cs > 8) KPMGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  // setup failures (no cluster support, attribute limits) are "does not
+  // apply here" (argument status), so automatic selection falls back
+  auto setup = [&](cudaError_t e) {
+    if (e == cudaSuccess) return KPMGB_OK;
+    cudaGetLastError();
+    return fail(KPMGB_ERR_ARGUMENT, "the cluster-resident kernel cannot run here: %s",
+                cudaGetErrorString(e));
+  };
+  KPMGB_TRY(setup(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)));
+  if (cs > 8)
+    KPMGB_TRY(setup(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1)));
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)(NR * cs));
   cfg.blockDim = dim3(kCT);
@@ -427,7 +436,7 @@ int launch_kpm1d_cluster(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, boo
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int nclusters = 0;
-  KPMGB_CUDA(cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg));
+  KPMGB_TRY(setup(cudaOccupancyMaxActiveClusters(&nclusters, fn, &cfg)));
   if (nclusters < 1)
     return fail(KPMGB_ERR_ARGUMENT, "a cluster of %d CTAs with %zu bytes of shared memory each "
                                     "cannot be resident on this device", cs, smem);

@@ -49,16 +49,23 @@ def test_golden_ring_exact_trace(prec):
     assert relerr(mu, f["mu_exact"]) < TOL[prec]
 
 
+# small operators run as one cluster launch by default ("auto"); "gather"
+# keeps the per-step kernels and their lane-group shapes under test
+KERNELS = ["auto", "gather"]
+
+
 @pytest.mark.parametrize("NR", [1, 2, 3, 4, 5, 8, 12, 16, 24, 32, 33, 64, 100, 128, 130, 200])
 @pytest.mark.parametrize("prec", ["fp64", "ff"])
-def test_probe_counts(NR, prec):
-    """Every lane-group shape and the >128-column batching."""
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_probe_counts(NR, prec, kernel):
+    """Every lane-group shape and the >128-column batching (per-step kernels),
+    and every probe count on the cluster path."""
     rng = np.random.default_rng(100 + NR)
     H = models.square_anderson(16, W=2.0, rng=rng)
     a, _, Hn = ko.normalizeH(H)
     psi = ko.random_phase_vectors(rng, 256, NR)
     ref = ko.kpm_1d_doubling(Hn, 64, psi)
-    got = kg.kpm_1d(Hn, 64, NR, psi_in=psi, avg_output=False, precision=prec)
+    got = kg.kpm_1d(Hn, 64, NR, psi_in=psi, avg_output=False, precision=prec, kernel=kernel)
     assert relerr(got, ref) < TOL[prec]
 
 
@@ -96,7 +103,8 @@ def test_complex_haldane(prec, lr):
 
 
 @pytest.mark.parametrize("prec", ["fp64", "ff"])
-def test_ragged_empty_and_long_rows(prec):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_ragged_empty_and_long_rows(prec, kernel):
     """Rows with 0, 1, ... 40 nonzeros (several float-float chunks), complex values."""
     rng = np.random.default_rng(3)
     n = 300
@@ -113,36 +121,38 @@ def test_ragged_empty_and_long_rows(prec):
     H = sp.csc_matrix(Hd)
     psi = ko.random_phase_vectors(rng, n, 6)
     ref = ko.kpm_1d_doubling(H, 96, psi)
-    got = kg.kpm_1d(H, 96, 6, psi_in=psi, avg_output=False, precision=prec)
+    got = kg.kpm_1d(H, 96, 6, psi_in=psi, avg_output=False, precision=prec, kernel=kernel)
     assert relerr(got, ref) < TOL[prec]
     ref = ko.kpm_1d_lr(H, 95, psi[:, ::-1].copy(), psi)
     got = kg.kpm_1d(H, 95, 6, psi_in_l=psi[:, ::-1].copy(), psi_in_r=psi, avg_output=False,
-                    precision=prec)
+                    precision=prec, kernel=kernel)
     assert relerr(got, ref) < TOL[prec]
 
 
 @pytest.mark.parametrize("prec", ["fp64", "ff"])
-def test_unnormalized_and_zero_columns(prec):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_unnormalized_and_zero_columns(prec, kernel):
     """mu scales as |c|^2 (test/dos_test.jl:80-93); a zero probe gives zero moments."""
     rng = np.random.default_rng(13)
     H = sp.csc_matrix(rand_herm(rng, 32, scale=2.0))
     psi = ko.random_phase_vectors(rng, 32, 4) * np.array([1.0, 1e6, 1e-7, 0.0])
     ref = ko.kpm_1d_doubling(H, 16, psi)
-    got = kg.kpm_1d(H, 16, 4, psi_in=psi, avg_output=False, precision=prec)
+    got = kg.kpm_1d(H, 16, 4, psi_in=psi, avg_output=False, precision=prec, kernel=kernel)
     for i in range(3):
         assert relerr(got[i], ref[i]) < TOL[prec]
     assert np.all(got[3] == 0)
 
 
 @pytest.mark.parametrize("prec", ["fp64", "ff"])
-def test_deterministic(prec):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_deterministic(prec, kernel):
     rng = np.random.default_rng(11)
     H = models.square_anderson(32, W=1.0, rng=rng)
     _, _, Hn = ko.normalizeH(H)
     op = kg.GB300Operator(Hn)
     psi = ko.random_phase_vectors(rng, 1024, 8)
-    m1 = kg.kpm_1d(op, 128, 8, psi_in=psi, avg_output=False, precision=prec)
-    m2 = kg.kpm_1d(op, 128, 8, psi_in=psi, avg_output=False, precision=prec)
+    m1 = kg.kpm_1d(op, 128, 8, psi_in=psi, avg_output=False, precision=prec, kernel=kernel)
+    m2 = kg.kpm_1d(op, 128, 8, psi_in=psi, avg_output=False, precision=prec, kernel=kernel)
     assert np.array_equal(m1, m2)
 
 
@@ -265,20 +275,22 @@ def test_anchored_kernel_matches_oracle(NR, lr):
 @pytest.mark.parametrize("prec", ["fp64", "ff"])
 @pytest.mark.parametrize("lr", [False, True])
 def test_cuda_graph_replay_identical(prec, lr):
-    """use_graph captures the recurrence once and replays it: results are
-    bitwise those of direct launches, on the first call and on replays, and a
-    changed NC or probe count is captured afresh."""
+    """use_graph captures the per-step recurrence once and replays it:
+    results are bitwise those of direct launches, on the first call and on
+    replays, and a changed NC or probe count is captured afresh."""
     rng = np.random.default_rng(17)
     H = models.square_anderson(24, W=2.0, rng=rng)
     op = kg.GB300Operator((H / 5.1).tocsc())
     for NC, NR in ((128, 12), (128, 12), (64, 12), (64, 7)):
         psi = ko.random_phase_vectors(rng, 576, NR)
         kw = dict(psi_in_l=psi, psi_in_r=psi[:, ::-1].copy()) if lr else dict(psi_in=psi)
-        ref = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, **kw)
+        ref = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, kernel="gather", **kw)
         n0 = kg.kernel_launch_count()
-        g1 = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, use_graph=True, **kw)
+        g1 = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, use_graph=True,
+                       kernel="gather", **kw)
         n1 = kg.kernel_launch_count()
-        g2 = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, use_graph=True, **kw)
+        g2 = kg.kpm_1d(op, NC, NR, avg_output=False, precision=prec, use_graph=True,
+                       kernel="gather", **kw)
         n2 = kg.kernel_launch_count()
         assert np.array_equal(g1, ref) and np.array_equal(g2, ref)
         assert n2 - n1 == n1 - n0 > 0
@@ -297,7 +309,8 @@ def test_cuda_graph_device_api_stream():
     mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
     for use_graph in (False, True, True):
         mu_t.zero_()
-        kg.kpm_1d_device(op, NC, psi_t, mu_t, precision="ff", stream=s, use_graph=use_graph)
+        kg.kpm_1d_device(op, NC, psi_t, mu_t, precision="ff", stream=s, use_graph=use_graph,
+                         kernel="gather")
         kg.sync(op, s)
         outs.append(mu_t.cpu().numpy())
     assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
