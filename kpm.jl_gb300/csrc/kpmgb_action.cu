@@ -24,11 +24,16 @@ namespace {
 constexpr int kKT = 8;      // outputs accumulated per pass
 constexpr int kMaxKc = 32;  // vectors per chunk
 
-// out[k0 + kk][m] += sum_{j < cnt} Ct[j][k0 + kk] * slot((n0 + j) % S)[m]
+// out[k0 + kk][m] += sum_{j < cnt} Ct[j][k0 + kk] * slot((n0 + j) % S)[m], KT
+// outputs per pass (the FP64 work is 4 KT FMAs per vector element, so a pass
+// covers no more outputs than remain: measured on GB300 for K = 2, a fixed
+// pass of 8 took 0.91 ms per chunk of 32 vectors at NH x NR = 524288)
+template <int KT>
 __global__ void __launch_bounds__(256)
 k_action_accumulate(const double2* __restrict__ ring, int S, int64_t M, int64_t n0, int cnt,
                     const double2* __restrict__ Ct /* [NC][K] */, int K, int k0,
                     double2* __restrict__ out) {
+  constexpr int kKT = KT;
   __shared__ double2 c[kMaxKc][kKT];
   const int kt = min(kKT, K - k0);
   for (int e = threadIdx.x; e < cnt * kKT; e += blockDim.x) {
@@ -176,9 +181,21 @@ int run_chebyshev_action(Operator* op, int64_t NH, int64_t NR, const double2* V_
     return KPMGB_OK;
   };
   auto accumulate = [&](int64_t n0, int cnt) -> int {
-    for (int k0 = 0; k0 < K; k0 += kKT) {
-      k_action_accumulate<<<grid_m(M), 256, 0, s>>>(ring, S, M, n0, cnt, Ct_dev, (int)K, k0, acc);
+    // each pass covers take = min(outputs left, kKT) outputs with the
+    // smallest pass width that holds them
+    for (int64_t k0 = 0; k0 < K;) {
+      const int take = (int)std::min<int64_t>(K - k0, kKT);
+      const int g = grid_m(M);
+      if (take > 4)
+        k_action_accumulate<8><<<g, 256, 0, s>>>(ring, S, M, n0, cnt, Ct_dev, (int)K, (int)k0, acc);
+      else if (take > 2)
+        k_action_accumulate<4><<<g, 256, 0, s>>>(ring, S, M, n0, cnt, Ct_dev, (int)K, (int)k0, acc);
+      else if (take == 2)
+        k_action_accumulate<2><<<g, 256, 0, s>>>(ring, S, M, n0, cnt, Ct_dev, (int)K, (int)k0, acc);
+      else
+        k_action_accumulate<1><<<g, 256, 0, s>>>(ring, S, M, n0, cnt, Ct_dev, (int)K, (int)k0, acc);
       KPMGB_LAUNCHED();
+      k0 += take;
     }
     return KPMGB_OK;
   };

@@ -68,9 +68,10 @@ def test_action_promotion_and_vector_forms():
     assert np.array_equal(out, full)
 
 
-@pytest.mark.parametrize("NC,K", [(1, 1), (2, 3), (33, 9), (200, 10)])
+@pytest.mark.parametrize("NC,K", [(1, 1), (2, 3), (40, 6), (33, 9), (200, 10), (70, 13)])
 def test_action_large_sparse(NC, K):
-    """chunk boundaries (32 vectors) and output tiles (8 per pass) at odd sizes"""
+    """chunk boundaries (32 vectors) and output passes (1, 2, 4 or 8 outputs
+    wide, the last one padded) at odd sizes"""
     rng = np.random.default_rng(NC + K)
     H = models.square_anderson(40, W=1.5, rng=rng)
     H = (H / 4.9).tocsc()
