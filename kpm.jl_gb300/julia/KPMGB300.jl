@@ -237,6 +237,21 @@ function kpm_1d_grad(H::SparseMatrixCSC, NC::Int64, psi_in::AbstractMatrix, g::A
     return SparseMatrixCSC(size(Hc, 1), size(Hc, 2), copy(Hc.colptr), copy(Hc.rowval), out)
 end
 
+# Directional derivative of the kpm_1d moments along H + t dH (forward mode):
+# the l/r recurrence over [H 0; dH H] with ket [ψ; 0] and bra [0; ψ], the
+# direction pre-scaled by a power of two near sqrt(NC) |dH|.  Returns NR × NC.
+function kpm_1d_derivative(H::SparseMatrixCSC, dH, NC::Int64, NR::Int64, NH::Int64,
+                           psi_in::AbstractMatrix; kwargs...)
+    Z = spzeros(ComplexF64, NH, NH)
+    g = sqrt(NC) * opnorm(dH, Inf)
+    s = g > 0 ? exp2(-round(log2(g))) : 1.0
+    Haug = GB300CSR([H Z; s .* SparseMatrixCSC{ComplexF64,Int64}(dH) H])
+    z = zeros(ComplexF64, NH, NR)
+    dμ = Matrix{ComplexF64}(undef, NR, NC)
+    KPM.kpm_1d!(Haug, NC, NR, 2NH, dμ, [z; psi_in], [psi_in; z]; kwargs...)
+    return dμ ./ s
+end
+
 # Directional derivative of the kpm_2d moments along (H, Jα, Jβ) + t (dH, dJα, dJβ)
 # (forward mode; no reference counterpart): one kpm_2d over the 2NH block operators
 # [H 0; dH H], [Jα 0; dJα Jα], [dJβ Jβ; Jβ 0] with probes [ψl; 0], [ψr; 0], the
