@@ -132,8 +132,8 @@ __global__ void __launch_bounds__(kCT, 1) k_kpm1d_cluster(ClusterParams p) {
                                        typename std::conditional<REALH, double, double2>::type>::type;
   extern __shared__ __align__(16) unsigned char smem[];
   V* slot = reinterpret_cast<V*>(smem);                          // [2][rows]
-  // partials of every CTA of the cluster, pushed into each rank's copy (only
-  // rank 0's is read): [2 parity][kMaxCluster][2 dots]
+  // partials of every CTA of the cluster, which each CTA stores into rank 0's
+  // copy (the other ranks' copies stay unused): [2 parity][kMaxCluster][2 dots]
   double2* part = reinterpret_cast<double2*>(slot + 2 * p.rows);
   double2* red = part + 2 * kMaxCluster * 2;                      // [2][kWarpsCT]
   HT* s_val = reinterpret_cast<HT*>(red + 2 * kWarpsCT);          // [cap]  (CACHE)
