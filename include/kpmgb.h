@@ -103,8 +103,10 @@ typedef struct kpmgb_kpm1d_options {
                               shared memory (one launch per call; NH up to
                               ~100k rows).
                               Automatic selection (0) is the cluster kernel
-                              (10) for NH <= 16384 and NH * NR <= 524288
-                              (FP64: NH <= 32768, NH * NR <= 1048576),
+                              (10) for small operators (float-float:
+                              NH <= 16384, NH * NR <= 131072; FP64:
+                              NH <= 16384, NH * NR <= 524288, or NH <= 32768
+                              with NR <= 4),
                               else per-step launches of the padded-row kernel
                               for real operators with 33..64 columns, else
                               of the register-gather kernel with the default

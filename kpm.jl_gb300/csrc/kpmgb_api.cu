@@ -204,10 +204,10 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   // recurrence resident in distributed shared memory.  Automatic selection
   // takes it for small operators, where it measured faster on GB300 than
   // per-step launches replayed from a CUDA graph (2D Anderson, NC=1024):
-  // 1.1-4.3x for NH <= 16384 at NR <= 32 in both precisions (L=64, NR=12:
-  // 3.6 ms against 6.9 ms), and in FP64 also at NH = 32768, NR <= 32
-  // (1.4-1.8x); float-float loses there from NR = 16 on (32.8 ms against
-  // 17.3 ms), and both lose at NH = 65536 beyond NR = 4.
+  // FP64 for NH <= 16384 at NR <= 32 (1.3-1.8x at NH = 16384; 2D Anderson
+  // L=64, NR=12: 3.6 ms against 6.9 ms) and at NH = 32768 with NR = 4;
+  // float-float for NH * NR <= 131072 (NH = 16384: 1.3x at NR = 4, 0.9x at
+  // NR = 16; NH = 32768: slower at every NR).
   // KPMGB_CLUSTER_AUTO=0 turns the automatic choice off.
   static const bool cluster_auto_on = [] {
     const char* e = std::getenv("KPMGB_CLUSTER_AUTO");
@@ -216,8 +216,9 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   const int variant = o ? o->kernel_variant : 0;
   const bool auto_cluster =
       variant == 0 && cluster_auto_on &&
-      (precision == KPMGB_PREC_FF ? NH <= 16384 && NH * NR <= 16384 * 32
-                                  : NH <= 32768 && NH * NR <= 32768 * 32);
+      (precision == KPMGB_PREC_FF
+           ? NH <= 16384 && NH * NR <= 131072
+           : (NH <= 16384 && NH * NR <= 524288) || (NH <= 32768 && NR <= 4));
   if (variant == 10 || auto_cluster) {
     const int rc = launch_kpm1d_cluster(op->csr, NH, (int)NR, NC, lr, precision, sl[0],
                                         lr ? ws.bra.ptr : nullptr, mu, mom_scale,
