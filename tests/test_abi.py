@@ -117,3 +117,35 @@ def test_derivative_host_checks_and_tangent_scale(built_lib):
     s = moment._tangent_scale(4, dH * 0.0, ((J, J * 64.0),))   # |dJ| / |J| = 64
     assert s == math.ldexp(1.0, -6)
     assert moment._tangent_scale(16, sp.csr_matrix((8, 8))) == 1.0
+
+
+def test_blocking_rule_agrees_with_oracle_everywhere():
+    """The host blocking rule (kpm_gb300.kpm_2d_blocking) and the oracle's
+    restatement of src/moment.jl:759-810 agree on random sizes, budgets and
+    explicit block sizes, including which inputs are rejected."""
+    import kpm_gb300 as kg
+    from oracle import kpm_oracle as ko
+    rng = np.random.default_rng(2024)
+    for _ in range(3000):
+        NH = int(rng.integers(1, 5000))
+        NR = int(rng.integers(1, 64))
+        NC = int(rng.integers(2, 600))
+        one = NH * NR * 16
+        budget = int(rng.integers(0, 60) * one + rng.integers(0, one))
+        arr = "auto" if rng.random() < 0.5 else int(rng.integers(0, 40))
+        rb = "auto" if rng.random() < 0.5 else int(rng.integers(1, 40))
+        try:
+            ref = ko.kpm_2d_blocking(NH, NR, NC, budget, arr_size=arr, right_block=rb)
+        except ValueError:
+            ref = None
+        try:
+            got = kg.kpm_2d_blocking(NH, NR, NC, workspace_bytes=budget, arr_size=arr,
+                                     right_block=rb)
+        except kg.KPMArgumentError:
+            got = None
+        if ref is None:
+            assert got is None, (NH, NR, NC, budget, arr, rb, got)
+        else:
+            assert got is not None, (NH, NR, NC, budget, arr, rb)
+            assert (got["arr_size"], got["right_block"], got["bytes"]) == ref, \
+                (NH, NR, NC, budget, arr, rb, got, ref)
