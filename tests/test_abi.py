@@ -149,3 +149,22 @@ def test_blocking_rule_agrees_with_oracle_everywhere():
             assert got is not None, (NH, NR, NC, budget, arr, rb)
             assert (got["arr_size"], got["right_block"], got["bytes"]) == ref, \
                 (NH, NR, NC, budget, arr, rb, got, ref)
+
+
+def test_dos_basis_and_jackson_match_oracle():
+    """The host-side DOS map used for gradient losses (frontend.dos_basis) is
+    the reconstruction of src/applications/dos.jl:76-161 as a matrix: Phi @ mu
+    equals the oracle's rho on the same grid (points outside |E - b| < a
+    give 0), and the Jackson factors match."""
+    import kpm_gb300 as kg
+    from oracle import kpm_oracle as ko
+    rng = np.random.default_rng(8)
+    for NC in (1, 2, 17, 128):
+        n = np.arange(NC)
+        assert np.allclose(kg.jackson_kernel(n, NC), ko.jackson_kernel(n, NC), rtol=0, atol=1e-15)
+        mu = rng.standard_normal(NC)
+        a, b = 1.7, -0.3
+        E = np.linspace(b - 1.2 * a, b + 1.2 * a, 301)
+        _, rho = ko.dos(mu, a, b=b, E_grid=E)
+        got = kg.dos_basis(NC, a, b, E) @ mu
+        assert np.abs(got - rho).max() <= 1e-12 * max(1.0, np.abs(rho).max())
