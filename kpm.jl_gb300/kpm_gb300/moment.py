@@ -107,6 +107,14 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
     average for ``psi_in_l``/``psi_in_r``, or the (NR, NC) matrix with
     ``avg_output=False``.  Without probes, random-phase probes are drawn from
     ``rng`` (a NumPy Generator; the reference draws from Xoshiro).
+
+    ``kernel`` picks the recurrence kernel (``include/kpmgb.h``,
+    ``kernel_variant``): ``"auto"`` (one thread-block-cluster launch per call
+    for small operators, else per-step launches of the padded-row kernel for
+    real operators with 33..64 columns or of the register-gather kernel),
+    ``"gather"``, ``"padded"``, ``"cluster"``, ``"single"``, ``"tune"``,
+    ``"tma"``, ``"anchored"``, ``"pipelined"``, ``"packed"``, ``"batched"``.
+    ``use_graph`` replays the per-step launches from a CUDA graph.
     """
     NH = H.shape[0] if NH is None else int(NH)
     NC, NR = int(NC), int(NR)
