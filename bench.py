@@ -53,8 +53,7 @@ def parse():
     p.add_argument("--cpu-steps", type=int, default=16,
                    help="recurrence steps in the bounded CPU-baseline sample")
     p.add_argument("--kernel", default="auto",
-                   choices=["auto", "gather", "tune", "anchored", "pipelined", "packed", "batched",
-                            "padded"],
+                   choices=["auto", "gather", "tune", "padded"],
                    help="float-float step kernel of the headline call")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-e2e", action="store_true")

@@ -79,29 +79,20 @@ typedef struct kpmgb_kpm1d_options {
                               options and device buffers repeat (host entry
                               points, and device entry points on a created
                               stream; ignored on the legacy default stream)  */
-  int32_t kernel_variant;  /* 0: automatic; 1: register-gather step kernel;
-                              2: TMA-fed step kernel (float-float, NR >= 32,
-                              at most 16 nonzeros per row); 3: float-float
-                              kernel with per-column maxima anchors instead
-                              of per-row chunk anchors; 4: autotune — time
-                              the register-gather shapes (and the TMA-fed
-                              kernel where it applies) once per (NR,
-                              precision, path) on this operator and reuse the
-                              fastest; 5: software-pipelined float-float
-                              kernel (cp.async neighbour staging, 17..64
-                              columns, at most 8 nonzeros per row); 6: the
-                              whole recurrence in one cooperative launch with
-                              a grid barrier per step (small operators,
-                              NR <= 256); 7: float-float on packed FP32x2
-                              pairs (real operators, 17..64 columns); 8:
-                              warp tiles with batched operator-index loads
-                              (17..64 columns, at most 8 nonzeros per row);
-                              9: fixed-width padded rows (float-float,
-                              5..64 columns, at most 16 nonzeros per row);
-                              10: one thread-block cluster per probe column
-                              with the recurrence resident in distributed
-                              shared memory (one launch per call; NH up to
-                              ~100k rows).
+  int32_t kernel_variant;  /* 0: automatic; 1: register-gather step kernel
+                              (CSR rows, one launch per step); 4: autotune --
+                              time the register-gather shapes and the
+                              padded-row kernel once per (NR, precision,
+                              path) on this operator and reuse the fastest;
+                              6: the whole recurrence in one cooperative
+                              launch with a grid barrier per step (small
+                              operators, NR <= 256); 9: fixed-width padded
+                              rows (float-float, 5..64 columns, at most 16
+                              nonzeros per row); 10: one thread-block cluster
+                              per probe column with the recurrence resident
+                              in distributed shared memory (one launch per
+                              call; NH up to ~100k rows).  Other values fail
+                              with KPMGB_ERR_ARGUMENT.
                               Automatic selection (0) is the cluster kernel
                               (10) for small operators (float-float:
                               NH <= 16384, NH * NR <= 131072; FP64:
@@ -290,9 +281,13 @@ int kpmgb_selftest_wait_expiry(kpmgb_operator H);
  * (2*NH*NR*16 bytes of recurrence vectors plus the moment partial sums must
  * fit; larger sizes fail with KPMGB_ERR_ARGUMENT), held by every GPU that
  * loads the library until exit.  The first call on a device resolves the
- * array's device address; make that first call before any stream capture.
- * Calls share the array, so calls that overlap on the GPU race.  Work runs on
- * `stream` and the call waits for it. */
+ * array's device address (and so does the first call after that device's
+ * context was replaced, e.g. by cudaDeviceReset); make that first call before
+ * any stream capture.  Buffers that are not device or managed memory, or not
+ * aligned (16 bytes for val, psi and mu_all; 4 for rowptr and col), fail with
+ * KPMGB_ERR_ARGUMENT before any work is queued.  Calls share the array, so
+ * calls that overlap on the GPU race.  Work runs on `stream` and the call
+ * waits for it. */
 int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int32_t* col,
                         const double* val, int64_t NC, int64_t NR,
                         const double* psi, double* mu_all, void* stream);

@@ -174,10 +174,8 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   const size_t slot = (size_t)NH * NR * 16;
   KPMGB_TRY(ws.slots.ensure(2 * slot));
   if (lr) KPMGB_TRY(ws.bra.ensure(slot));
-  // scales: 3*NR doubles, then 5*NR floats of column maxima (4-slot ring for
-  // the recurrence vectors + the bra), float-float path only
-  const size_t scale_bytes = (size_t)(3 * NR + 2) * sizeof(double);
-  KPMGB_TRY(ws.scales.ensure(scale_bytes + (size_t)5 * NR * sizeof(float)));
+  // scales: column factors of the ket and the bra, and their products
+  KPMGB_TRY(ws.scales.ensure((size_t)(3 * NR + 2) * sizeof(double)));
   KPMGB_TRY(ws.partials.ensure(step_partials_bytes(op->csr, NH, (int)NR, precision)));
   KPMGB_TRY(ensure_sync(op, s));
   char* slots = ws.slots.as<char>();
@@ -187,18 +185,9 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   KPMGB_TRY(launch_load_block(psi_r, sl[0], NH, (int)NR, precision, sc, false, s));
   if (lr) KPMGB_TRY(launch_load_block(psi_l, ws.bra.ptr, NH, (int)NR, precision, sc + NR, false, s));
   const double* mom_scale = nullptr;
-  float* mx = reinterpret_cast<float*>(ws.scales.as<char>() + scale_bytes);
-  auto ring = [&](int64_t k) { return mx + (k % 4) * NR; };
-  float* bmax = mx + 4 * NR;
-  const bool use_max = ff && o && o->kernel_variant == 3;
   if (ff) {
     KPMGB_TRY(launch_scale_product(sc, lr ? sc + NR : sc, sc + 2 * NR, (int)NR, s));
     mom_scale = sc + 2 * NR;
-  }
-  if (use_max) {
-    KPMGB_CUDA(cudaMemsetAsync(mx, 0, (size_t)5 * NR * sizeof(float), s));
-    KPMGB_TRY(launch_colmax(sl[0], NH, (int)NR, ring(0), s));
-    if (lr) KPMGB_TRY(launch_colmax(ws.bra.ptr, NH, (int)NR, bmax, s));
   }
   // kernel_variant 10: one thread-block cluster per probe column, the
   // recurrence resident in distributed shared memory.  Automatic selection
@@ -214,6 +203,9 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
     return !(e && std::atoi(e) == 0);
   }();
   const int variant = o ? o->kernel_variant : 0;
+  if (variant != 0 && variant != 1 && variant != 4 && variant != 6 && variant != 9 &&
+      variant != 10)
+    return fail(KPMGB_ERR_ARGUMENT, "unknown kernel_variant %d", variant);
   const bool auto_cluster =
       variant == 0 && cluster_auto_on &&
       (precision == KPMGB_PREC_FF
@@ -289,12 +281,6 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   a.dot = lr ? DOT_LR2 : DOT_DOUBLING;
   a.mom = MOM_STORE;
   a.i0 = 0;
-  if (use_max) {
-    a.xmax = ring(0);
-    a.bmax = lr ? bmax : nullptr;
-    a.ymax_out = ring(1);
-    a.ymax_clear = ring(2);
-  }
   KPMGB_TRY(launch_step(a, precision, s));
   int ip = 1, ipp = 0;
   a.alpha = 2.0;
@@ -311,12 +297,6 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       a.mom = MOM_DOUBLING;
       a.i0 = 2 * n - 2;
       a.growth_limit = check ? 2.25 : 0.0;
-      if (use_max) {
-        a.xmax = ring(n - 1);
-        a.zmax = ring(n - 2);
-        a.ymax_out = ring(n);
-        a.ymax_clear = ring(n + 1);
-      }
       KPMGB_TRY(launch_step(a, precision, s));
       std::swap(ip, ipp);
     }
@@ -329,12 +309,6 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       a.dot = DOT_LR1;
       a.mom = MOM_STORE;
       a.i0 = n;
-      if (use_max) {
-        a.xmax = ring(n - 1);
-        a.zmax = ring(n - 2);
-        a.ymax_out = ring(n);
-        a.ymax_clear = ring(n + 1);
-      }
       KPMGB_TRY(launch_step(a, precision, s));
       std::swap(ip, ipp);
     }

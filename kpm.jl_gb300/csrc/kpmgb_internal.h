@@ -162,17 +162,9 @@ struct StepArgs {
   unsigned* sync = nullptr;  // ticket counter + status word
   void* partials = nullptr;
   size_t partials_bytes = 0;  // 0: capacity not checked
-  int variant = 0;           // 0 auto, 1 register-gather kernel, 2 TMA-fed kernel,
-                             // 3 maxima-anchored kernel
+  int variant = 0;           // 0 auto, 1 register-gather kernel, 9 padded-row kernel
   int shape = 0;             // lanes-per-row * 10 + columns-per-lane of the
                              // register-gather kernel; 0 = automatic
-  // per-column maxima (float-float moment steps): when xmax is set the
-  // maxima-anchored kernel is used and writes the maxima of y
-  const float* xmax = nullptr;
-  const float* zmax = nullptr;
-  const float* bmax = nullptr;
-  float* ymax_out = nullptr;
-  float* ymax_clear = nullptr;
 };
 
 // precision: KPMGB_PREC_FP64 or KPMGB_PREC_FF.  Returns KPMGB_OK or an error.
@@ -209,10 +201,6 @@ size_t small_partials_bytes(int NR);
 // Row-major NH x NR FP64 blocks (K of them, consecutive) -> column-major.
 int launch_rowmajor_to_colmajor(const double2* in, double2* out, int64_t NH, int NR, int K,
                                 cudaStream_t s);
-
-// Per-column max |hi| of a row-major float-float block, atomically merged into
-// out[0..NR) (out must be zeroed first).
-int launch_colmax(const void* slot, int64_t NH, int NR, float* out, cudaStream_t s);
 
 // Moment-scale helpers for the float-float path.
 int launch_scale_product(const double* sa, const double* sb, double* out, int NR,

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <mutex>
 
 #include "kpmgb_internal.h"
@@ -30,25 +31,70 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_noalloc_mtx;
-void* g_noalloc_ptr[kMaxDevices] = {};
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;  // context the address was resolved in
+  void* ptr = nullptr;
+};
+ScratchAddr g_noalloc_addr[kMaxDevices];
 
-// Device address of the scratch array on the current device.  The first call
-// on each device resolves it with cudaGetSymbolAddress (the host-side name of
-// the array is only a stand-in, never a device address).
+// Id of the current context (0 when the driver cannot tell), looked up through
+// the runtime's driver entry point so that the library needs no link-time
+// dependency on the driver library.
+unsigned long long current_context_id() {
+  using CtxGetId = int (*)(void* ctx, unsigned long long* id);
+  static CtxGetId fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    cudaGetLastError();
+    return reinterpret_cast<CtxGetId>(f);
+  }();
+  unsigned long long id = 0;
+  if (fn && fn(nullptr, &id) != 0) id = 0;
+  return id;
+}
+
+// Device address of the scratch array on the current device.  The host-side
+// name of the array is only a stand-in, never a device address: the address
+// is resolved with cudaGetSymbolAddress on the first call on each device, and
+// again when that device's context has been replaced since (cudaDeviceReset).
 int noalloc_scratch(void** out) {
   int dev = 0;
   KPMGB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(KPMGB_ERR_CUDA, "device ordinal %d out of range", dev);
+  KPMGB_CUDA(cudaSetDevice(dev));  // makes the device's primary context current
+  const unsigned long long id = current_context_id();
   std::lock_guard<std::mutex> lk(g_noalloc_mtx);
-  if (!g_noalloc_ptr[dev]) {
+  ScratchAddr& a = g_noalloc_addr[dev];
+  if (!a.ptr || a.ctx_id != id) {
     void* p = nullptr;
     const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
       return fail(KPMGB_ERR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch failed: %s",
                   cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = p;
+    a.ptr = p;
+    a.ctx_id = id;
   }
-  *out = g_noalloc_ptr[dev];
+  *out = a.ptr;
+  return KPMGB_OK;
+}
+
+// A caller buffer must be device (or managed) memory and aligned for the
+// vector loads of the kernels.
+int check_device_buffer(const void* p, size_t align, const char* name) {
+  if (reinterpret_cast<uintptr_t>(p) % align != 0)
+    return fail(KPMGB_ERR_ARGUMENT, "%s is not %zu-byte aligned", name, align);
+  cudaPointerAttributes at{};
+  const cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(KPMGB_ERR_ARGUMENT, "%s is not a device address (%s)", name, cudaGetErrorString(e));
+  }
+  if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)
+    return fail(KPMGB_ERR_ARGUMENT, "%s must be device or managed memory", name);
   return KPMGB_OK;
 }
 
@@ -67,6 +113,11 @@ extern "C" int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int3
   if (NR < 1 || NR > (1 << 20)) return fail(KPMGB_ERR_ARGUMENT, "invalid NR=%lld", (long long)NR);
   if (NC < 2 || NC % 2 != 0) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be even.");
   if (!rowptr || !col || !val || !psi || !mu_all) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
+  KPMGB_TRY(check_device_buffer(rowptr, 4, "rowptr"));
+  KPMGB_TRY(check_device_buffer(col, 4, "col"));
+  KPMGB_TRY(check_device_buffer(val, 16, "val"));
+  KPMGB_TRY(check_device_buffer(psi, 16, "psi"));
+  KPMGB_TRY(check_device_buffer(mu_all, 16, "mu_all"));
   DeviceCSR H;
   H.n = NH;
   H.rowptr = const_cast<int*>(rowptr);
@@ -98,6 +149,7 @@ extern "C" int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int3
   a.mu = reinterpret_cast<double2*>(mu_all);
   a.sync = sync;
   a.partials = partials;
+  a.partials_bytes = part;  // the step kernels check their grid against it
   a.x = sl[0];
   a.y = sl[1];
   a.alpha = 1.0;
@@ -121,7 +173,13 @@ extern "C" int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int3
   unsigned status = 0;
   KPMGB_CUDA(cudaMemcpyAsync(&status, sync + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   KPMGB_CUDA(cudaStreamSynchronize(s));
+  if (status & STATUS_SCRATCH)
+    return fail(KPMGB_ERR_CUDA, "the no-alloc scratch is too small for the launch grid");
+  if (status & STATUS_TIMEOUT)
+    return fail(KPMGB_ERR_TIMEOUT, "a bounded wait inside a kernel expired");
   if (status & STATUS_NONFINITE)
     return fail(KPMGB_ERR_NUMERICAL, "non-finite moment produced by the recurrence");
+  if (status != 0)
+    return fail(KPMGB_ERR_CUDA, "unexpected kernel status 0x%x", status);
   return KPMGB_OK;
 }

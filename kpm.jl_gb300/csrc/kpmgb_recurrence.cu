@@ -29,7 +29,6 @@
 #include <unordered_map>
 
 #include "kpmgb_step.cuh"
-#include "kpmgb_step_tma.cuh"
 
 namespace kpmgb {
 namespace {
@@ -163,27 +162,6 @@ int launch_step_kernel(KernelFn fn, int G, cudaStream_t s, const KParams& p,
   return KPMGB_OK;
 }
 
-int pipe_grid(const PipeGeom& g, int64_t NH) {
-  static std::mutex m;
-  static std::unordered_map<const void*, int> cache;
-  int per_sm = 1;
-  {
-    std::lock_guard<std::mutex> lk(m);
-    auto it = cache.find((const void*)g.fn);
-    if (it != cache.end()) {
-      per_sm = it->second;
-    } else {
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.fn, g.threads, g.smem) !=
-          cudaSuccess)
-        per_sm = 1;
-      per_sm = std::max(per_sm, 1);
-      cache.emplace((const void*)g.fn, per_sm);
-    }
-  }
-  const int64_t blocks = (NH + g.rows_per_block - 1) / g.rows_per_block;
-  return (int)std::max<int64_t>(1, std::min<int64_t>(blocks, (int64_t)per_sm * num_sms()));
-}
-
 // Columns per step launch: kMaxCols, or fewer through KPMGB_COLS_PER_LAUNCH
 // (a tuning knob: narrower launches give each lane group shorter rows).
 int cols_per_launch() {
@@ -219,7 +197,6 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
   const int W = cols_per_launch();
   for (int c0 = 0; c0 < NR; c0 += W) {
     const int ncols = std::min(W, NR - c0);
-    const Shape s = pick_shape(ncols);
     for (const Shape& c : candidate_shapes(ncols))
       for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
         KernelFn fn = select_kernel(c, precision, dot, H.is_real != 0);
@@ -228,25 +205,6 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
       }
     if (precision == KPMGB_PREC_FF) {
       for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
-        KernelFn fn = select_kernel_ffg(s, dot, H.is_real != 0);
-        const int G = grid_for(fn, NH, s.lpr);
-        worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
-      }
-    }
-    // the TMA-fed kernel launches min(SMs, ceil(NH / consumer warps)) blocks
-    // with at least 4 consumer warps per block
-    if (precision == KPMGB_PREC_FF && ncols >= 32) {
-      const int64_t G = std::max<int64_t>(1, std::min<int64_t>(num_sms(), (NH + 3) / 4));
-      worst = std::max(worst, (size_t)G * 2 * ncols * sizeof(double2));
-    }
-    if (precision == KPMGB_PREC_FF) {
-      for (int dot : {DOT_DOUBLING, DOT_LR2, DOT_LR1}) {
-        const PipeGeom g = select_kernel_ffp(ncols, dot, H.is_real != 0, H.max_row_nnz);
-        if (g.fn) worst = std::max(worst, (size_t)pipe_grid(g, NH) * 2 * ncols * sizeof(double2));
-        if (KernelFn fx = select_kernel_ffx(ncols, dot, H.is_real != 0))
-          worst = std::max(worst, (size_t)grid_for(fx, NH, 32) * 2 * ncols * sizeof(double2));
-        if (KernelFn fb = select_kernel_ffb(ncols, dot, H.is_real != 0, H.max_row_nnz))
-          worst = std::max(worst, (size_t)grid_for(fb, NH, 32) * 2 * ncols * sizeof(double2));
         if (KernelFn fe = select_kernel_ffe(ncols, dot, H.is_real != 0))
           worst = std::max(worst, (size_t)grid_for(fe, NH, ffe_lanes(ncols)) * 2 * ncols *
                                       sizeof(double2));
@@ -292,13 +250,6 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     p.sync = a.sync;
     p.partials = static_cast<double2*>(a.partials);
     p.partials_cap = (int64_t)(a.partials_bytes / sizeof(double2));
-    p.xmax = a.xmax;
-    p.zmax = a.zmax;
-    p.bmax = a.bmax;
-    p.ymax_out = a.ymax_out;
-    p.ymax_clear = a.ymax_clear;
-    p.rmax = (float)(H.rmax * (1.0 + 1e-6));
-    p.anchor_slack = (float)((2.0 * H.max_row_nnz + 4.0) * 0x1p-22 + 0x1p-20);
     p.ell_col = H.ell_col;
     p.ell_val = H.ell_val;
     p.ell_w = H.ell_w;
@@ -322,60 +273,6 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
         continue;
       }
     }
-    if (precision == KPMGB_PREC_FF && a.xmax && a.dot != DOT_NONE && a.variant == 3) {
-      const Shape sh = pick_shape(p.ncols);
-      KernelFn fn = select_kernel_ffg(sh, a.dot, H.is_real != 0);
-      const int G = grid_for(fn, a.NH, sh.lpr);
-      KPMGB_TRY(launch_step_kernel(fn, G, s, p));
-      continue;
-    }
-    if (precision == KPMGB_PREC_FF && a.variant == 8) {
-      KernelFn fb = select_kernel_ffb(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz);
-      if (!fb)
-        return fail(KPMGB_ERR_ARGUMENT, "the batched-index kernel serves float-float steps with "
-                                        "17..64 columns and at most 8 nonzeros per row");
-      KPMGB_TRY(launch_step_kernel(fb, grid_for(fb, a.NH, 32), s, p));
-      continue;
-    }
-    if (precision == KPMGB_PREC_FF && a.variant == 7) {
-      KernelFn fx = select_kernel_ffx(p.ncols, a.dot, H.is_real != 0);
-      if (!fx)
-        return fail(KPMGB_ERR_ARGUMENT, "the packed float-float kernel serves real operators "
-                                        "with 17..64 columns");
-      KPMGB_TRY(launch_step_kernel(fx, grid_for(fx, a.NH, 32), s, p));
-      continue;
-    }
-    if (precision == KPMGB_PREC_FF && a.variant == 5) {
-      const PipeGeom g = select_kernel_ffp(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz);
-      if (!g.fn)
-        return fail(KPMGB_ERR_ARGUMENT, "the pipelined kernel serves float-float steps with "
-                                        "17..64 columns and at most 8 nonzeros per row");
-      KPMGB_TRY(launch_step_kernel(g.fn, pipe_grid(g, a.NH), s, p, g.threads, g.smem));
-      continue;
-    }
-    // The TMA-fed kernel serves float-float steps with at least one warp of
-    // columns and at most 16 nonzeros per row; variant 1 forces the
-    // register-gather kernel, variant 2 requires the TMA-fed one.
-    const bool tma_ok = precision == KPMGB_PREC_FF && p.ncols >= 32 &&
-                        tma_chmax(H.max_row_nnz) > 0;
-    if (a.variant == 2 && !tma_ok)
-      return fail(KPMGB_ERR_ARGUMENT, "the TMA-fed kernel needs float-float precision, NR >= 32 "
-                                      "and at most 16 nonzeros per row");
-    // Automatic selection keeps the register-gather kernel: measured on GB300
-    // it sustains ~1.8x the TMA-fed kernel's bandwidth on the 3D Anderson
-    // workload (the producer's dependent CSR loads limit the latter).
-    if (tma_ok && a.variant == 2) {
-      const TmaGeom g = select_kernel_ff_tma(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz);
-      if (!g.fn)
-        return fail(KPMGB_ERR_ARGUMENT,
-                    "the TMA-fed kernel's shared-memory stages do not fit for this NR and row length");
-      const int ncw = g.threads / 32 - 1;
-      const int G = (int)std::max<int64_t>(
-          1, std::min<int64_t>(num_sms(), (a.NH + ncw - 1) / ncw));
-      g.fn<<<G, g.threads, g.smem, s>>>(p);
-      KPMGB_LAUNCHED();
-      continue;
-    }
     const Shape sh = shape_for(a, p.ncols);
     KernelFn fn = select_kernel(sh, precision, a.dot, H.is_real != 0);
     const int G = grid_for(fn, a.NH, sh.lpr);
@@ -393,16 +290,6 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
   };
   std::vector<Cand> cands;
   for (const Shape& c : candidate_shapes(a0.NR)) cands.push_back({1, c.lpr * 10 + c.cpl});
-  if (precision == KPMGB_PREC_FF && a0.NR >= 32 && tma_chmax(a0.H->max_row_nnz) > 0)
-    cands.push_back({2, 0});
-  if (precision == KPMGB_PREC_FF &&
-      select_kernel_ffp(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz).fn)
-    cands.push_back({5, 0});
-  if (precision == KPMGB_PREC_FF && select_kernel_ffx(a0.NR, a0.dot, a0.H->is_real != 0))
-    cands.push_back({7, 0});
-  if (precision == KPMGB_PREC_FF &&
-      select_kernel_ffb(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz))
-    cands.push_back({8, 0});
   if (precision == KPMGB_PREC_FF && a0.H->ell_w > 0 &&
       select_kernel_ffe(a0.NR, a0.dot, a0.H->is_real != 0))
     cands.push_back({9, 0});
@@ -419,8 +306,7 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
     StepArgs a = a0;
     a.variant = c.variant;
     a.shape = c.shape;
-    a.xmax = nullptr;
-    if (launch_step(a, precision, s) != KPMGB_OK) {  // e.g. TMA stages that do not fit
+    if (launch_step(a, precision, s) != KPMGB_OK) {
       clear_error();
       continue;
     }
@@ -519,15 +405,6 @@ __global__ void k_uniform_scale(double* s, int n) {
   s[n] = m;
 }
 
-__global__ void k_colmax(const float4* __restrict__ v, int64_t n, int NR, float* out) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const float4 e = v[i];
-    const float m = fmaxf(fabsf(e.x), fabsf(e.z));
-    if (m > 0.f) atomicMax(reinterpret_cast<unsigned*>(out) + (i % NR), __float_as_uint(m));
-  }
-}
-
 __global__ void k_scale_product(const double* a, const double* b, double* out, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = a[i] * b[i];
@@ -559,14 +436,6 @@ int launch_load_block(const void* psi, void* slot, int64_t NH, int NR, int preci
   else
     k_transpose_in<false><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
                                                nullptr);
-  KPMGB_LAUNCHED();
-  return KPMGB_OK;
-}
-
-int launch_colmax(const void* slot, int64_t NH, int NR, float* out, cudaStream_t s) {
-  const int64_t n = NH * NR;
-  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4 * 1024);
-  k_colmax<<<std::max(blocks, 1), 256, 0, s>>>(static_cast<const float4*>(slot), n, NR, out);
   KPMGB_LAUNCHED();
   return KPMGB_OK;
 }

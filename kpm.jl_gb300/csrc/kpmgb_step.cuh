@@ -112,14 +112,6 @@ struct KParams {
   unsigned* sync;
   double2* partials;
   int64_t partials_cap;  // capacity in double2 elements (0: unchecked)
-  // maxima-anchored float-float kernel (k_step_ffg)
-  const float* xmax;     // per-column max |hi| of x, z and the bra
-  const float* zmax;
-  const float* bmax;
-  float* ymax_out;       // per-column max |hi| of y (atomicMax, pre-zeroed)
-  float* ymax_clear;     // maxima array zeroed by block 0 for the next step
-  float rmax;            // max over rows of sum |H_rk| (re + im)
-  float anchor_slack;    // relative slack of the H x anchor bound
   // fixed-width padded rows (k_step_ffe): NH x ell_w columns / values
   const int* ell_col;
   const void* ell_val;
@@ -733,29 +725,6 @@ KernelFn select_kernel_impl(Shape s, int dot, bool real) {
 
 KernelFn select_kernel_f64(Shape s, int dot, bool real);
 KernelFn select_kernel_ff(Shape s, int dot, bool real);
-KernelFn select_kernel_ffg(Shape s, int dot, bool real);
-
-struct TmaGeom;
-int tma_chmax(int max_row_nnz);
-
-// Software-pipelined float-float kernel (kpmgb_step_ffp.cu): 17..64 columns,
-// rows of at most 8 nonzeros; fn == nullptr when it does not serve the shape.
-struct PipeGeom {
-  KernelFn fn;
-  int threads;
-  size_t smem;
-  int rows_per_block;
-};
-PipeGeom select_kernel_ffp(int ncols, int dot, bool real, int max_row_nnz);
-
-// Packed-FP32x2 float-float kernel for real operators (kpmgb_step_ffx.cu):
-// 17..64 columns; nullptr when it does not serve the shape.
-KernelFn select_kernel_ffx(int ncols, int dot, bool real);
-
-// Float-float kernel with batched operator-index loads per warp tile
-// (kpmgb_step_ffb.cu): 17..64 columns, rows of at most 8 nonzeros.
-KernelFn select_kernel_ffb(int ncols, int dot, bool real, int max_row_nnz);
-
 // Float-float kernel over fixed-width padded rows (kpmgb_step_ffe.cu): 5..64
 // columns; nullptr otherwise.  ffe_lanes: lanes per row of its shape.
 KernelFn select_kernel_ffe(int ncols, int dot, bool real);

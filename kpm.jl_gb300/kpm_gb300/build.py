@@ -25,11 +25,6 @@ SOURCES = [
     "kpmgb_recurrence.cu",
     "kpmgb_step_f64.cu",
     "kpmgb_step_ff.cu",
-    "kpmgb_step_ff_tma.cu",
-    "kpmgb_step_ffg.cu",
-    "kpmgb_step_ffp.cu",
-    "kpmgb_step_ffx.cu",
-    "kpmgb_step_ffb.cu",
     "kpmgb_step_ffe.cu",
     "kpmgb_small.cu",
     "kpmgb_cluster.cu",

@@ -55,7 +55,7 @@ def _colmajor(psi, NH, NR, name):
     return np.asfortranarray(a, dtype=np.complex128)
 
 
-_VARIANT = {"auto": 0, "gather": 1, "tma": 2, "anchored": 3, "tune": 4, "pipelined": 5, "single": 6, "packed": 7, "batched": 8, "padded": 9, "cluster": 10}
+_VARIANT = {"auto": 0, "gather": 1, "tune": 4, "single": 6, "padded": 9, "cluster": 10}
 
 
 def _opts1d(precision, stability_check, kernel="auto", use_graph=False):
@@ -112,9 +112,10 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
     ``kernel_variant``): ``"auto"`` (one thread-block-cluster launch per call
     for small operators, else per-step launches of the padded-row kernel for
     real operators with 33..64 columns or of the register-gather kernel),
-    ``"gather"``, ``"padded"``, ``"cluster"``, ``"single"``, ``"tune"``,
-    ``"tma"``, ``"anchored"``, ``"pipelined"``, ``"packed"``, ``"batched"``.
-    ``use_graph`` replays the per-step launches from a CUDA graph.
+    ``"gather"``, ``"padded"``, ``"cluster"``, ``"single"``, ``"tune"``.
+    ``use_graph`` replays the per-step launches from a CUDA graph.  With
+    ``NR_parallel=False`` the columns run one call each, with the same
+    options.
     """
     NH = H.shape[0] if NH is None else int(NH)
     NC, NR = int(NC), int(NR)
@@ -151,10 +152,13 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
             row = np.zeros((1, NC), dtype=np.complex128)
             if lr:
                 kpm_1d_bang(op, NC, 1, NH, row, np.asarray(psi_in_l)[:, i:i + 1],
-                            np.asarray(psi_in_r)[:, i:i + 1], precision=precision)
+                            np.asarray(psi_in_r)[:, i:i + 1], precision=precision,
+                            stability_check=stability_check, kernel=kernel,
+                            use_graph=use_graph)
             else:
                 kpm_1d_bang(op, NC, 1, NH, row, np.asarray(psi_in)[:, i:i + 1],
-                            precision=precision)
+                            precision=precision, stability_check=stability_check,
+                            kernel=kernel, use_graph=use_graph)
             mu_all[i] = row[0]
     if avg_output:
         avg = mu_all.sum(axis=0) / NR

@@ -35,6 +35,9 @@ def test_noalloc_matches_kpm1d_twice(built_lib):
     stream = torch.cuda.Stream()
     for _ in range(2):
         mu_t = torch.full((NC, NR), float("nan"), dtype=torch.complex128, device=dev)
+        # the uploads and the NaN fill run on torch's current stream; the
+        # entry point works on `stream` (non-blocking), so order it after them
+        stream.wait_stream(torch.cuda.current_stream())
         rc = lib.kpmgb_kpm1d_noalloc(NH, C.c_void_p(rowptr.data_ptr()), C.c_void_p(col.data_ptr()),
                                      C.c_void_p(val.data_ptr()), NC, NR,
                                      C.c_void_p(psi_t.data_ptr()), C.c_void_p(mu_t.data_ptr()),
@@ -49,3 +52,15 @@ def test_noalloc_matches_kpm1d_twice(built_lib):
                                  C.c_void_p(mu_t.data_ptr()), C.c_void_p(stream.cuda_stream))
     assert rc == _native.ERR_ARGUMENT
     assert "static" in lib.kpmgb_last_error().decode()
+
+    # host memory and misaligned device pointers are rejected before any work
+    host_mu = np.zeros((NC, NR), dtype=np.complex128)
+    rc = lib.kpmgb_kpm1d_noalloc(NH, C.c_void_p(rowptr.data_ptr()), C.c_void_p(col.data_ptr()),
+                                 C.c_void_p(val.data_ptr()), NC, NR, C.c_void_p(psi_t.data_ptr()),
+                                 C.c_void_p(host_mu.ctypes.data), C.c_void_p(stream.cuda_stream))
+    assert rc == _native.ERR_ARGUMENT
+    rc = lib.kpmgb_kpm1d_noalloc(NH, C.c_void_p(rowptr.data_ptr()), C.c_void_p(col.data_ptr()),
+                                 C.c_void_p(val.data_ptr() + 8), NC, NR,
+                                 C.c_void_p(psi_t.data_ptr()), C.c_void_p(mu_t.data_ptr()),
+                                 C.c_void_p(stream.cuda_stream))
+    assert rc == _native.ERR_ARGUMENT and "aligned" in lib.kpmgb_last_error().decode()
