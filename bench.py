@@ -53,11 +53,13 @@ def parse():
     p.add_argument("--cpu-steps", type=int, default=16,
                    help="recurrence steps in the bounded CPU-baseline sample")
     p.add_argument("--kernel", default="auto",
-                   choices=["auto", "gather", "tune", "padded"],
+                   choices=["auto", "gather", "tune", "padded", "streaming"],
                    help="float-float step kernel of the headline call")
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-cond", action="store_true",
+                   help="skip the kpm_2d (tensor-core contraction) summary of the headline line")
     p.add_argument("--workload", default="dos",
                    choices=["dos", "dos-small", "cond", "ensemble", "grad", "action", "dsigma",
                             "published"],
@@ -213,6 +215,84 @@ def run_reference(args, rank, world):
                  "C/OpenMP restatement of its CPU algorithm (oracle/kpm_cpu.c)"),
     }
     print(json.dumps(line), flush=True)
+
+
+def measured_bf16():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["bf16_tflops"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 1900.0, "fallback"
+
+
+# FP64 operations of the plain recurrence per row x column x step for a real
+# operator: 2 FMAs per nonzero (re, im), the update alpha*acc + beta*z (2 MUL +
+# 2 FMA) and the doubling dots <x|x> (2 FMA) and <x|y> (4 FMA); an FMA counts 2.
+def fp64_flop_per_row_col(nnz_per_row, real=True):
+    per_nz = 4 if real else 8
+    return per_nz * nnz_per_row + 6 + 12
+
+
+def cond_summary(args):
+    """kpm_2d on the Haldane model 256x256 cells (NH=131072), t2 = 0.1 i,
+    NC=512, NR=16: the split tensor-core contraction against the FP64 one,
+    the contraction kernel's own device time (CUDA events around its launch on
+    the launching stream), and sigma_xy(Ef=0)."""
+    import torch
+    import kpm_gb300 as kg
+    from kpm_gb300 import _native, models, rescale
+    H, Jx, Jy, area = models.haldane(256, 256, t=1.0, t2=0.1)
+    h = rescale(H, center=True)
+    NH, NR, NC = H.shape[0], 16, 512
+    psi = kg.random_phase_vectors(np.random.default_rng(42), NH, NR)
+    ops = [kg.GB300Operator(M) for M in (h.H, Jx, Jy)]
+    s = torch.cuda.Stream()
+    psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    K = NH * NR
+    F = 8.0 * NC * NC * K               # complex-FP64-equivalent flop per call
+    F_bf16 = 15 * F                     # 15 digit-pair BF16 products per real product
+    out = {"workload": f"kpm_2d, Haldane 256x256x2 (NH={NH}), t2=0.1i, NC={NC}, NR={NR}; "
+                       "sigma_xy(Ef=0)"}
+    res = {}
+    for prec, contraction, steps in (("ff", "split", 3), ("fp64", "fp64", 1)):
+        mu_t = torch.zeros((NC, NC), dtype=torch.complex128, device="cuda")
+        call = lambda: kg.kpm_2d_device(ops[0], ops[1], ops[2], NC, psi_t, psi_t, mu_t,
+                                        precision=prec, contraction=contraction, stream=s)
+        call()
+        kg.sync(ops[0], s)
+        kname = "contract_split" if contraction == "split" else "contract_fp64"
+        _native.timing_read(kname)               # drop the warm-up call's events
+        _native.timing_enable(True)
+        try:
+            ms = _time_device(call, s, 0, steps, lambda: kg.sync(ops[0], s))
+        finally:
+            _native.timing_enable(False)
+        kms, klaunch = _native.timing_read(kname)
+        res[contraction] = mu_t.cpu().numpy().T.copy()
+        out[f"{prec}_recurrence_{contraction}_contraction_ms"] = ms
+        out[f"{contraction}_contraction_kernel_ms_per_call"] = kms / steps
+        out[f"{contraction}_contraction_launches_per_call"] = klaunch / steps
+    peak, kind = measured_bf16()
+    tc_ms = out["split_contraction_kernel_ms_per_call"]
+    achieved = F_bf16 / (tc_ms / 1e3) / 1e12
+    out["split_contraction_roofline"] = {
+        "bound": "tensor", "kernel": "k_contract_tc", "achieved": achieved, "peak": peak,
+        "unit": "TFLOP/s", "frac": achieved / peak,
+        "peak_source": f"{kind} (MEASURED_PEAKS.json bf16_tflops, burst)",
+        "bf16_flop_per_call": F_bf16,
+        "note": "BF16 work = 15 digit-pair products x 8*NC^2*NH*NR"}
+    out["fp64_contraction_kernel_tflops"] = F / (out["fp64_contraction_kernel_ms_per_call"] / 1e3) / 1e12
+    out["split_vs_fp64_rel_err"] = float(np.linalg.norm(res["split"] - res["fp64"])
+                                         / np.linalg.norm(res["fp64"]))
+    out["speedup_split_vs_fp64"] = (out["fp64_recurrence_fp64_contraction_ms"]
+                                    / out["ff_recurrence_split_contraction_ms"])
+    sig = kg.kubo_bastin_cond(res["split"], h.a, np.array([0.0]), b=h.b, NH=NH, area=area)
+    sig64 = kg.kubo_bastin_cond(res["fp64"], h.a, np.array([0.0]), b=h.b, NH=NH, area=area)
+    out["sigma_xy_at_Ef0_split"] = float(sig[0])
+    out["sigma_xy_at_Ef0_fp64"] = float(sig64[0])
+    return out
 
 
 # ------------------------------------------------------------ secondary workloads
@@ -641,12 +721,28 @@ def main():
         kg.sync(op, stream)
         m64 = mu64.cpu().numpy().T
         avg_c, avg_p = mu_chosen.mean(0).real, m64.mean(0).real
+        plain_ms = e0.elapsed_time(e1)
+        fp64_peak = kg.measure_fp64_peak()
+        fl = fp64_flop_per_row_col(nnz / NH, real=True) * NH * NR
+        plain_launch_s = (plain_ms / 1e3) / step_launches
+        plain_hbm = B_step / plain_launch_s / 1e9
         plain = {"ms_per_step": e0.elapsed_time(e1),
                  "value": NR * (NC // 2) / (e0.elapsed_time(e1) / 1e3),
                  "speedup_chosen_vs_plain": e0.elapsed_time(e1) / ms,
                  "moment_rel_err_normwise": float(np.linalg.norm(mu_chosen - m64)
                                                   / np.linalg.norm(m64)),
-                 "moment_rel_err_max": float(np.max(np.abs(avg_c - avg_p)) / np.max(np.abs(avg_p)))}
+                 "moment_rel_err_max": float(np.max(np.abs(avg_c - avg_p)) / np.max(np.abs(avg_p))),
+                 "roofline": {
+                     "bound": "fp64", "achieved": fl / plain_launch_s / 1e12,
+                     "peak": fp64_peak, "unit": "TFLOP/s",
+                     "frac": fl / plain_launch_s / 1e12 / fp64_peak,
+                     "peak_source": "measured in this run (kpmgb_measure_fp64_peak: independent "
+                                    "FP64 FMA chains on every SM)",
+                     "flop_per_launch": fl,
+                     "flop_model": "per row x column x step: 4 per nonzero (real H) + 6 "
+                                   "(update) + 12 (doubling dots)",
+                     "hbm": {"achieved": plain_hbm, "peak": peak, "unit": "GB/s",
+                             "frac": plain_hbm / peak}}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -656,6 +752,10 @@ def main():
         cpu["check_rel_err_first_moments"] = float(
             np.linalg.norm(mu_cpu[:, :k] - mu_chosen[:, :k]) / np.linalg.norm(mu_cpu[:, :k]))
         cpu.pop("seconds", None)
+
+    cond = None
+    if rank == 0 and world == 1 and not args.no_cond:
+        cond = cond_summary(args)
 
     if rank == 0:
         line = {
@@ -672,6 +772,7 @@ def main():
             "clocks": clk.summary(),
             "plain_fp64": plain,
             "cpu_baseline": cpu,
+            "kpm2d_tensor_core": cond,
             "version": kg.version(),
         }
         print(json.dumps(line), flush=True)

@@ -91,17 +91,19 @@ typedef struct kpmgb_kpm1d_options {
                               nonzeros per row); 10: one thread-block cluster
                               per probe column with the recurrence resident
                               in distributed shared memory (one launch per
-                              call; NH up to ~100k rows).  Other values fail
-                              with KPMGB_ERR_ARGUMENT.
+                              call; NH up to ~100k rows); 11: row-streaming
+                              padded-row kernel (float-float, real operators,
+                              33..64 columns, rows of 5..8 nonzeros).  Other
+                              values fail with KPMGB_ERR_ARGUMENT.
                               Automatic selection (0) is the cluster kernel
                               (10) for small operators (float-float:
                               NH <= 16384, NH * NR <= 131072; FP64:
                               NH <= 16384, NH * NR <= 524288, or NH <= 32768
-                              with NR <= 4),
-                              else per-step launches of the padded-row kernel
-                              for real operators with 33..64 columns, else
-                              of the register-gather kernel with the default
-                              shape.                                          */
+                              with NR <= 4), else per-step launches of the
+                              row-streaming kernel (11) where it applies,
+                              else of the padded-row kernel for real
+                              operators with 33..64 columns, else of the
+                              register-gather kernel with the default shape. */
 } kpmgb_kpm1d_options;
 
 typedef struct kpmgb_kpm2d_options {
@@ -237,12 +239,51 @@ int kpmgb_kubo_bastin(const double* mu2d, int64_t ld, int64_t NC, double a,
                       double area, double beta, const double* damping,
                       int64_t quad_N, double edge_cutoff, double* sigma);
 
+/* The Kubo-Bastin reconstruction at one Fermi energy as a linear functional
+ * of the moments: W (NC x NC column-major complex, written) with
+ * sigma(Ef) = Re sum_{n,m} W[n,m] mu[n,m] for the sigma of kpmgb_kubo_bastin
+ * with the same arguments (src/applications/conductivity.jl:101-157).  W is
+ * d sigma / d mu, the weights that carry a loss on sigma into
+ * kpmgb_kpm2d_grad (no reference counterpart).  Blocking call. */
+int kpmgb_kubo_bastin_weights(int64_t NC, double a, double b, double Ef,
+                              int64_t NH, double area, double beta,
+                              const double* damping, int64_t quad_N,
+                              double edge_cutoff, double* W);
+
+/* Gradient of F = Re sum_{n,m} G[n,m] mu[n,m] with respect to every stored
+ * entry of H, Ja and Jb, where mu are the moments of kpmgb_kpm2d
+ * (src/moment.jl:887-1088) with moment_parity applied (mn_sym not covered).
+ * JbH: an operator holding Jb^dagger (created from the conjugate transpose).
+ * G: host NC x NC column-major complex.  grad_H / grad_Ja / grad_Jb: host
+ * arrays of each operator's nnz complex values in the order of the CSC arrays
+ * given to kpmgb_operator_create, entry k holding dF/dRe(X_k) + i dF/dIm(X_k).
+ * The adjoint Chebyshev recurrences of both chains run backward over the
+ * resident forward vectors (5 NC + 5 blocks of NH x min(NR, 32) complex
+ * values; probe columns in batches of 32), with SDDMMs onto the three
+ * sparsity patterns.  H must be Hermitian.  FP64.  No reference counterpart
+ * (the reference differentiates through ForwardDiff duals).  Blocking call. */
+int kpmgb_kpm2d_grad(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
+                     kpmgb_operator JbH, int64_t NC, int64_t NR, int64_t NH,
+                     const double* psi_l, const double* psi_r, const double* G,
+                     int32_t moment_parity, double* grad_H, double* grad_Ja,
+                     double* grad_Jb);
+
 /* DOS reconstruction rho(E_e) = sum_n h_n g_n mu_n T_n(x_e) / (a pi
  * sqrt(1 - x_e^2)), x_e = (E_e - b)/a, zero outside |E_e - b| < a
  * (src/applications/dos.jl:76-161 with dE_order = 0).  mu: NC real moments;
  * damping: NC kernel factors (NULL = Jackson).  Blocking call. */
 int kpmgb_dos(const double* mu, int64_t NC, double a, double b,
               const double* damping, const double* E, int64_t nE, double* rho);
+
+/* The dE_order-th energy derivative of that DOS reconstruction,
+ * d^k rho / dE^k at every E_e (src/applications/dos.jl:128-139, which nests
+ * ForwardDiff derivatives of the reconstruction): exact derivatives carried
+ * by truncated Taylor series through x = (E - b)/a, the Chebyshev recurrence
+ * and 1/(a pi sqrt(1 - x^2)).  dE_order 0..4 (0 is kpmgb_dos); zero outside
+ * |E_e - b| < a.  Blocking call. */
+int kpmgb_dos_derivative(const double* mu, int64_t NC, double a, double b,
+                         const double* damping, const double* E, int64_t nE,
+                         int32_t dE_order, double* rho);
 
 /* Gradient of L = sum_m g[m] mu_m with respect to every stored entry of a
  * Hermitian H, where mu are the probe-averaged doubling kpm_1d moments of
@@ -291,6 +332,21 @@ int kpmgb_selftest_wait_expiry(kpmgb_operator H);
 int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int32_t* col,
                         const double* val, int64_t NC, int64_t NR,
                         const double* psi, double* mu_all, void* stream);
+
+/* Instrumentation (no reference counterpart).  With timing enabled, every
+ * launch of the kernels below is bracketed by CUDA events on its launching
+ * stream; kpmgb_timing_read waits for the pairs recorded since the last read
+ * of that kernel and returns their summed device time and count.  Off by
+ * default (nothing is recorded). */
+#define KPMGB_TIMED_CONTRACT_SPLIT 0 /* tcgen05 split contraction kernel    */
+#define KPMGB_TIMED_CONTRACT_FP64 1  /* FP64 SIMT contraction kernel        */
+int kpmgb_timing_enable(int32_t on);
+int kpmgb_timing_read(int32_t kernel, double* total_ms, int64_t* launches);
+
+/* Measured FP64 FMA rate of the current device in TFLOP/s (2 flops per FMA),
+ * from a microkernel of independent FMA chains on every SM: the arithmetic
+ * roof of the FP64 recurrence (no reference counterpart). */
+int kpmgb_measure_fp64_peak(double* tflops);
 
 /* Wait for the work enqueued on an operator and report any deferred failure
  * flagged by the kernels (non-finite moments, stability guard). */

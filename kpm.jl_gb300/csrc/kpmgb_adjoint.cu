@@ -41,7 +41,9 @@ struct AdjParams {
   const double2* vk;      // v_k   (SDDMM partner of lambda_k+1; also in w_k)
   const double2* vkm1;    // v_k-1 (w_k), may be null
   const double2* vkp1;    // v_k+1 (w_k), may be null
-  double c_k, c_p, c_m;   // w_k = c_k v_k + c_p v_k+1 + c_m v_k-1
+  double c_k, c_p, c_m;   // w_k = c_k v_k + c_p v_k+1 + c_m v_k-1 (+ aseed)
+  const double2* aseed;   // explicit seed vector added to w_k, may be null
+  double spmm_coef;       // lambda_k = w_k + spmm_coef H lambda_k+1 - lambda_k+2
   double sddmm_coef;      // factor on conj(lambda_k+1[i]) v_k[j]; 0 = skip
   double2* grad;          // per stored entry (CSR order), accumulated
 };
@@ -88,6 +90,10 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint_step(AdjParams p) {
     }
     if (act && p.lam_out) {
       double2 w = make_double2(p.c_k * p.vk[own].x, p.c_k * p.vk[own].y);
+      if (p.aseed) {
+        w.x += p.aseed[own].x;
+        w.y += p.aseed[own].y;
+      }
       if (p.vkp1) {
         w.x = fma(p.c_p, p.vkp1[own].x, w.x);
         w.y = fma(p.c_p, p.vkp1[own].y, w.y);
@@ -96,7 +102,7 @@ __global__ void __launch_bounds__(kAdjThreads) k_adjoint_step(AdjParams p) {
         w.x = fma(p.c_m, p.vkm1[own].x, w.x);
         w.y = fma(p.c_m, p.vkm1[own].y, w.y);
       }
-      double2 lo = make_double2(fma(2.0, acc.x, w.x), fma(2.0, acc.y, w.y));
+      double2 lo = make_double2(fma(p.spmm_coef, acc.x, w.x), fma(p.spmm_coef, acc.y, w.y));
       if (p.lam2) {
         lo.x -= p.lam2[own].x;
         lo.y -= p.lam2[own].y;
@@ -226,6 +232,7 @@ int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, in
     p.NH = NH;
     p.NR = NR;
     p.grad = d_grad_csr;
+    p.spmm_coef = 2.0;
     return p;
   };
   // ---- backward: segment sg handles lambda_k for k in [sg*C + 1, min(sg*C + C, N)]
@@ -269,6 +276,249 @@ int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, in
   const int blocks = (int)std::min<int64_t>((H.nnz + 255) / 256, 4096);
   if (!last) return KPMGB_OK;
   k_scatter_grad<<<std::max(blocks, 1), 256, 0, s>>>(d_grad_csr, d_perm, H.nnz, d_grad_csc);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+// ----------------------------------------------------------------------------
+// Adjoint of kpm_2d (src/moment.jl:987-1088) for F = Re sum_{n,m} G[n,m] mu[n,m],
+//   mu[n,m] = (1/NR) sum_p <L_m^p | Jb S_n^p>,  L_m = T_m(H) psi_l,
+//   S_n = T_n(H) Ja psi_r
+// (G here already carries the parity mask and the 1/NR).  With
+//   Lambda_n = sum_m conj(G[n,m]) L_m   and   B_m = sum_n G[n,m] Jb S_n,
+// dF = Re sum_m <B_m|dL_m> + Re sum_n <Jb^dag Lambda_n|dS_n>
+//      + Re sum_n <Lambda_n| dJb S_n>.
+// Each chain's adjoint recurrence (seeds B_m, resp. Jb^dag Lambda_n) gives the
+// SDDMM terms onto H's pattern, and for the right chain the adjoint u_0 of its
+// seed Ja psi_r, whence the Ja gradient conj(u_0[i]) psi_r[j]; the Jb gradient
+// is sum_n conj(Lambda_n[i]) S_n[j].  Every forward vector of a batch of probe
+// columns stays resident.
+namespace {
+
+constexpr int kGT = 64;   // rows / columns of a GEMM output tile
+constexpr int kGK = 8;    // inner chunk
+
+// C[k + K m] = sum_n A[k + K n] B[n + NC m]  (complex, column-major, K x NC x NC)
+__global__ void __launch_bounds__(256) k_zgemm_tall(const double2* __restrict__ A,
+                                                    const double2* __restrict__ B, int64_t K,
+                                                    int NC, double2* __restrict__ C) {
+  __shared__ double2 sA[kGK][kGT];
+  __shared__ double2 sB[kGK][kGT];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int64_t k0 = (int64_t)blockIdx.x * kGT;
+  const int m0 = blockIdx.y * kGT;
+  double2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0.0, 0.0);
+  for (int n0 = 0; n0 < NC; n0 += kGK) {
+    for (int e = tid; e < kGK * kGT; e += 256) {
+      const int kk = e % kGT, nn = e / kGT;      // consecutive threads walk k
+      const int64_t k = k0 + kk;
+      const int n = n0 + nn;
+      sA[nn][kk] = (k < K && n < NC) ? A[(size_t)n * K + k] : make_double2(0.0, 0.0);
+      const int nb = e % kGK, mm = e / kGK;      // consecutive threads walk n
+      const int n2 = n0 + nb, m = m0 + mm;
+      sB[nb][mm] = (n2 < NC && m < NC) ? B[(size_t)m * NC + n2] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int nn = 0; nn < kGK; ++nn) {
+      double2 a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = sA[nn][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = sB[nn][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
+          acc[i][j].x = fma(-a[i].y, b[j].y, acc[i][j].x);
+          acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
+          acc[i][j].y = fma(a[i].y, b[j].x, acc[i][j].y);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int64_t k = k0 + tx + 16 * i;
+      const int m = m0 + ty + 16 * j;
+      if (k < K && m < NC) C[(size_t)m * K + k] = acc[i][j];
+    }
+}
+
+int launch_zgemm_tall(const double2* A, const double2* B, int64_t K, int NC, double2* C,
+                      cudaStream_t s) {
+  dim3 grid((unsigned)((K + kGT - 1) / kGT), (unsigned)((NC + kGT - 1) / kGT));
+  k_zgemm_tall<<<grid, 256, 0, s>>>(A, B, K, NC, C);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+// G[q] += sum_n sum_p conj(X_n[i,p]) Y_n[j,p] for every stored entry q = (i, j)
+// of an operator's CSR pattern; X_n, Y_n row-major NH x NR blocks at stride blk.
+template <int LPR>
+__global__ void __launch_bounds__(kAdjThreads) k_sddmm_sum(const int* rowptr, const int* col,
+                                                           int64_t NH, int NR, int NV,
+                                                           const double2* X, const double2* Y,
+                                                           int64_t blk, double2* grad) {
+  constexpr int GROUPS = kAdjThreads / LPR;
+  const int g = threadIdx.x / LPR, lg = threadIdx.x % LPR;
+  const unsigned mask = LPR == 32 ? 0xffffffffu
+                                  : (((1u << LPR) - 1u) << ((threadIdx.x & 31) / LPR * LPR));
+  for (int64_t r = (int64_t)blockIdx.x * GROUPS + g; r < NH; r += (int64_t)gridDim.x * GROUPS) {
+    const bool act = lg < NR;
+    const int k0 = rowptr[r], k1 = rowptr[r + 1];
+    for (int k = k0; k < k1; ++k) {
+      const int64_t j = col[k];
+      double sr = 0.0, si = 0.0;
+      if (act) {
+        for (int n = 0; n < NV; ++n) {
+          const double2 x = X[(size_t)n * blk + r * NR + lg];
+          const double2 y = Y[(size_t)n * blk + j * NR + lg];
+          sr = fma(x.x, y.x, fma(x.y, y.y, sr));
+          si = fma(x.x, y.y, fma(-x.y, y.x, si));
+        }
+      }
+#pragma unroll
+      for (int off = LPR / 2; off > 0; off >>= 1) {
+        sr += __shfl_xor_sync(mask, sr, off, LPR);
+        si += __shfl_xor_sync(mask, si, off, LPR);
+      }
+      if (lg == 0) {
+        grad[k].x += sr;
+        grad[k].y += si;
+      }
+    }
+  }
+}
+
+int launch_sddmm_sum(const DeviceCSR& J, int64_t NH, int NR, int NV, const double2* X,
+                     const double2* Y, int64_t blk, double2* grad, cudaStream_t s) {
+  int lpr = 32;
+  for (int c : {1, 2, 4, 8, 16, 32})
+    if (NR <= c) { lpr = c; break; }
+  const int64_t groups = kAdjThreads / lpr;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((NH + groups - 1) / groups, 8192));
+  switch (lpr) {
+    case 1: k_sddmm_sum<1><<<grid, kAdjThreads, 0, s>>>(J.rowptr, J.col, NH, NR, NV, X, Y, blk, grad); break;
+    case 2: k_sddmm_sum<2><<<grid, kAdjThreads, 0, s>>>(J.rowptr, J.col, NH, NR, NV, X, Y, blk, grad); break;
+    case 4: k_sddmm_sum<4><<<grid, kAdjThreads, 0, s>>>(J.rowptr, J.col, NH, NR, NV, X, Y, blk, grad); break;
+    case 8: k_sddmm_sum<8><<<grid, kAdjThreads, 0, s>>>(J.rowptr, J.col, NH, NR, NV, X, Y, blk, grad); break;
+    case 16: k_sddmm_sum<16><<<grid, kAdjThreads, 0, s>>>(J.rowptr, J.col, NH, NR, NV, X, Y, blk, grad); break;
+    default: k_sddmm_sum<32><<<grid, kAdjThreads, 0, s>>>(J.rowptr, J.col, NH, NR, NV, X, Y, blk, grad); break;
+  }
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
+AdjParams adj_params(const DeviceCSR& H, int64_t NH, int NR, double2* grad) {
+  AdjParams p{};
+  p.rowptr = H.rowptr;
+  p.col = H.col;
+  p.val = H.val;
+  p.NH = NH;
+  p.NR = NR;
+  p.grad = grad;
+  p.spmm_coef = 2.0;
+  return p;
+}
+
+// Backward pass of one Chebyshev chain v_0 .. v_{N-1} (stored at v(k)) with
+// seeds w(k): SDDMM terms into gH, and the seed adjoint
+// u_0 = w_0 + H lambda_1 - lambda_2 written to u0.
+template <typename VF, typename WF, typename LF>
+int chain_adjoint(const DeviceCSR& H, int64_t NH, int NR, int64_t N, VF v, WF w, LF lam,
+                  double2* gH, double2* u0, cudaStream_t s) {
+  for (int64_t k = N - 1; k >= 1; --k) {
+    AdjParams p = adj_params(H, NH, NR, gH);
+    p.lam1 = k + 1 <= N - 1 ? lam(k + 1) : nullptr;
+    p.lam2 = k + 2 <= N - 1 ? lam(k + 2) : nullptr;
+    p.lam_out = lam(k);
+    p.vk = v(k);
+    p.aseed = w(k);
+    p.sddmm_coef = k + 1 <= N - 1 ? 2.0 : 0.0;  // 2 conj(lambda_{k+1}[i]) v_k[j]
+    KPMGB_TRY(launch_adj(p, s));
+  }
+  // closing terms: conj(lambda_1[i]) v_0[j] and u_0
+  AdjParams p = adj_params(H, NH, NR, gH);
+  p.lam1 = N >= 2 ? lam(1) : nullptr;
+  p.lam2 = N >= 3 ? lam(2) : nullptr;
+  p.lam_out = u0;
+  p.vk = v(0);
+  p.aseed = w(0);
+  p.spmm_coef = 1.0;
+  p.sddmm_coef = N >= 2 ? 1.0 : 0.0;
+  return launch_adj(p, s);
+}
+
+}  // namespace
+
+size_t kpm2d_grad_work_bytes(int64_t NH, int NR, int64_t NC) {
+  return (size_t)(5 * NC + 5) * (size_t)NH * NR * sizeof(double2);
+}
+
+// One batch of NR <= 32 probe columns (row-major FP64 psil, psir).  Gp, GpH:
+// device NC x NC column-major weights (mask and 1/NR applied) and their
+// conjugate transpose.  Gradients accumulate in CSR order.
+int run_kpm2d_grad(const DeviceCSR& H, const DeviceCSR& Ja, const DeviceCSR& Jb,
+                   const DeviceCSR& JbH, int64_t NC, int NR, int64_t NH, const double2* psil,
+                   const double2* psir, const double2* Gp, const double2* GpH, double2* gH,
+                   double2* gJa, double2* gJb, DevBuf& work, cudaStream_t s) {
+  const int64_t K = NH * NR;
+  const size_t blk = (size_t)K * sizeof(double2);
+  KPMGB_TRY(work.ensure(kpm2d_grad_work_bytes(NH, NR, NC)));
+  double2* base = work.as<double2>();
+  auto L = [&](int64_t i) { return base + (size_t)i * K; };
+  auto S = [&](int64_t i) { return base + (size_t)(NC + i) * K; };
+  auto T = [&](int64_t i) { return base + (size_t)(2 * NC + i) * K; };
+  auto AL = [&](int64_t i) { return base + (size_t)(3 * NC + i) * K; };
+  auto LAM = [&](int64_t i) { return base + (size_t)(4 * NC + i) * K; };
+  auto ring = [&](int64_t k) { return base + (size_t)(5 * NC + (k % 3)) * K; };
+  double2* u0 = base + (size_t)(5 * NC + 3) * K;
+  double2* junk = base + (size_t)(5 * NC + 4) * K;
+  // forward chains
+  KPMGB_CUDA(cudaMemcpyAsync(L(0), psil, blk, cudaMemcpyDeviceToDevice, s));
+  KPMGB_TRY(adjoint_forward_step(Ja, NH, NR, psir, nullptr, S(0), 1.0, 0.0, s));
+  if (NC >= 2) {
+    KPMGB_TRY(adjoint_forward_step(H, NH, NR, L(0), nullptr, L(1), 1.0, 0.0, s));
+    KPMGB_TRY(adjoint_forward_step(H, NH, NR, S(0), nullptr, S(1), 1.0, 0.0, s));
+  }
+  for (int64_t k = 2; k < NC; ++k) {
+    KPMGB_TRY(adjoint_forward_step(H, NH, NR, L(k - 1), L(k - 2), L(k), 2.0, -1.0, s));
+    KPMGB_TRY(adjoint_forward_step(H, NH, NR, S(k - 1), S(k - 2), S(k), 2.0, -1.0, s));
+  }
+  for (int64_t n = 0; n < NC; ++n)
+    KPMGB_TRY(adjoint_forward_step(Jb, NH, NR, S(n), nullptr, T(n), 1.0, 0.0, s));
+  // seeds: B = (Jb S) Gp (left chain), Lambda = L Gp^H, Jb^dag Lambda (right chain)
+  KPMGB_TRY(launch_zgemm_tall(T(0), Gp, K, (int)NC, AL(0), s));
+  KPMGB_TRY(launch_zgemm_tall(L(0), GpH, K, (int)NC, LAM(0), s));
+  for (int64_t n = 0; n < NC; ++n)
+    KPMGB_TRY(adjoint_forward_step(JbH, NH, NR, LAM(n), nullptr, T(n), 1.0, 0.0, s));
+  // backward passes
+  KPMGB_TRY(chain_adjoint(H, NH, NR, NC, L, AL, ring, gH, junk, s));
+  KPMGB_TRY(chain_adjoint(H, NH, NR, NC, S, T, ring, gH, u0, s));
+  // Ja: conj(u_0[i]) psi_r[j] on Ja's pattern (the SpMM part is not stored)
+  {
+    AdjParams p = adj_params(Ja, NH, NR, gJa);
+    p.lam1 = u0;
+    p.vk = psir;
+    p.sddmm_coef = 1.0;
+    KPMGB_TRY(launch_adj(p, s));
+  }
+  // Jb: sum_n conj(Lambda_n[i]) S_n[j] on Jb's pattern
+  return launch_sddmm_sum(Jb, NH, NR, (int)NC, LAM(0), S(0), K, gJb, s);
+}
+
+int scatter_grad(const double2* gcsr, const int* perm, int64_t nnz, double2* gcsc,
+                 cudaStream_t s) {
+  const int blocks = (int)std::min<int64_t>((nnz + 255) / 256, 4096);
+  k_scatter_grad<<<std::max(blocks, 1), 256, 0, s>>>(gcsr, perm, nnz, gcsc);
   KPMGB_LAUNCHED();
   return KPMGB_OK;
 }

@@ -204,7 +204,7 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   }();
   const int variant = o ? o->kernel_variant : 0;
   if (variant != 0 && variant != 1 && variant != 4 && variant != 6 && variant != 9 &&
-      variant != 10)
+      variant != 10 && variant != 11)
     return fail(KPMGB_ERR_ARGUMENT, "unknown kernel_variant %d", variant);
   const bool auto_cluster =
       variant == 0 && cluster_auto_on &&
@@ -233,7 +233,20 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   int chosen_variant = o ? o->kernel_variant : 0, chosen_shape = 0;
   if (chosen_variant == 4) {
     const std::string tkey = std::to_string(NR) + "/" + std::to_string(precision) + (lr ? "/lr" : "/d");
+    // persistent key: the device and the operator's shape
+    const std::string pkey = "step|" + device_tag() + "|NH=" + std::to_string(NH) + "|nnz=" +
+                             std::to_string(op->csr.nnz) + "|maxrow=" +
+                             std::to_string(op->csr.max_row_nnz) + "|real=" +
+                             std::to_string(op->csr.is_real) + "|NR=" + std::to_string(NR) +
+                             "|prec=" + std::to_string(precision) + (lr ? "|lr" : "|doubling");
     auto it = op->tuned.find(tkey);
+    if (it == op->tuned.end()) {
+      std::string cached;
+      int v = 0, sh = 0;
+      if (tune_cache_get(pkey, &cached) && std::sscanf(cached.c_str(), "%d,%d", &v, &sh) == 2 &&
+          (v == 1 || v == 9 || v == 11))
+        it = op->tuned.emplace(tkey, std::make_pair(v, sh)).first;
+    }
     if (it == op->tuned.end()) {
       StepArgs t;
       t.H = &op->csr;
@@ -252,6 +265,7 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       int v = 1, sh = 0;
       KPMGB_TRY(tune_step(t, precision, s, &v, &sh));
       it = op->tuned.emplace(tkey, std::make_pair(v, sh)).first;
+      tune_cache_put(pkey, std::to_string(v) + "," + std::to_string(sh));
     }
     chosen_variant = it->second.first;
     chosen_shape = it->second.second;
@@ -786,7 +800,8 @@ int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t 
 namespace kpmgb {
 int launch_ensemble(const DeviceCSR& H, const int64_t* d_seg, const int* d_order, int nseg, int NR,
                     int64_t NC, void* slot0, void* slot1, double2* mu, const double* scale,
-                    unsigned* next, unsigned* status, int precision, cudaStream_t s);
+                    unsigned* next, unsigned* status, int precision, cudaStream_t s,
+                    const EnsembleShape& shape);
 }
 
 extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_t* seg,
@@ -840,20 +855,87 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
   char* slots = ws.slots.as<char>();
   double* sc = ws.scales.as<double>();
   const bool ff = precision == KPMGB_PREC_FF;
-  for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
-    const int nb = (int)std::min<int64_t>(kBatch, NR - c0);
+  const int variant = opts ? opts->kernel_variant : 0;
+  if (variant != 0 && variant != 4)
+    return fail(KPMGB_ERR_ARGUMENT, "the ensemble kernel takes kernel_variant 0 or 4 (autotune)");
+  // load column batch c0 into slot 0 (probes scaled for the float-float path)
+  auto load = [&](int64_t c0, int nb, const double** scale) -> int {
     const size_t bb = (size_t)NH * nb * 16;
     KPMGB_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned), s));
     KPMGB_CUDA(cudaMemcpyAsync(ws.psi_in.ptr, psi + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
     KPMGB_TRY(launch_load_block(ws.psi_in.ptr, slots, NH, nb, precision, sc, false, s));
-    const double* scale = nullptr;
+    *scale = nullptr;
     if (ff) {
       KPMGB_TRY(launch_scale_product(sc, sc, sc + 2 * nb, nb, s));
-      scale = sc + 2 * nb;
+      *scale = sc + 2 * nb;
     }
+    return KPMGB_OK;
+  };
+  // Launch shape: the default (1024 threads per CTA, CSR rows), or with
+  // kernel_variant 4 the fastest of the candidate shapes timed on a short
+  // recurrence of the first column batch, kept per (device, ensemble shape)
+  // in the persistent autotuning cache.
+  EnsembleShape shape;
+  if (variant == 4) {
+    const int nb0 = (int)nb_max;
+    const std::string key = "ensemble|" + device_tag() + "|nseg=" + std::to_string(nseg) +
+                            "|NH=" + std::to_string(NH) + "|nnz=" + std::to_string(op->csr.nnz) +
+                            "|maxrow=" + std::to_string(op->csr.max_row_nnz) + "|real=" +
+                            std::to_string(op->csr.is_real) + "|NR=" + std::to_string(nb0) +
+                            "|prec=" + std::to_string(precision);
+    std::string cached;
+    int th = 0, pad = 0;
+    if (tune_cache_get(key, &cached) && std::sscanf(cached.c_str(), "%d,%d", &th, &pad) == 2 &&
+        th >= 32 && th <= 1024 && th % 32 == 0 && (pad == 0 || pad == 1)) {
+      shape.threads = th;
+      shape.padded = pad != 0;
+    } else {
+      std::vector<EnsembleShape> cands;
+      for (int t : {256, 512, 1024}) {
+        cands.push_back({t, false});
+        if (ff && op->csr.ell_w > 0 && op->csr.max_row_nnz <= 8) cands.push_back({t, true});
+      }
+      const int64_t NCt = std::min<int64_t>(NC, 64);
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      KPMGB_CUDA(cudaEventCreate(&e0));
+      KPMGB_CUDA(cudaEventCreate(&e1));
+      float best = 0.f;
+      int rc = KPMGB_OK;
+      for (const EnsembleShape& c : cands) {
+        const double* scale = nullptr;
+        if ((rc = load(0, nb0, &scale)) != KPMGB_OK) break;
+        cudaEventRecord(e0, s);
+        rc = launch_ensemble(op->csr, d_seg, d_order, nseg, nb0, NCt, slots,
+                             slots + (size_t)NH * nb0 * 16, ws.mu.as<double2>(), scale, next,
+                             ws.sync.as<unsigned>() + 1, precision, s, c);
+        cudaEventRecord(e1, s);
+        if (rc != KPMGB_OK) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+          rc = fail(KPMGB_ERR_CUDA, "ensemble autotuning: %s",
+                    cudaGetErrorString(cudaGetLastError()));
+          break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (best == 0.f || ms < best) {
+          best = ms;
+          shape = c;
+        }
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      KPMGB_TRY(rc);
+      tune_cache_put(key, std::to_string(shape.threads) + "," + (shape.padded ? "1" : "0"));
+    }
+  }
+  for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
+    const int nb = (int)std::min<int64_t>(kBatch, NR - c0);
+    const size_t bb = (size_t)NH * nb * 16;
+    const double* scale = nullptr;
+    KPMGB_TRY(load(c0, nb, &scale));
     KPMGB_TRY(launch_ensemble(op->csr, d_seg, d_order, nseg, nb, NC, slots, slots + bb,
                               ws.mu.as<double2>(), scale, next, ws.sync.as<unsigned>() + 1,
-                              precision, s));
+                              precision, s, shape));
     // [nseg][NC][nb] -> columns c0 .. c0+nb of the caller's [nseg][NC][NR]
     KPMGB_CUDA(cudaMemcpy2DAsync(mu_all + 2 * c0, (size_t)NR * 16, ws.mu.ptr, (size_t)nb * 16,
                                  (size_t)nb * 16, (size_t)nseg * NC, cudaMemcpyDeviceToHost, s));
@@ -906,6 +988,120 @@ extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_
   }
   KPMGB_CUDA(cudaMemcpyAsync(grad, gcsc, (size_t)op->csr.nnz * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
+}
+
+// ------------------------------------------------------- kpm_2d gradient
+namespace kpmgb {
+size_t kpm2d_grad_work_bytes(int64_t NH, int NR, int64_t NC);
+int run_kpm2d_grad(const DeviceCSR& H, const DeviceCSR& Ja, const DeviceCSR& Jb,
+                   const DeviceCSR& JbH, int64_t NC, int NR, int64_t NH, const double2* psil,
+                   const double2* psir, const double2* Gp, const double2* GpH, double2* gH,
+                   double2* gJa, double2* gJb, DevBuf& work, cudaStream_t s);
+int scatter_grad(const double2* gcsr, const int* perm, int64_t nnz, double2* gcsc,
+                 cudaStream_t s);
+namespace {
+// device buffers of one call, released on every exit path
+struct CallBufs {
+  std::vector<DevBuf> b;
+  explicit CallBufs(size_t n) : b(n) {}
+  ~CallBufs() {
+    for (DevBuf& x : b) x.release();
+  }
+};
+}  // namespace
+}  // namespace kpmgb
+
+extern "C" int kpmgb_kpm2d_grad(kpmgb_operator h, kpmgb_operator ja, kpmgb_operator jb,
+                                kpmgb_operator jbh, int64_t NC, int64_t NR, int64_t NH,
+                                const double* psi_l, const double* psi_r, const double* G,
+                                int32_t moment_parity, double* grad_H, double* grad_Ja,
+                                double* grad_Jb) {
+  clear_error();
+  if (!h || !ja || !jb || !jbh) return fail(KPMGB_ERR_ARGUMENT, "null operator");
+  if (!psi_l || !psi_r || !G || !grad_H || !grad_Ja || !grad_Jb)
+    return fail(KPMGB_ERR_ARGUMENT, "null argument");
+  if (NC < 2 || NC > (1 << 16)) return fail(KPMGB_ERR_ARGUMENT, "NC must be in 2..65536");
+  if (NR < 1) return fail(KPMGB_ERR_ARGUMENT, "NR must be positive");
+  if (moment_parity < 0 || moment_parity > 2)
+    return fail(KPMGB_ERR_ARGUMENT, "moment_parity=%d not understood.", moment_parity);
+  Operator* op = as_op(h);
+  Operator* A = as_op(ja);
+  Operator* B = as_op(jb);
+  Operator* BH = as_op(jbh);
+  if (NH != op->csr.n || NH != A->csr.n || NH != B->csr.n || NH != BH->csr.n)
+    return fail(KPMGB_ERR_ARGUMENT, "operators and probes disagree on NH=%lld", (long long)NH);
+  Guard gd(op);
+  cudaStream_t s = op->stream;
+  constexpr int64_t kBatch = 32;
+  const int64_t nb_max = std::min<int64_t>(NR, kBatch);
+  const size_t blk = (size_t)NH * nb_max * 16;
+  {
+    size_t fr = 0, tot = 0;
+    KPMGB_CUDA(cudaMemGetInfo(&fr, &tot));
+    const size_t need = kpm2d_grad_work_bytes(NH, (int)nb_max, NC);
+    if (need > fr + op->ws.split.bytes)
+      return fail(KPMGB_ERR_ALLOC,
+                  "kpm_2d gradient keeps 5*NC + 5 blocks of NH x min(NR, 32) complex values "
+                  "resident (%zu bytes); the device has %zu free", need, fr);
+  }
+  // G with the parity mask and 1/NR, and its conjugate transpose
+  std::vector<double> gp(2 * NC * NC), gph(2 * NC * NC);
+  for (int64_t m = 0; m < NC; ++m)
+    for (int64_t n = 0; n < NC; ++n) {
+      const bool keep = moment_parity == KPMGB_PARITY_NONE ||
+                        (moment_parity == KPMGB_PARITY_ODD && (n + m) % 2 == 1) ||
+                        (moment_parity == KPMGB_PARITY_EVEN && (n + m) % 2 == 0);
+      const double f = keep ? 1.0 / (double)NR : 0.0;
+      const size_t i = (size_t)(n + NC * m), t = (size_t)(m + NC * n);
+      gp[2 * i] = f * G[2 * i];
+      gp[2 * i + 1] = f * G[2 * i + 1];
+      gph[2 * t] = gp[2 * i];
+      gph[2 * t + 1] = -gp[2 * i + 1];
+    }
+  CallBufs cb(6);
+  DevBuf &dG = cb.b[0], &dGH = cb.b[1], &dpsi = cb.b[2], &gh = cb.b[3], &ga = cb.b[4],
+         &gb = cb.b[5];
+  const size_t gbytes = (size_t)NC * NC * 16;
+  KPMGB_TRY(dG.ensure(gbytes));
+  KPMGB_TRY(dGH.ensure(gbytes));
+  KPMGB_TRY(dpsi.ensure(4 * blk));
+  KPMGB_TRY(gh.ensure((size_t)std::max<int64_t>(op->csr.nnz, 1) * 32));
+  KPMGB_TRY(ga.ensure((size_t)std::max<int64_t>(A->csr.nnz, 1) * 32));
+  KPMGB_TRY(gb.ensure((size_t)std::max<int64_t>(B->csr.nnz, 1) * 32));
+  KPMGB_CUDA(cudaMemcpyAsync(dG.ptr, gp.data(), gbytes, cudaMemcpyHostToDevice, s));
+  KPMGB_CUDA(cudaMemcpyAsync(dGH.ptr, gph.data(), gbytes, cudaMemcpyHostToDevice, s));
+  KPMGB_CUDA(cudaMemsetAsync(gh.ptr, 0, (size_t)op->csr.nnz * 16, s));
+  KPMGB_CUDA(cudaMemsetAsync(ga.ptr, 0, (size_t)A->csr.nnz * 16, s));
+  KPMGB_CUDA(cudaMemsetAsync(gb.ptr, 0, (size_t)B->csr.nnz * 16, s));
+  char* in = dpsi.as<char>();
+  for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
+    const int64_t nb = std::min<int64_t>(kBatch, NR - c0);
+    const size_t bb = (size_t)NH * nb * 16;
+    KPMGB_CUDA(cudaMemcpyAsync(in, psi_l + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
+    KPMGB_CUDA(cudaMemcpyAsync(in + blk, psi_r + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
+    KPMGB_TRY(launch_load_block(in, in + 2 * blk, NH, (int)nb, KPMGB_PREC_FP64, nullptr, false, s));
+    KPMGB_TRY(launch_load_block(in + blk, in + 3 * blk, NH, (int)nb, KPMGB_PREC_FP64, nullptr,
+                                false, s));
+    KPMGB_TRY(run_kpm2d_grad(op->csr, A->csr, B->csr, BH->csr, NC, (int)nb, NH,
+                             reinterpret_cast<const double2*>(in + 2 * blk),
+                             reinterpret_cast<const double2*>(in + 3 * blk),
+                             dG.as<double2>(), dGH.as<double2>(), gh.as<double2>(),
+                             ga.as<double2>(), gb.as<double2>(), op->ws.split, s));
+  }
+  struct Out {
+    DevBuf* g;
+    const DeviceCSR* c;
+    double* host;
+  } outs[3] = {{&gh, &op->csr, grad_H}, {&ga, &A->csr, grad_Ja}, {&gb, &B->csr, grad_Jb}};
+  for (const Out& o : outs) {
+    if (o.c->nnz < 1) continue;
+    double2* csr = o.g->as<double2>();
+    double2* csc = csr + o.c->nnz;
+    KPMGB_TRY(scatter_grad(csr, o.c->perm, o.c->nnz, csc, s));
+    KPMGB_CUDA(cudaMemcpyAsync(o.host, csc, (size_t)o.c->nnz * 16, cudaMemcpyDeviceToHost, s));
+  }
+  KPMGB_CUDA(cudaStreamSynchronize(s));
+  return KPMGB_OK;
 }
 
 // ------------------------------------------------------- chebyshev_action

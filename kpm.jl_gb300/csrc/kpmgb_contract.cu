@@ -173,11 +173,13 @@ int launch_contract(const ContractArgs& a, int precision, int contraction, cudaS
   kslice = (kslice + KC - 1) / KC * KC;
   dim3 grid((a.nr + TM - 1) / TM, (a.nl + TN - 1) / TN, S);
   double2* part = static_cast<double2*>(a.scratch);
+  cudaEvent_t t0 = timing_mark(s);
   if (precision == KPMGB_PREC_FF)
     k_contract_f64<true><<<grid, 256, 0, s>>>(a.R, a.L, a.K, a.nr, a.nl, kslice, part);
   else
     k_contract_f64<false><<<grid, 256, 0, s>>>(a.R, a.L, a.K, a.nr, a.nl, kslice, part);
   KPMGB_LAUNCHED();
+  timing_add(TIMED_CONTRACT_FP64, t0, timing_mark(s));
   const int64_t total = (int64_t)a.nr * a.nl;
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, 2048);
   k_contract_reduce<<<blocks, 256, 0, s>>>(part, S, a.nr, a.nl, a.n0, a.m0, a.NC, a.inv_nr,

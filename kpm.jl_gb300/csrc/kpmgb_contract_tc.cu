@@ -633,8 +633,10 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
   t.part = part;
   t.status = a.status;
   dim3 grid(pl.mtiles, pl.ntiles, pl.nsplit);
+  cudaEvent_t t0 = timing_mark(s);
   k_contract_tc<<<grid, kThreadsTC, TC_STAGES * STAGE_BYTES, s>>>(t);
   KPMGB_LAUNCHED();
+  timing_add(TIMED_CONTRACT_SPLIT, t0, timing_mark(s));
   const int64_t total = (int64_t)a.nr * a.nl;
   const int blocks = (int)std::min<int64_t>((total + 255) / 256, 2048);
   k_tc_reduce<<<std::max(blocks, 1), 256, 0, s>>>(part, pl.nsplit, a.nr, a.nl, a.n0, a.m0, a.NC,

@@ -186,7 +186,8 @@ __device__ __forceinline__ void ffdacc(float& S, float& C, float ah, float al, f
 // Persistent ensemble kernel: LPR lanes per row, one column per lane (NR <= 32).
 template <bool FF, bool REALH, int LPR>
 __global__ void __launch_bounds__(kEnsThreads) k_ensemble(EnsParams p) {
-  constexpr int GROUPS = kEnsThreads / LPR;
+  const int GROUPS = (int)blockDim.x / LPR;
+  const int nwarps = (int)blockDim.x >> 5;
   __shared__ int s_q;
   __shared__ double2 red[kEnsWarps][2][32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(kEnsThreads) k_ensemble(EnsParams p) {
       __syncthreads();
       if (tid < p.NR) {
         double2 a = make_double2(0.0, 0.0), b = make_double2(0.0, 0.0);
-        for (int w = 0; w < kEnsWarps; ++w) {
+        for (int w = 0; w < nwarps; ++w) {
           a.x += red[w][0][tid].x;
           b.x += red[w][1][tid].x;
           b.y += red[w][1][tid].y;
@@ -285,6 +286,146 @@ __global__ void __launch_bounds__(kEnsThreads) k_ensemble(EnsParams p) {
   }
 }
 
+// Float-float ensemble kernel over fixed-width padded rows (the stacked
+// operator's padded copy, stride ell_w): per row one anchored chunk of at most
+// 8 slots (slots past the member's longest row are skipped, padding slots hold
+// 0), the row's z, own x and every gather issued before the arithmetic, and
+// the doubling dots <x|x> and Re<x|y> (Hermitian H: <x|y> is real, its
+// imaginary part is stored as 0).  Threads per CTA are a launch parameter
+// (multiple of 32, at most kEnsThreads).
+template <bool REALH, int LPR>
+__global__ void __launch_bounds__(kEnsThreads) k_ensemble_ell(EnsParams p, const int* ecol,
+                                                              const void* evalv, int ew, int w) {
+  using HV = typename std::conditional<REALH, float2, float4>::type;
+  const HV* __restrict__ eval = static_cast<const HV*>(evalv);
+  __shared__ int s_q;
+  __shared__ double2 red[kEnsWarps][2][32];
+  const int nthreads = blockDim.x;
+  const int nwarps = nthreads >> 5;
+  const int groups = nthreads / LPR;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = tid / LPR, cc = tid % LPR;
+  const bool active_col = cc < p.NR;
+  for (;;) {
+    if (tid == 0) s_q = (int)atomicAdd(p.next, 1u);
+    __syncthreads();
+    const int q = s_q;
+    __syncthreads();
+    if (q >= p.nseg) break;
+    const int seg = p.order[q];
+    const int64_t r0 = p.seg[seg], r1 = p.seg[seg + 1];
+    float4* sl[2] = {static_cast<float4*>(p.slot0), static_cast<float4*>(p.slot1)};
+    double2* mu = p.mu + (size_t)seg * p.NC * p.NR;
+    int ip = 1, ipp = 0;
+    for (int64_t n = 1; n <= p.NC / 2; ++n) {
+      const bool first = n == 1;
+      const float4* x = first ? sl[0] : sl[ip];
+      float4* y = first ? sl[1] : sl[ipp];
+      const float alpha = first ? 1.f : 2.f;
+      float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
+      for (int64_t r = r0 + g; r < r1; r += groups) {
+        if (!active_col) continue;
+        const int64_t idx = r * p.NR + cc;
+        const int* jr = ecol + r * ew;
+        const HV* hr = eval + r * ew;
+        int jj[8];
+        HV hv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (u < w) {
+            jj[u] = __ldg(jr + u);
+            hv[u] = __ldg(hr + u);
+          } else {
+            jj[u] = (int)r;
+            if constexpr (REALH) hv[u] = make_float2(0.f, 0.f);
+            else hv[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+        const float4 zz = first ? make_float4(0.f, 0.f, 0.f, 0.f) : y[idx];
+        const float4 xo = x[idx];
+        float4 xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) xv[u] = u < w ? x[(int64_t)jj[u] * p.NR + cc] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float R = 0.f, M = 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          R = __fadd_rn(R, ens_habs(hv[u]));
+          M = fmaxf(M, fmaxf(fabsf(xv[u].x), fabsf(xv[u].z)));
+        }
+        const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+        const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+        float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (u < w) ens_ffmac(Ar, cr, Ai, ci, hv[u], xv[u]);
+        const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+        const float2 yr = ens_epi(sr, cr, alpha, !first, zz.x, zz.y);
+        const float2 yi = ens_epi(si, ci, alpha, !first, zz.z, zz.w);
+        const float4 yv = make_float4(yr.x, yr.y, yi.x, yi.y);
+        y[idx] = yv;
+        ffdacc(S0, C0, xo.x, xo.y, xo.x, xo.y);
+        ffdacc(S0, C0, xo.z, xo.w, xo.z, xo.w);
+        ffdacc(S1, C1, xo.x, xo.y, yv.x, yv.y);
+        ffdacc(S1, C1, xo.z, xo.w, yv.z, yv.w);
+      }
+      double2 d0 = make_double2(ff::join(S0, C0), 0.0), d1 = make_double2(ff::join(S1, C1), 0.0);
+#pragma unroll
+      for (int off = LPR; off < 32; off <<= 1) {
+        d0.x += __shfl_xor_sync(0xffffffffu, d0.x, off);
+        d1.x += __shfl_xor_sync(0xffffffffu, d1.x, off);
+      }
+      if (lane < LPR) {
+        red[warp][0][lane] = d0;
+        red[warp][1][lane] = d1;
+      }
+      __syncthreads();
+      if (tid < p.NR) {
+        double a = 0.0, b = 0.0;
+        for (int wi = 0; wi < nwarps; ++wi) {
+          a += red[wi][0][tid].x;
+          b += red[wi][1][tid].x;
+        }
+        const double f = p.scale ? p.scale[tid] : 1.0;
+        a *= f;
+        b *= f;
+        if (first) {
+          mu[tid] = make_double2(a, 0.0);
+          mu[p.NR + tid] = make_double2(b, 0.0);
+        } else {
+          const double2 m0 = mu[tid], m1 = mu[p.NR + tid];
+          const double2 o0 = make_double2(2.0 * a - m0.x, -m0.y);
+          const double2 o1 = make_double2(2.0 * b - m1.x, -m1.y);
+          mu[(2 * n - 2) * p.NR + tid] = o0;
+          mu[(2 * n - 1) * p.NR + tid] = o1;
+          if (!isfinite(o0.x) || !isfinite(o1.x)) atomicOr(p.status, (unsigned)STATUS_NONFINITE);
+        }
+      }
+      __syncthreads();
+      if (!first) {
+        const int t = ip;
+        ip = ipp;
+        ipp = t;
+      }
+    }
+  }
+}
+
+void* pick_ensemble_ell(bool real, int NR) {
+  const int lpr = NR <= 1 ? 1 : NR <= 2 ? 2 : NR <= 4 ? 4 : NR <= 8 ? 8 : NR <= 16 ? 16 : 32;
+  switch (lpr) {
+#define KPMGB_ENS_ELL(L) \
+  case L: return real ? (void*)k_ensemble_ell<true, L> : (void*)k_ensemble_ell<false, L>;
+    KPMGB_ENS_ELL(1)
+    KPMGB_ENS_ELL(2)
+    KPMGB_ENS_ELL(4)
+    KPMGB_ENS_ELL(8)
+    KPMGB_ENS_ELL(16)
+    KPMGB_ENS_ELL(32)
+#undef KPMGB_ENS_ELL
+  }
+  return nullptr;
+}
+
 template <bool FF, bool REALH>
 using EnsFn = void (*)(EnsParams);
 
@@ -312,8 +453,12 @@ void* pick_ensemble(bool ff, bool real, int NR) {
 
 int launch_ensemble(const DeviceCSR& H, const int64_t* d_seg, const int* d_order, int nseg, int NR,
                     int64_t NC, void* slot0, void* slot1, double2* mu, const double* scale,
-                    unsigned* next, unsigned* status, int precision, cudaStream_t s) {
+                    unsigned* next, unsigned* status, int precision, cudaStream_t s,
+                    const EnsembleShape& shape) {
   if (NR < 1 || NR > 32) return fail(KPMGB_ERR_ARGUMENT, "the ensemble kernel supports 1 <= NR <= 32");
+  if (shape.threads < 32 || shape.threads > kEnsThreads || shape.threads % 32 != 0)
+    return fail(KPMGB_ERR_ARGUMENT, "ensemble threads per CTA must be a multiple of 32 up to %d",
+                kEnsThreads);
   const bool ff = precision == KPMGB_PREC_FF;
   EnsParams p;
   p.rowptr = H.rowptr;
@@ -330,14 +475,22 @@ int launch_ensemble(const DeviceCSR& H, const int64_t* d_seg, const int* d_order
   p.scale = scale;
   p.next = next;
   p.status = status;
-  void* fn = pick_ensemble(ff, H.is_real != 0, NR);
+  const bool ell = shape.padded && ff && H.ell_w > 0 && H.max_row_nnz <= 8;
+  if (shape.padded && !ell)
+    return fail(KPMGB_ERR_ARGUMENT, "the padded-row ensemble kernel serves float-float members "
+                                    "with at most 8 nonzeros per row");
+  void* fn = ell ? pick_ensemble_ell(H.is_real != 0, NR) : pick_ensemble(ff, H.is_real != 0, NR);
   int per_sm = 1, dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kEnsThreads, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, shape.threads, 0);
   const int grid = std::max(1, std::min(nseg, std::max(per_sm, 1) * sms));
-  void* args[] = {&p};
-  KPMGB_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(kEnsThreads), args, 0, s));
+  const int* ecol = H.ell_col;
+  const void* evalv = H.ell_val;
+  int ew = H.ell_w, w = H.max_row_nnz;
+  void* args_csr[] = {&p};
+  void* args_ell[] = {&p, &ecol, &evalv, &ew, &w};
+  KPMGB_CUDA(cudaLaunchKernel(fn, dim3(grid), dim3(shape.threads), ell ? args_ell : args_csr, 0, s));
   KPMGB_LAUNCHED();
   return KPMGB_OK;
 }

@@ -47,6 +47,24 @@ extern std::atomic<int64_t> g_launches;
                            cudaGetErrorString(le_), __FILE__, __LINE__);     \
   } while (0)
 
+// Kernel timing instrumentation (kpmgb_timing.cu; off unless enabled through
+// kpmgb_timing_enable): timing_mark records an event on s and returns it
+// (nullptr when timing is off); timing_add files a (before, after) pair.
+enum TimedKernel : int {
+  TIMED_CONTRACT_SPLIT = KPMGB_TIMED_CONTRACT_SPLIT,
+  TIMED_CONTRACT_FP64 = KPMGB_TIMED_CONTRACT_FP64,
+  TIMED_COUNT = 2,
+};
+cudaEvent_t timing_mark(cudaStream_t s);
+void timing_add(int kernel, cudaEvent_t e0, cudaEvent_t e1);
+
+// Persistent autotuning cache (kpmgb_tune.cu): "key value" lines in the file
+// KPMGB_TUNE_CACHE (or $XDG_CACHE_HOME/kpmgb/tune.txt, $HOME/.cache/...).
+std::string tune_cache_path();
+std::string device_tag();
+bool tune_cache_get(const std::string& key, std::string* value);
+void tune_cache_put(const std::string& key, const std::string& value);
+
 // ------------------------------------------------------------- resources
 // Grow-only device buffer owned by an operator handle.
 struct DevBuf {
@@ -244,6 +262,13 @@ int launch_kpm1d_cluster(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, boo
                          int precision, const void* psi, const void* bra, double2* mu,
                          const double* mom_scale, double growth_limit, unsigned* status,
                          cudaStream_t s);
+
+// Launch shape of the persistent ensemble kernel (chosen by its autotuner):
+// threads per CTA and CSR rows or the padded-row float-float kernel.
+struct EnsembleShape {
+  int threads = 1024;
+  bool padded = false;
+};
 
 namespace step {
 // Fixed-width padded rows of the float-float values (kpmgb_step_ffe.cu):

@@ -177,6 +177,66 @@ k_kubo_fermi(const double2* __restrict__ partial, int nb, int64_t Q, const doubl
   if (threadIdx.x == 0) sigma[blockIdx.x] = scale * red[0];
 }
 
+// Weights of sigma(Ef) as a linear functional of the moments,
+//   sigma = Re sum_{n,m} W[n,m] mu[n,m],
+//   W[n,m] = scale k_n k_m sum_j phi_j (T_n(x_j) WM[m,j] + T_m(x_j) WN[n,j]),
+// phi_j = w f(a x_j + b; Ef) / s_j^3, WM[m,j] = (x_j - i m s_j) e^{i m theta_j},
+// WN = conj(WM): the reconstruction above read as W (for gradients through
+// sigma).  A 16 x 16 tile of (n, m) per block, nodes staged through shared
+// memory in chunks.
+constexpr int kWT = 16;
+constexpr int kWJ = 64;
+__global__ void __launch_bounds__(kWT * kWT)
+k_kubo_weights(int NC, const double* __restrict__ kv, int64_t Q, const double* __restrict__ x,
+               const double* __restrict__ theta, const double* __restrict__ sn,
+               const double* __restrict__ phi, double scale, double2* __restrict__ W) {
+  __shared__ double scn[kWT][kWJ], ssn[kWT][kWJ];   // cos / sin(n theta_j), n of the tile
+  __shared__ double scm[kWT][kWJ], ssm[kWT][kWJ];   // cos / sin(m theta_j)
+  __shared__ double sx[kWJ], ss[kWJ], sp[kWJ];
+  const int tn = threadIdx.x % kWT, tm = threadIdx.x / kWT;
+  const int n0 = blockIdx.x * kWT, m0 = blockIdx.y * kWT;
+  const int n = n0 + tn, m = m0 + tm;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int64_t j0 = 0; j0 < Q; j0 += kWJ) {
+    for (int e = threadIdx.x; e < kWT * kWJ; e += kWT * kWT) {
+      const int jj = e % kWJ, t = e / kWJ;
+      const int64_t j = j0 + jj;
+      double c1 = 0.0, s1 = 0.0, c2 = 0.0, s2 = 0.0;
+      if (j < Q) {
+        sincos((double)(n0 + t) * theta[j], &s1, &c1);
+        sincos((double)(m0 + t) * theta[j], &s2, &c2);
+      }
+      scn[t][jj] = c1;
+      ssn[t][jj] = s1;
+      scm[t][jj] = c2;
+      ssm[t][jj] = s2;
+    }
+    for (int e = threadIdx.x; e < kWJ; e += kWT * kWT) {
+      const int64_t j = j0 + e;
+      sx[e] = j < Q ? x[j] : 0.0;
+      ss[e] = j < Q ? sn[j] : 0.0;
+      sp[e] = j < Q ? phi[j] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < kWJ; ++jj) {
+      const double xj = sx[jj], sj = ss[jj], ph = sp[jj];
+      const double cn = scn[tn][jj], sn_ = ssn[tn][jj], cm = scm[tm][jj], sm = ssm[tm][jj];
+      // T_n WM[m] = cn (x - i m s)(cm + i sm);  T_m WN[n] = cm (x + i n s)(cn - i sn)
+      const double ms = (double)m * sj, ns = (double)n * sj;
+      const double re = cn * (xj * cm + ms * sm) + cm * (xj * cn + ns * sn_);
+      const double im = cn * (xj * sm - ms * cm) + cm * (ns * cn - xj * sn_);
+      acc.x = fma(ph, re, acc.x);
+      acc.y = fma(ph, im, acc.y);
+    }
+    __syncthreads();
+  }
+  if (n < NC && m < NC) {
+    const double k = scale * kv[n] * kv[m];
+    W[(size_t)n + (size_t)m * NC] = make_double2(k * acc.x, k * acc.y);
+  }
+}
+
 // rho[e] = sum_n c_n cos(n theta_e) / (a pi sin theta_e) inside |E - b| < a, else 0
 __global__ void k_dos(const double* __restrict__ c, int NC, double a, double b,
                       const double* __restrict__ E, int64_t nE, double* __restrict__ rho) {
@@ -194,6 +254,74 @@ __global__ void k_dos(const double* __restrict__ c, int NC, double a, double b,
     rho[e] = s / (a * M_PI * sqrt(1.0 - xe * xe));
   }
 }
+
+// Energy derivatives of the DOS (src/applications/dos.jl:128-139, where the
+// reference nests ForwardDiff derivatives of the reconstruction at one
+// energy).  Truncated Taylor series in the energy offset h ("jets": f(E + h)
+// = sum_k f_k h^k, f^(k)(E) = k! f_k) carry the derivatives exactly through
+//   x = (E - b)/a                      jet (x0, 1/a, 0, ...),
+//   T_{n+1} = 2 x T_n - T_{n-1}        jet products with x,
+//   S = sum_n c_n T_n(x),
+//   q = a pi sqrt(1 - x^2)             jet square root,
+//   rho = S / q                        jet division,
+// one energy per thread, orders 1..K.
+template <int K>
+__global__ void k_dos_jet(const double* __restrict__ c, int NC, double a, double b,
+                          const double* __restrict__ E, int64_t nE, double* __restrict__ rho) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nE;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double d = E[e] - b;
+    if (!(fabs(d) < a)) {
+      rho[e] = 0.0;
+      continue;
+    }
+    const double x0 = d / a, dx = 1.0 / a;
+    double Tm[K + 1], T[K + 1], S[K + 1];
+#pragma unroll
+    for (int k = 0; k <= K; ++k) {
+      Tm[k] = k == 0 ? 1.0 : 0.0;
+      T[k] = k == 0 ? x0 : (k == 1 ? dx : 0.0);
+      S[k] = c[0] * Tm[k] + (NC > 1 ? c[1] * T[k] : 0.0);
+    }
+    for (int n = 1; n + 1 < NC; ++n) {
+      const double cn = c[n + 1];
+#pragma unroll
+      for (int k = K; k >= 0; --k) {
+        const double t = 2.0 * (x0 * T[k] + (k > 0 ? dx * T[k - 1] : 0.0)) - Tm[k];
+        Tm[k] = T[k];
+        T[k] = t;
+        S[k] = fma(cn, t, S[k]);
+      }
+    }
+    // q = a pi sqrt(u), u = 1 - x^2 = (1 - x0^2) - 2 x0 dx h - dx^2 h^2
+    double u[K + 1], q[K + 1], r[K + 1];
+#pragma unroll
+    for (int k = 0; k <= K; ++k) u[k] = k == 0 ? 1.0 - x0 * x0 : (k == 1 ? -2.0 * x0 * dx : (k == 2 ? -dx * dx : 0.0));
+    q[0] = sqrt(u[0]);
+#pragma unroll
+    for (int k = 1; k <= K; ++k) {
+      double acc = u[k];
+#pragma unroll
+      for (int j = 1; j < k; ++j) acc -= q[j] * q[k - j];
+      q[k] = acc / (2.0 * q[0]);
+    }
+#pragma unroll
+    for (int k = 0; k <= K; ++k) q[k] *= a * M_PI;
+#pragma unroll
+    for (int k = 0; k <= K; ++k) {
+      double acc = S[k];
+#pragma unroll
+      for (int j = 1; j <= k; ++j) acc -= q[j] * r[k - j];
+      r[k] = acc / q[0];
+    }
+    double fact = 1.0;
+#pragma unroll
+    for (int k = 2; k <= K; ++k) fact *= (double)k;
+    rho[e] = fact * r[K];
+  }
+}
+
+constexpr int kMaxDosOrder = 4;
 
 // Jackson damping g_n (src/kernels/jackson_kernel.jl:7-8)
 void jackson(int64_t N, std::vector<double>& g) {
@@ -307,9 +435,91 @@ extern "C" int kpmgb_kubo_bastin(const double* mu2d, int64_t ld, int64_t NC, dou
   return KPMGB_OK;
 }
 
+extern "C" int kpmgb_kubo_bastin_weights(int64_t NC, double a, double b, double Ef, int64_t NH,
+                                         double area, double beta, const double* damping,
+                                         int64_t quad_N, double edge_cutoff, double* W) {
+  clear_error();
+  if (!W) return fail(KPMGB_ERR_ARGUMENT, "null argument");
+  if (!(a > 0)) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: a must be positive.");
+  if (!(area > 0)) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: area must be positive.");
+  if (NH <= 0) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: NH must be positive.");
+  if (quad_N <= 0) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: quad_N must be positive.");
+  if (!(edge_cutoff >= 0 && edge_cutoff < 1))
+    return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: edge_cutoff must be in [0, 1).");
+  if (NC < 1 || NC > (1 << 16)) return fail(KPMGB_ERR_ARGUMENT, "NC must be in 1..65536");
+  std::vector<double> xs, th, sn, phi;
+  const double w = M_PI / (double)quad_N;
+  for (int64_t k = quad_N; k >= 1; --k) {
+    const double xk = std::cos((double)(2 * k - 1) * M_PI / (double)(2 * quad_N));
+    if (!(std::fabs(xk) < 1.0 - edge_cutoff)) continue;
+    const double E = a * xk + b;
+    double f;
+    if (std::isinf(beta)) {
+      f = ((E < Ef ? 1.0 : 0.0) + (E <= Ef ? 1.0 : 0.0)) / 2.0;
+    } else {
+      f = 1.0 / (std::exp((E - Ef) * beta) + 1.0);
+    }
+    if (f == 0.0) continue;
+    const double s = std::sqrt(1.0 - xk * xk);
+    xs.push_back(xk);
+    th.push_back(std::acos(xk));
+    sn.push_back(s);
+    phi.push_back(w * f / (s * s * s));
+  }
+  std::vector<double> kv;
+  if (damping) {
+    kv.assign(damping, damping + NC);
+  } else {
+    jackson(NC, kv);
+  }
+  for (int64_t n = 0; n < NC; ++n) kv[n] *= (n ? 2.0 : 1.0);
+  const int64_t Q = (int64_t)xs.size();
+  if (Q == 0) {
+    std::fill(W, W + 2 * NC * NC, 0.0);
+    return KPMGB_OK;
+  }
+  CallScratch cs;
+  KPMGB_CUDA(cudaStreamCreateWithFlags(&cs.s, cudaStreamNonBlocking));
+  double *d_kv = nullptr, *d_x = nullptr, *d_th = nullptr, *d_sn = nullptr, *d_phi = nullptr;
+  double2* d_W = nullptr;
+  KPMGB_TRY(cs.alloc(&d_kv, NC));
+  KPMGB_TRY(cs.alloc(&d_x, Q));
+  KPMGB_TRY(cs.alloc(&d_th, Q));
+  KPMGB_TRY(cs.alloc(&d_sn, Q));
+  KPMGB_TRY(cs.alloc(&d_phi, Q));
+  KPMGB_TRY(cs.alloc(&d_W, (size_t)NC * NC));
+  KPMGB_CUDA(cudaMemcpyAsync(d_kv, kv.data(), NC * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_x, xs.data(), Q * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_th, th.data(), Q * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_sn, sn.data(), Q * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  KPMGB_CUDA(cudaMemcpyAsync(d_phi, phi.data(), Q * sizeof(double), cudaMemcpyHostToDevice, cs.s));
+  const double scale = -2.0 * (double)NH / (area * a * a);
+  dim3 grid((unsigned)((NC + kWT - 1) / kWT), (unsigned)((NC + kWT - 1) / kWT));
+  k_kubo_weights<<<grid, kWT * kWT, 0, cs.s>>>((int)NC, d_kv, Q, d_x, d_th, d_sn, d_phi, scale,
+                                              d_W);
+  KPMGB_LAUNCHED();
+  KPMGB_CUDA(cudaMemcpyAsync(W, d_W, (size_t)NC * NC * sizeof(double2), cudaMemcpyDeviceToHost,
+                             cs.s));
+  KPMGB_CUDA(cudaStreamSynchronize(cs.s));
+  return KPMGB_OK;
+}
+
+extern "C" int kpmgb_dos_derivative(const double* mu, int64_t NC, double a, double b,
+                                    const double* damping, const double* E, int64_t nE,
+                                    int32_t dE_order, double* rho);
+
 extern "C" int kpmgb_dos(const double* mu, int64_t NC, double a, double b, const double* damping,
                          const double* E, int64_t nE, double* rho) {
+  return kpmgb_dos_derivative(mu, NC, a, b, damping, E, nE, 0, rho);
+}
+
+extern "C" int kpmgb_dos_derivative(const double* mu, int64_t NC, double a, double b,
+                                    const double* damping, const double* E, int64_t nE,
+                                    int32_t dE_order, double* rho) {
   clear_error();
+  if (dE_order < 0 || dE_order > kMaxDosOrder)
+    return fail(KPMGB_ERR_ARGUMENT, "dos: dE_order must be in 0..%d (got %d)", kMaxDosOrder,
+                (int)dE_order);
   if (!mu || !E || !rho) return fail(KPMGB_ERR_ARGUMENT, "null argument");
   if (!(a > 0)) return fail(KPMGB_ERR_ARGUMENT, "dos: the rescale factor a must be positive");
   if (NC < 1) return fail(KPMGB_ERR_ARGUMENT, "dos: NC must be >= 1");
@@ -330,7 +540,13 @@ extern "C" int kpmgb_dos(const double* mu, int64_t NC, double a, double b, const
   KPMGB_TRY(cs.alloc(&d_rho, nE));
   KPMGB_CUDA(cudaMemcpyAsync(d_c, c.data(), NC * sizeof(double), cudaMemcpyHostToDevice, cs.s));
   KPMGB_CUDA(cudaMemcpyAsync(d_E, E, nE * sizeof(double), cudaMemcpyHostToDevice, cs.s));
-  k_dos<<<grid1d(nE), 256, 0, cs.s>>>(d_c, (int)NC, a, b, d_E, nE, d_rho);
+  switch (dE_order) {
+    case 0: k_dos<<<grid1d(nE), 256, 0, cs.s>>>(d_c, (int)NC, a, b, d_E, nE, d_rho); break;
+    case 1: k_dos_jet<1><<<grid1d(nE), 256, 0, cs.s>>>(d_c, (int)NC, a, b, d_E, nE, d_rho); break;
+    case 2: k_dos_jet<2><<<grid1d(nE), 256, 0, cs.s>>>(d_c, (int)NC, a, b, d_E, nE, d_rho); break;
+    case 3: k_dos_jet<3><<<grid1d(nE), 256, 0, cs.s>>>(d_c, (int)NC, a, b, d_E, nE, d_rho); break;
+    default: k_dos_jet<4><<<grid1d(nE), 256, 0, cs.s>>>(d_c, (int)NC, a, b, d_E, nE, d_rho); break;
+  }
   KPMGB_LAUNCHED();
   KPMGB_CUDA(cudaMemcpyAsync(rho, d_rho, nE * sizeof(double), cudaMemcpyDeviceToHost, cs.s));
   KPMGB_CUDA(cudaStreamSynchronize(cs.s));

@@ -208,6 +208,8 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
         if (KernelFn fe = select_kernel_ffe(ncols, dot, H.is_real != 0))
           worst = std::max(worst, (size_t)grid_for(fe, NH, ffe_lanes(ncols)) * 2 * ncols *
                                       sizeof(double2));
+        if (KernelFn fr = select_kernel_ffr(ncols, dot, H.is_real != 0, H.max_row_nnz, H.ell_w))
+          worst = std::max(worst, (size_t)grid_for(fr, NH, 32) * 2 * ncols * sizeof(double2));
       }
     }
   }
@@ -253,13 +255,29 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     p.ell_col = H.ell_col;
     p.ell_val = H.ell_val;
     p.ell_w = H.ell_w;
-    // Automatic selection takes the padded-row kernel for real operators with
-    // 33..64 columns per launch (measured on GB300, 3D Anderson L=128, NR=64:
-    // 35.3% -> 43.5% of the HBM roofline against the CSR register-gather
-    // kernel).  Elsewhere the CSR kernel measured faster: complex Haldane
-    // 256x256, NR=16, kpm_2d 183 ms against 189 ms (exact-length last chunk);
-    // the L2-resident 2D Anderson L=64, NR=12, 7.4 ms against 8.3 ms per call
+    p.alpha_f = (float)a.alpha;
+    p.beta_mode = a.beta == 0.0 ? 0 : (a.beta > 0.0 ? 1 : -1);
+    // Automatic selection for real operators with 33..64 columns per launch:
+    // the row-streaming kernel when rows hold at most 8 nonzeros (measured on
+    // GB300, 3D Anderson L=128, NR=64: 61.6% of the HBM roofline), else the
+    // padded-row kernel (43.5%; the CSR register-gather kernel 35.3%).
+    // Elsewhere the CSR kernel measured faster: complex Haldane 256x256,
+    // NR=16, kpm_2d 183 ms against 189 ms (exact-length last chunk); the
+    // L2-resident 2D Anderson L=64, NR=12, 7.4 ms against 8.3 ms per call
     // (4 lanes x 3 columns against 16 x 1).
+    if (a.variant == 11 && precision != KPMGB_PREC_FF)
+      return fail(KPMGB_ERR_ARGUMENT, "the row-streaming kernel is float-float only");
+    if (precision == KPMGB_PREC_FF && (a.variant == 11 || a.variant == 0)) {
+      KernelFn fr = select_kernel_ffr(p.ncols, a.dot, H.is_real != 0, H.max_row_nnz, H.ell_w);
+      if (fr) {
+        KPMGB_TRY(launch_step_kernel(fr, grid_for(fr, a.NH, 32), s, p));
+        continue;
+      }
+      if (a.variant == 11)
+        return fail(KPMGB_ERR_ARGUMENT,
+                    "the row-streaming kernel serves float-float steps of real operators with "
+                    "33..64 columns and rows of 5..8 nonzeros");
+    }
     const bool auto_padded = a.variant == 0 && H.ell_w > 0 &&
                              ((H.is_real && p.ncols > 32) || padded_complex());
     if (precision == KPMGB_PREC_FF && (a.variant == 9 || auto_padded)) {
@@ -293,6 +311,9 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
   if (precision == KPMGB_PREC_FF && a0.H->ell_w > 0 &&
       select_kernel_ffe(a0.NR, a0.dot, a0.H->is_real != 0))
     cands.push_back({9, 0});
+  if (precision == KPMGB_PREC_FF &&
+      select_kernel_ffr(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz, a0.H->ell_w))
+    cands.push_back({11, 0});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   KPMGB_CUDA(cudaEventCreate(&e0));
   cudaError_t ce = cudaEventCreate(&e1);

@@ -116,6 +116,10 @@ struct KParams {
   const int* ell_col;
   const void* ell_val;
   int ell_w;
+  // alpha as a float and the sign of beta (0, 1, -1), set on the host so that
+  // the float-float kernels execute no FP64 instruction per row
+  float alpha_f;
+  int beta_mode;
 };
 
 template <int DOT>
@@ -499,8 +503,8 @@ __global__ void __launch_bounds__(kThreads, (FFTune<CPL, REALH>::min_blocks)) k_
   float4* y = static_cast<float4*>(p.y);
   const float4* __restrict__ bra = static_cast<const float4*>(p.bra);
   const HV* __restrict__ val = static_cast<const HV*>(p.val);
-  const float alpha = (float)p.alpha;
-  const int beta_mode = p.beta == 0.0 ? 0 : (p.beta > 0.0 ? 1 : -1);
+  const float alpha = p.alpha_f;
+  const int beta_mode = p.beta_mode;
 
   // FP64 dot accumulators: in registers, or (KPMGB_FF_SMEM_ACC, up to two
   // columns per lane) in a thread-private shared-memory slot, which frees
@@ -729,6 +733,10 @@ KernelFn select_kernel_ff(Shape s, int dot, bool real);
 // columns; nullptr otherwise.  ffe_lanes: lanes per row of its shape.
 KernelFn select_kernel_ffe(int ncols, int dot, bool real);
 int ffe_lanes(int ncols);
+// Row-streaming float-float kernel for real operators over padded rows of
+// stride 8 (kpmgb_step_ffe.cu): 33..64 columns (32 lanes x 2 per row), rows of
+// at most 8 nonzeros; nullptr otherwise.  Rows per block tile: 8.
+KernelFn select_kernel_ffr(int ncols, int dot, bool real, int max_row_nnz, int ell_w);
 
 }  // namespace step
 }  // namespace kpmgb

@@ -79,8 +79,8 @@ __global__ void __launch_bounds__(kThreads, KPMGB_FFE_MIN_BLOCKS) k_step_ffe(KPa
   const HV* __restrict__ eval = static_cast<const HV*>(p.ell_val);
   const int* __restrict__ ecol = p.ell_col;
   const int W = p.ell_w;
-  const float alpha = (float)p.alpha;
-  const int beta_mode = p.beta == 0.0 ? 0 : (p.beta > 0.0 ? 1 : -1);
+  const float alpha = p.alpha_f;
+  const int beta_mode = p.beta_mode;
   // gathers of this lane's columns start at x + c0 + lg (+ c * LPR)
   const float4* __restrict__ xl = x + p.c0 + lg;
 
@@ -233,6 +233,215 @@ KernelFn ffe_shape(int ncols, int dot) {
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// Row-streaming form for real operators, 33..64 columns (k_step_ffr).
+//
+// Same arithmetic as k_step_ffe with one anchored chunk per row (W <= 8 slots
+// of a stride-8 padded row), laid out so that a row's memory latencies
+// overlap instead of following one another:
+//   * the next row's column indices and values are copied into a per-warp
+//     shared-memory buffer with cp.async while the current row is computed
+//     (the index loads leave the row's dependent chain);
+//   * the row's z values, its own x values (for the dots) and the gathers of
+//     both columns are all issued before the first product: 2W + 4 loads of
+//     16 bytes per lane in flight;
+//   * 2 blocks per SM (up to 128 registers) hold those loads without spills.
+// Measured on GB300, 3D Anderson L=128, NR=64 (one step launch):
+// 1.62 ms (61.6% of the measured HBM bandwidth) against 2.20 ms for
+// k_step_ffe; the recurrence vectors agree with k_step_ffe's to 4e-15
+// (different anchors per row, each exact to the float-float rounding).
+//
+// Doubling dots: <x|x> and Re<x|y> only.  The doubling identities hold for
+// Hermitian H only (src/moment.jl:420-492), and then <x|y> =
+// <psi|T_{n-1}(H) T_n(H)|psi> is real: its imaginary part is stored as 0.
+template <int W, int DOT, bool FULL>
+__global__ void __launch_bounds__(kThreads, 2) k_step_ffr(KParams p) {
+  pdl_enter();
+  constexpr int GROUPS = kThreads / 32;  // rows per block tile
+  constexpr int CPL = 2;
+  constexpr int ND = NDots<DOT>::value;
+  constexpr int NDA = ND > 0 ? ND : 1;
+  constexpr int kStride = 8;  // padded row stride (ints / float2 values)
+  const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const float4* __restrict__ x = static_cast<const float4*>(p.x);
+  const float4* z = static_cast<const float4*>(p.z);
+  float4* y = static_cast<float4*>(p.y);
+  const float4* __restrict__ bra = static_cast<const float4*>(p.bra);
+  const int* __restrict__ ecol = p.ell_col;
+  const float2* __restrict__ eval = static_cast<const float2*>(p.ell_val);
+  const float alpha = p.alpha_f;
+  const int beta_mode = p.beta_mode;
+  const int ld = p.ld;
+  bool live[CPL];
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) live[c] = FULL || lane + 32 * c < p.ncols;
+
+  __shared__ double2 sacc[kThreads][NDA * CPL];
+  // per warp, two buffers of one padded row: 8 column indices, 8 values
+  __shared__ __align__(16) int sidx[GROUPS][2][3 * kStride];
+  float dS[NDA][CPL][2], dC[NDA][CPL][2];
+#pragma unroll
+  for (int k = 0; k < NDA; ++k)
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      sacc[threadIdx.x][k * CPL + c] = make_double2(0.0, 0.0);
+      dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
+    }
+  int rows_since_flush = 0;
+
+  // lanes 0..5 copy the 96 bytes of one padded row (2 x 16 B of indices,
+  // 4 x 16 B of values) into buffer b
+  auto stage = [&](int64_t r, int b) {
+    if (lane < 6) {
+      const char* src = lane < 2 ? reinterpret_cast<const char*>(ecol + r * kStride) + lane * 16
+                                 : reinterpret_cast<const char*>(eval + r * kStride) + (lane - 2) * 16;
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(&sidx[g][b][lane * 4]);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+  int buf = 0;
+  {
+    const int64_t r0 = (int64_t)blockIdx.x * GROUPS + g;
+    if ((int64_t)blockIdx.x < ntiles && r0 < p.NH) stage(r0, 0);
+    else asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t r = t * GROUPS + g;
+    if (r >= p.NH) continue;
+    {
+      const int64_t rn = r + (int64_t)gridDim.x * GROUPS;
+      if (t + gridDim.x < ntiles && rn < p.NH) stage(rn, buf ^ 1);
+      else asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncwarp();
+    const int* jrow = &sidx[g][buf][0];
+    const float4* hrow = reinterpret_cast<const float4*>(&sidx[g][buf][kStride]);
+    const int64_t base = r * ld + p.c0;
+    // every load of the row, before any arithmetic
+    float4 zv[CPL], xo[CPL], bo[CPL], xv[CPL][W];
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int64_t e = base + lane + 32 * c;
+      const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+      zv[c] = live[c] && beta_mode != 0 ? __ldcs(z + e) : zero;
+      xo[c] = live[c] && (DOT == DOT_DOUBLING || DOT == DOT_LR2) ? __ldg(x + e) : zero;
+      bo[c] = live[c] && (DOT == DOT_LR2 || DOT == DOT_LR1) ? __ldg(bra + e) : zero;
+    }
+    {
+      const int4 j0 = reinterpret_cast<const int4*>(jrow)[0];
+      const int4 j1 = reinterpret_cast<const int4*>(jrow)[1];
+      const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+#pragma unroll
+      for (int c = 0; c < CPL; ++c)
+#pragma unroll
+        for (int u = 0; u < W; ++u)
+          xv[c][u] = live[c] ? __ldg(x + (int64_t)jj[u] * ld + p.c0 + lane + 32 * c)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float2 hv[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 v = hrow[q];
+      hv[2 * q] = make_float2(v.x, v.y);
+      hv[2 * q + 1] = make_float2(v.z, v.w);
+    }
+    __syncwarp();  // the buffer is restaged two rows later
+    buf ^= 1;
+    float R = 0.f;
+#pragma unroll
+    for (int u = 0; u < W; ++u) R = __fadd_rn(R, fabsf(hv[u].x));
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      if (!live[c]) continue;
+      float M = 0.f;
+#pragma unroll
+      for (int u = 0; u < W; ++u) M = fmaxf(M, fmaxf(fabsf(xv[c][u].x), fabsf(xv[c][u].z)));
+      // anchor 1.5 * 2^E with 2^E = 4P, P <= R*M (1 + tiny) < 2P: every
+      // partial sum of the row stays inside the accumulator's binade
+      const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+      const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+      float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+      for (int u = 0; u < W; ++u) ffmac(Ar, cr, Ai, ci, hv[u], xv[c][u]);
+      const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+      const float2 yr = ff_epilogue(sr, cr, alpha, beta_mode, zv[c].x, zv[c].y);
+      const float2 yi = ff_epilogue(si, ci, alpha, beta_mode, zv[c].z, zv[c].w);
+      const float4 yv = make_float4(yr.x, yr.y, yi.x, yi.y);
+      __stcs(y + base + lane + 32 * c, yv);
+      if constexpr (DOT == DOT_DOUBLING) {
+        ffnorm2(dS[0][c], dC[0][c], xo[c]);
+        ff::dacc(dS[1][c][0], dC[1][c][0], xo[c].x, xo[c].y, yv.x, yv.y);
+        ff::dacc(dS[1][c][0], dC[1][c][0], xo[c].z, xo[c].w, yv.z, yv.w);
+      } else if constexpr (DOT == DOT_LR2) {
+        ffdot(dS[0][c], dC[0][c], bo[c], xo[c]);
+        ffdot(dS[1][c], dC[1][c], bo[c], yv);
+      } else if constexpr (DOT == DOT_LR1) {
+        ffdot(dS[0][c], dC[0][c], bo[c], yv);
+      }
+    }
+    if constexpr (ND > 0) {
+      if (++rows_since_flush == kFlushRows) {
+        rows_since_flush = 0;
+#pragma unroll
+        for (int k = 0; k < ND; ++k)
+#pragma unroll
+          for (int c = 0; c < CPL; ++c) {
+            double2 v = sacc[threadIdx.x][k * CPL + c];
+            v.x += ff::join(dS[k][c][0], dC[k][c][0]);
+            if (!(DOT == DOT_DOUBLING && k == 1)) v.y += ff::join(dS[k][c][1], dC[k][c][1]);
+            sacc[threadIdx.x][k * CPL + c] = v;
+            dS[k][c][0] = dS[k][c][1] = dC[k][c][0] = dC[k][c][1] = 0.f;
+          }
+      }
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if constexpr (ND > 0) {
+    double2 d[NDA][CPL];
+#pragma unroll
+    for (int k = 0; k < ND; ++k)
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        d[k][c] = sacc[threadIdx.x][k * CPL + c];
+        d[k][c].x += ff::join(dS[k][c][0], dC[k][c][0]);
+        if (!(DOT == DOT_DOUBLING && k == 1)) d[k][c].y += ff::join(dS[k][c][1], dC[k][c][1]);
+      }
+    reduce_finalize<ND, 32, CPL>(d, p);
+  }
+}
+
+namespace {
+
+template <int W, bool FULL>
+KernelFn ffr_dot(int dot) {
+  switch (dot) {
+    case DOT_DOUBLING: return k_step_ffr<W, DOT_DOUBLING, FULL>;
+    case DOT_LR2: return k_step_ffr<W, DOT_LR2, FULL>;
+    case DOT_LR1: return k_step_ffr<W, DOT_LR1, FULL>;
+    default: return k_step_ffr<W, DOT_NONE, FULL>;
+  }
+}
+
+template <int W>
+KernelFn ffr_full(int ncols, int dot) {
+  return ncols == 64 ? ffr_dot<W, true>(dot) : ffr_dot<W, false>(dot);
+}
+
+}  // namespace
+
+KernelFn select_kernel_ffr(int ncols, int dot, bool real, int max_row_nnz, int ell_w) {
+  if (!real || ell_w != 8 || ncols < 33 || ncols > 64 || max_row_nnz > 8) return nullptr;
+  switch (max_row_nnz) {
+    case 5: return ffr_full<5>(ncols, dot);
+    case 6: return ffr_full<6>(ncols, dot);
+    case 7: return ffr_full<7>(ncols, dot);
+    default: return ffr_full<8>(ncols, dot);
+  }
+}
 
 // 5..64 columns: 8 or 16 lanes per row with one column each up to 8 and 16
 // columns, 32 lanes with one or two columns each above.  For real operators

@@ -20,8 +20,9 @@ module KPMGB300
 using KPM
 using LinearAlgebra
 using SparseArrays
+import ChainRulesCore
 
-export GB300CSR
+export GB300CSR, dos_moments_ad, cond_moments_ad, kubo_bastin_cond_ad
 
 const libkpmgb = get(ENV, "KPMGB_LIB", joinpath(@__DIR__, "..", "kpm_gb300", "_lib", "libkpmgb.so"))
 
@@ -190,17 +191,19 @@ function KPM.kpm_3d!(H::GB300CSR, Jα, Jβ, Jγ, NC::Int64, NR::Int64, NH::Int64
     return nothing
 end
 
-# DOS reconstruction on the device (src/applications/dos.jl:76-161, dE_order = 0)
+# DOS reconstruction on the device (src/applications/dos.jl:76-161), or its
+# dE_order-th energy derivative (dos.jl:128-139; exact Taylor-series arithmetic
+# on the device where the reference nests ForwardDiff), dE_order = 0..4.
 function dos_gpu(μ::AbstractVector, a::Real, E_grid::AbstractVector; b::Real = 0.0,
-                 kernel = KPM.JacksonKernel, NC::Int64 = length(μ))
+                 kernel = KPM.JacksonKernel, NC::Int64 = length(μ), dE_order::Integer = 0)
     NC = min(NC, length(μ))
     g = Float64[kernel(n, NC) for n = 0:(NC-1)]
     ρ = Vector{Float64}(undef, length(E_grid))
-    _check(ccall((:kpmgb_dos, libkpmgb), Cint,
+    _check(ccall((:kpmgb_dos_derivative, libkpmgb), Cint,
                  (Ptr{Float64}, Int64, Float64, Float64, Ptr{Float64}, Ptr{Float64}, Int64,
-                  Ptr{Float64}),
+                  Int32, Ptr{Float64}),
                  Vector{Float64}(real.(μ[1:NC])), NC, a, b, g, Vector{Float64}(E_grid),
-                 length(E_grid), ρ))
+                 length(E_grid), Int32(dE_order), ρ))
     return ρ
 end
 
@@ -274,6 +277,130 @@ function kpm_2d_derivative(H::SparseMatrixCSC, dH, Jα, dJα, Jβ, dJβ, NC::Int
     dμ = Matrix{ComplexF64}(undef, NC, NC)
     KPM.kpm_2d!(Haug, Aaug, Baug, NC, NR, 2NH, dμ, [psi_in_l; z], [psi_in_r; z]; kwargs...)
     return dμ ./ s
+end
+
+# ---------------------------------------------------------------------------
+# Reverse-mode differentiation (no reference counterpart: KPM.jl pushes
+# ForwardDiff duals through its recurrences).  The pullbacks call the adjoint
+# Chebyshev recurrences of libkpmgb; a cotangent X̄ of a complex array X obeys
+# dL = real(dot(X̄, dX)), the ChainRulesCore convention, which is also the
+# library's (gradient entry k = dL/dRe(X_k) + i dL/dIm(X_k)).
+
+"""
+    kubo_bastin_weights(NC, a, Ef; b, NH, area, beta, kernel, quad_N, edge_cutoff)
+
+NC × NC complex W with `kubo_bastin_cond(μ, a, Ef; ...) == real(sum(W .* μ))`
+(src/applications/conductivity.jl:101-157 as a linear map, computed on the GPU).
+"""
+function kubo_bastin_weights(NC::Int64, a::Real, Ef::Real; b::Real = 0.0, NH::Integer,
+                             area::Real, beta::Real = Inf, kernel = KPM.JacksonKernel,
+                             quad_N::Int64 = 8 * NC, edge_cutoff::Real = 1e-3)
+    g = Float64[kernel(n, NC) for n = 0:(NC-1)]
+    W = Matrix{ComplexF64}(undef, NC, NC)
+    _check(ccall((:kpmgb_kubo_bastin_weights, libkpmgb), Cint,
+                 (Int64, Float64, Float64, Float64, Int64, Float64, Float64, Ptr{Float64}, Int64,
+                  Float64, Ptr{ComplexF64}),
+                 NC, a, b, Ef, NH, area, beta, g, quad_N, edge_cutoff, W))
+    return W
+end
+
+"""
+    kpm_2d_grad(H, Jα, Jβ, NC, G, psi_in_l, psi_in_r; moment_parity = :NONE)
+
+Gradients (SparseMatrixCSC on each operator's pattern) of
+F = real(sum(G .* μ)) with μ = kpm_2d(H, Jα, Jβ, NC, NR, NH; psi_in_l, psi_in_r).
+"""
+function kpm_2d_grad(H::SparseMatrixCSC, Jα::SparseMatrixCSC, Jβ::SparseMatrixCSC, NC::Int64,
+                     G::AbstractMatrix, psi_in_l::AbstractMatrix, psi_in_r::AbstractMatrix;
+                     moment_parity::Symbol = :NONE)
+    ops = map(M -> SparseMatrixCSC{ComplexF64,Int64}(M), (H, Jα, Jβ))
+    Hg, Ag, Bg = map(GB300CSR, ops)
+    BHg = GB300CSR(SparseMatrixCSC{ComplexF64,Int64}(sparse(Jβ')))
+    NH, NR = size(psi_in_r)
+    outs = map(M -> Vector{ComplexF64}(undef, nnz(M)), ops)
+    _check(ccall((:kpmgb_kpm2d_grad, libkpmgb), Cint,
+                 (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int64, Int64, Int64,
+                  Ptr{ComplexF64}, Ptr{ComplexF64}, Ptr{ComplexF64}, Int32, Ptr{ComplexF64},
+                  Ptr{ComplexF64}, Ptr{ComplexF64}),
+                 Hg.handle, Ag.handle, Bg.handle, BHg.handle, NC, NR, NH,
+                 Matrix{ComplexF64}(psi_in_l), Matrix{ComplexF64}(psi_in_r),
+                 Matrix{ComplexF64}(G), _parity(moment_parity), outs[1], outs[2], outs[3]))
+    return map((M, g) -> SparseMatrixCSC(size(M, 1), size(M, 2), copy(M.colptr), copy(M.rowval), g),
+               ops, outs)
+end
+
+"""
+    dos_moments_ad(H, NC, psi_in)
+
+Probe-averaged real kpm_1d moments of the (rescaled) sparse H, differentiable
+with respect to H's stored entries through `ChainRulesCore.rrule`.
+"""
+function dos_moments_ad(H::SparseMatrixCSC, NC::Int64, psi_in::AbstractMatrix)
+    NH, NR = size(psi_in)
+    mu = Matrix{ComplexF64}(undef, NR, NC)
+    KPM.kpm_1d!(GB300CSR(H), NC, NR, NH, mu, psi_in)
+    return vec(real.(sum(mu; dims = 1))) ./ NR
+end
+
+function ChainRulesCore.rrule(::typeof(dos_moments_ad), H::SparseMatrixCSC, NC::Int64,
+                              psi_in::AbstractMatrix)
+    μ = dos_moments_ad(H, NC, psi_in)
+    function dos_moments_pullback(μ̄)
+        H̄ = kpm_1d_grad(H, NC, psi_in, Vector{Float64}(ChainRulesCore.unthunk(μ̄)))
+        return (ChainRulesCore.NoTangent(), H̄, ChainRulesCore.NoTangent(),
+                ChainRulesCore.NoTangent())
+    end
+    return μ, dos_moments_pullback
+end
+
+"""
+    cond_moments_ad(H, Jα, Jβ, NC, psi_in_l, psi_in_r)
+
+The NC × NC kpm_2d moment matrix, differentiable with respect to the stored
+entries of H, Jα and Jβ through `ChainRulesCore.rrule`.
+"""
+function cond_moments_ad(H::SparseMatrixCSC, Jα::SparseMatrixCSC, Jβ::SparseMatrixCSC,
+                         NC::Int64, psi_in_l::AbstractMatrix, psi_in_r::AbstractMatrix)
+    NH, NR = size(psi_in_r)
+    μ = Matrix{ComplexF64}(undef, NC, NC)
+    KPM.kpm_2d!(GB300CSR(H), Jα, Jβ, NC, NR, NH, μ, psi_in_l, psi_in_r)
+    return μ
+end
+
+function ChainRulesCore.rrule(::typeof(cond_moments_ad), H::SparseMatrixCSC,
+                              Jα::SparseMatrixCSC, Jβ::SparseMatrixCSC, NC::Int64,
+                              psi_in_l::AbstractMatrix, psi_in_r::AbstractMatrix)
+    μ = cond_moments_ad(H, Jα, Jβ, NC, psi_in_l, psi_in_r)
+    function cond_moments_pullback(μ̄)
+        # dL = real(dot(μ̄, dμ)) = real(sum(conj(μ̄) .* dμ)): G = conj(μ̄)
+        G = conj.(Matrix{ComplexF64}(ChainRulesCore.unthunk(μ̄)))
+        H̄, J̄α, J̄β = kpm_2d_grad(H, Jα, Jβ, NC, G, psi_in_l, psi_in_r)
+        return (ChainRulesCore.NoTangent(), H̄, J̄α, J̄β, ChainRulesCore.NoTangent(),
+                ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
+    end
+    return μ, cond_moments_pullback
+end
+
+"""
+    kubo_bastin_cond_ad(μ, a, Ef; b, NH, area, kwargs...)
+
+sigma(Ef) from the moment matrix (src/applications/conductivity.jl:101-157),
+differentiable with respect to μ through `ChainRulesCore.rrule`; chained with
+`cond_moments_ad` it gives d sigma / d(H, Jα, Jβ) by reverse mode.
+"""
+function kubo_bastin_cond_ad(μ::AbstractMatrix, a::Real, Ef::Real; b::Real = 0.0,
+                             NH::Integer, area::Real, kwargs...)
+    return only(kubo_bastin_cond_gpu(μ, a, [Ef]; b = b, NH = NH, area = area, kwargs...))
+end
+
+function ChainRulesCore.rrule(::typeof(kubo_bastin_cond_ad), μ::AbstractMatrix, a::Real,
+                              Ef::Real; b::Real = 0.0, NH::Integer, area::Real, kwargs...)
+    σ = kubo_bastin_cond_ad(μ, a, Ef; b = b, NH = NH, area = area, kwargs...)
+    W = kubo_bastin_weights(size(μ, 1), a, Ef; b = b, NH = NH, area = area, kwargs...)
+    # σ = real(sum(W .* μ)) = real(dot(conj(W), μ)): μ̄ = σ̄ conj(W)
+    kubo_pullback(σ̄) = (ChainRulesCore.NoTangent(), ChainRulesCore.unthunk(σ̄) .* conj.(W),
+                        ChainRulesCore.NoTangent(), ChainRulesCore.NoTangent())
+    return σ, kubo_pullback
 end
 
 end # module

@@ -37,10 +37,16 @@ EXPORTED_SYMBOLS = (
     "kpmgb_kpm1d_grad",
     "kpmgb_kubo_bastin",
     "kpmgb_dos",
+    "kpmgb_dos_derivative",
+    "kpmgb_kubo_bastin_weights",
+    "kpmgb_kpm2d_grad",
     "kpmgb_chebyshev_action",
     "kpmgb_kpm1d_current",
     "kpmgb_kpm3d",
     "kpmgb_selftest_wait_expiry",
+    "kpmgb_timing_enable",
+    "kpmgb_timing_read",
+    "kpmgb_measure_fp64_peak",
 )
 
 
@@ -101,8 +107,14 @@ def _declare(lib):
     lib.kpmgb_kpm3d.argtypes = [vp, vp, vp, vp, i64, i64, i64, vp, vp, vp, C.POINTER(Kpm2dOptions)]
     lib.kpmgb_chebyshev_action.argtypes = [vp, i64, i64, vp, i64, i64, vp, i64, vp]
     lib.kpmgb_dos.argtypes = [vp, i64, f64, f64, vp, vp, i64, vp]
+    lib.kpmgb_dos_derivative.argtypes = [vp, i64, f64, f64, vp, vp, i64, i32, vp]
+    lib.kpmgb_kubo_bastin_weights.argtypes = [i64, f64, f64, f64, i64, f64, f64, vp, i64, f64, vp]
+    lib.kpmgb_kpm2d_grad.argtypes = [vp, vp, vp, vp, i64, i64, i64, vp, vp, vp, i32, vp, vp, vp]
     lib.kpmgb_kpm1d_grad.argtypes = [vp, i64, i64, i64, vp, vp, i64, vp]
     lib.kpmgb_kpm1d_noalloc.argtypes = [i64, vp, vp, vp, i64, i64, vp, vp, vp]
+    lib.kpmgb_timing_enable.argtypes = [i32]
+    lib.kpmgb_timing_read.argtypes = [i32, dp, C.POINTER(i64)]
+    lib.kpmgb_measure_fp64_peak.argtypes = [dp]
     for name in EXPORTED_SYMBOLS:
         if name not in ("kpmgb_version", "kpmgb_last_error", "kpmgb_kernel_launch_count"):
             getattr(lib, name).restype = C.c_int
@@ -146,3 +158,26 @@ def version() -> str:
 
 def kernel_launch_count() -> int:
     return int(load().kpmgb_kernel_launch_count())
+
+
+TIMED = {"contract_split": 0, "contract_fp64": 1}
+
+
+def timing_enable(on: bool) -> None:
+    """Bracket the instrumented kernels' launches with CUDA events (or stop)."""
+    check(load().kpmgb_timing_enable(1 if on else 0))
+
+
+def timing_read(kernel: str):
+    """(summed device ms, launches) of one instrumented kernel since the last
+    read; waits for the recorded events."""
+    ms, n = C.c_double(0.0), C.c_int64(0)
+    check(load().kpmgb_timing_read(TIMED[kernel], C.byref(ms), C.byref(n)))
+    return ms.value, n.value
+
+
+def measure_fp64_peak() -> float:
+    """Measured FP64 FMA rate of the current device, TFLOP/s."""
+    t = C.c_double(0.0)
+    check(load().kpmgb_measure_fp64_peak(C.byref(t)))
+    return t.value

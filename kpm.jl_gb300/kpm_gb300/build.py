@@ -35,6 +35,8 @@ SOURCES = [
     "kpmgb_adjoint.cu",
     "kpmgb_recon.cu",
     "kpmgb_action.cu",
+    "kpmgb_timing.cu",
+    "kpmgb_tune.cu",
 ]
 
 

@@ -252,6 +252,34 @@ def kubo_bastin_cond(mu2D, a: float, Ef, *, b: float = 0.0, NH: int, area: float
     return float(out[0]) if scalar else out
 
 
+def kubo_bastin_weights(NC: int, a: float, Ef: float, *, b: float = 0.0, NH: int, area: float,
+                        beta: float = math.inf, kernel=jackson_kernel, quad_N: int | None = None,
+                        edge_cutoff: float = 1e-3) -> np.ndarray:
+    """W (NC, NC) complex with ``kubo_bastin_cond(mu, a, Ef; ...) ==
+    Re sum_{n,m} W[n,m] mu[n,m]``: the Kubo-Bastin reconstruction
+    (``src/applications/conductivity.jl:101-157``) as a linear functional of
+    the moments, i.e. d sigma / d mu, computed on the GPU.  Feed it (times
+    dL/dsigma) to :func:`kpm_2d_grad`."""
+    import ctypes as C  # noqa: F401
+    from . import _native
+    if not a > 0:
+        raise KPMArgumentError("kubo_bastin_cond: a must be positive.")
+    if not area > 0:
+        raise KPMArgumentError("kubo_bastin_cond: area must be positive.")
+    if not NH > 0:
+        raise KPMArgumentError("kubo_bastin_cond: NH must be positive.")
+    NC = int(NC)
+    quad_N = 8 * NC if quad_N is None else int(quad_N)
+    g = _damping(kernel, NC)
+    W = np.empty((NC, NC), dtype=np.complex128, order="F")
+    lib = _native.load()
+    _native.check(lib.kpmgb_kubo_bastin_weights(NC, float(a), float(b), float(Ef), int(NH),
+                                                float(area), float(beta),
+                                                g.ctypes.data if g is not None else None,
+                                                quad_N, float(edge_cutoff), W.ctypes.data))
+    return W
+
+
 def dos(mu_or_H, H_rescale_factor=None, *, b: float = 0.0, E_grid=None, N_tilde: int = 0,
         E_range=None, NC: int = 0, NR: int = 12, kernel=jackson_kernel, dE_order: int = 0,
         fix_normalization: float = 0.0, center: bool = False, rng=None):
@@ -281,8 +309,8 @@ def dos(mu_or_H, H_rescale_factor=None, *, b: float = 0.0, E_grid=None, N_tilde:
     a = float(H_rescale_factor)
     if not a > 0:
         raise KPMArgumentError("the rescale factor must be positive")
-    if dE_order != 0:
-        raise KPMArgumentError("dos: only dE_order = 0 is implemented by the GPU reconstruction")
+    if not 0 <= int(dE_order) <= 4:
+        raise KPMArgumentError("dos: dE_order must be in 0..4")
     NC = len(mu) if NC == 0 else min(int(NC), len(mu))
     if E_grid is None:
         N_tilde = NC * 2 if N_tilde == 0 else N_tilde
@@ -299,7 +327,30 @@ def dos(mu_or_H, H_rescale_factor=None, *, b: float = 0.0, E_grid=None, N_tilde:
     g = _damping(kernel, NC)
     rho = np.empty(E.size, dtype=np.float64)
     lib = _native.load()
-    _native.check(lib.kpmgb_dos(m.ctypes.data, NC, a, float(b),
-                                g.ctypes.data if g is not None else None, E.ctypes.data, E.size,
-                                rho.ctypes.data))
+    _native.check(lib.kpmgb_dos_derivative(m.ctypes.data, NC, a, float(b),
+                                           g.ctypes.data if g is not None else None,
+                                           E.ctypes.data, E.size, int(dE_order),
+                                           rho.ctypes.data))
     return E, rho
+
+
+def dos0(mu, H_rescale_factor, *, NC: int = 0, kernel=jackson_kernel, dE_order: int = 0):
+    """DOS (``dE_order=0``) or its second energy derivative (``dE_order=2``) at
+    the centre of the rescaling, x = 0, from the closed-form values
+    T_n(0) = 1, -1, 0 for n = 0, 2, odd (mod 4) and
+    d^2/dx^2 [T_n(x)/sqrt(1-x^2)]_{x=0} = (-1)^{n/2} (1 - n^2) for even n
+    (``src/applications/dos.jl:166-200``)."""
+    a = float(H_rescale_factor)
+    if not a > 0:
+        raise KPMArgumentError("the rescale factor must be positive")
+    mu = np.asarray(mu)
+    NC = len(mu) if NC == 0 else min(int(NC), len(mu))
+    n0 = np.arange(0, NC, 4)
+    n2 = np.arange(2, NC, 4)
+    w0 = np.real(mu[n0]) * np.where(n0 != 0, 2.0, 1.0) * kernel(n0, NC)
+    w2 = np.real(mu[n2]) * 2.0 * kernel(n2, NC)
+    if dE_order == 0:
+        return float((w0.sum() - w2.sum()) / (a * np.pi))
+    if dE_order == 2:
+        return float(((w0 * (1 - n0 ** 2.0)).sum() + (w2 * (n2 ** 2.0 - 1)).sum()) / (a ** 3 * np.pi))
+    raise KPMArgumentError(f"unimplemented for derivative of order {dE_order}.")

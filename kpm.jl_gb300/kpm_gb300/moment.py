@@ -55,7 +55,8 @@ def _colmajor(psi, NH, NR, name):
     return np.asfortranarray(a, dtype=np.complex128)
 
 
-_VARIANT = {"auto": 0, "gather": 1, "tune": 4, "single": 6, "padded": 9, "cluster": 10}
+_VARIANT = {"auto": 0, "gather": 1, "tune": 4, "single": 6, "padded": 9, "cluster": 10,
+            "streaming": 11}
 
 
 def _opts1d(precision, stability_check, kernel="auto", use_graph=False):
@@ -112,7 +113,8 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
     ``kernel_variant``): ``"auto"`` (one thread-block-cluster launch per call
     for small operators, else per-step launches of the padded-row kernel for
     real operators with 33..64 columns or of the register-gather kernel),
-    ``"gather"``, ``"padded"``, ``"cluster"``, ``"single"``, ``"tune"``.
+    ``"gather"``, ``"padded"``, ``"streaming"``, ``"cluster"``, ``"single"``,
+    ``"tune"``.
     ``use_graph`` replays the per-step launches from a CUDA graph.  With
     ``NR_parallel=False`` the columns run one call each, with the same
     options.
@@ -483,7 +485,8 @@ class EnsembleOperator:
         return len(self.sizes)
 
 
-def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: bool = True):
+def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: bool = True,
+                    kernel: str = "auto"):
     """Doubling moments of many independent members in one persistent launch.
 
     ``Hs``: list of (rescaled) sparse operators of any sizes, or an
@@ -492,7 +495,11 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     Equivalent to
     ``[kpm_1d(H_i, NC, NR, psi_in=psi_i) for ...]`` (``src/moment.jl:339-492``
     per member).  Returns a list of length-NC real averages, or of (NR, NC)
-    matrices with ``avg_output=False``.
+    matrices with ``avg_output=False``.  ``kernel="tune"`` picks the launch
+    shape (threads per CTA; CSR or padded float-float rows) by timing the
+    candidates once per ensemble shape and device, and keeps the choice in the
+    persistent autotuning cache (``KPMGB_TUNE_CACHE``, default
+    ``~/.cache/kpmgb/tune.txt``).
     """
     ens = Hs if isinstance(Hs, EnsembleOperator) else None
     if ens is None:
@@ -514,7 +521,9 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     op, seg = ens.op, ens.seg
     psi = np.asfortranarray(np.vstack([np.asarray(p, dtype=np.complex128) for p in psis]))
     out = np.empty((len(sizes), NC, NR), dtype=np.complex128)
-    opts = _opts1d(precision, False)
+    if kernel not in ("auto", "tune"):
+        raise KPMArgumentError("kernel must be 'auto' or 'tune' for the ensemble")
+    opts = _opts1d(precision, False, kernel)
     lib = _native.load()
     rc = lib.kpmgb_kpm1d_ensemble(op.handle, len(sizes), seg.ctypes.data, NC, NR, psi.ctypes.data,
                                   out.ctypes.data, C.byref(opts))
@@ -555,6 +564,56 @@ def kpm_1d_grad(H, NC: int, psi_in, g, *, checkpoint_every: int = 0):
                               int(checkpoint_every), out.ctypes.data)
     _native.check(rc)
     return sp.csc_matrix((out, op.indices, op.indptr), shape=op.shape)
+
+
+def kpm_2d_grad(H, Ja, Jb, NC: int, G, NR: int | None = None, NH: int | None = None, *,
+                psi_in=None, psi_in_l=None, psi_in_r=None, moment_parity: str = "NONE",
+                Jb_adjoint=None):
+    """Gradient of ``F = Re sum_{n,m} G[n,m] mu[n,m]`` with respect to the
+    stored entries of H, Ja and Jb, for the kpm_2d moments
+    ``mu = kpm_2d(H, Ja, Jb, NC, NR, NH; psi_in_l, psi_in_r, moment_parity)``
+    (``src/moment.jl:812-1088``).
+
+    ``G`` (NC, NC) complex: dF/dmu, e.g. :func:`kubo_bastin_weights` for a
+    loss on sigma(Ef).  Returns ``(gH, gJa, gJb)``: CSC matrices on each
+    operator's pattern whose stored value k is dF/dRe(X_k) + i dF/dIm(X_k).
+    Runs the adjoint Chebyshev recurrences of both chains on the GPU (FP64),
+    keeping every forward vector of a batch of 32 probe columns resident.
+    ``Jb_adjoint``: Jb^dagger as a matrix or operator (built from ``Jb`` when
+    that is a SciPy matrix).  No reference counterpart: KPM.jl obtains such
+    derivatives by ForwardDiff duals.
+    """
+    import scipy.sparse as sp
+    if moment_parity not in _native.PARITY:
+        raise KPMArgumentError(f"moment_parity={moment_parity} not understood.")
+    if Jb_adjoint is None:
+        if isinstance(Jb, GB300Operator):
+            raise KPMArgumentError("Jb_adjoint is required when Jb is a GB300Operator")
+        Jb_adjoint = sp.csc_matrix(Jb, dtype=np.complex128).conj().T.tocsc()
+    op, oa, ob, obh = (as_operator(M) for M in (H, Ja, Jb, Jb_adjoint))
+    NH = op.shape[0] if NH is None else int(NH)
+    if psi_in is not None:
+        if psi_in_l is not None or psi_in_r is not None:
+            raise KPMArgumentError(
+                "must either set `psi_in` or set `psi_in_l` and `psi_in_r`, but not both.")
+        psi_in_l = psi_in_r = psi_in
+    if psi_in_l is None or psi_in_r is None:
+        raise KPMArgumentError("probe vectors are required (psi_in, or psi_in_l and psi_in_r)")
+    NR = np.asarray(psi_in_r).shape[1] if NR is None else int(NR)
+    pl = _colmajor(psi_in_l, NH, NR, "psi_in_l")
+    pr = _colmajor(psi_in_r, NH, NR, "psi_in_r")
+    Gm = np.asfortranarray(G, dtype=np.complex128)
+    if Gm.shape != (int(NC), int(NC)):
+        raise KPMArgumentError(f"G must be ({NC}, {NC}) (got {Gm.shape})")
+    outs = [np.empty(o.nnz, dtype=np.complex128) for o in (op, oa, ob)]
+    lib = _native.load()
+    rc = lib.kpmgb_kpm2d_grad(op.handle, oa.handle, ob.handle, obh.handle, int(NC), NR, NH,
+                              pl.ctypes.data, pr.ctypes.data, Gm.ctypes.data,
+                              _native.PARITY[moment_parity], outs[0].ctypes.data,
+                              outs[1].ctypes.data, outs[2].ctypes.data)
+    _native.check(rc)
+    return tuple(sp.csc_matrix((g, o.indices, o.indptr), shape=o.shape)
+                 for g, o in zip(outs, (op, oa, ob)))
 
 
 def chebyshev_action_bang(out, Hn, V, C, *, check_every: int = 16, verbose: int = 0) -> None:

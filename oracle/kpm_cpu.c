@@ -48,15 +48,29 @@ static void csc_mul5(int64_t n, const int64_t* colptr, const int64_t* rowval, co
   }
 }
 
-/* dot(a, b) = sum conj(a) * b */
-static cplx zdotc(int64_t n, const cplx* a, const cplx* b) {
-  double sr = 0.0, si = 0.0;
+/* dot(a, b) = sum conj(a) * b.  The reference calls LinearAlgebra.dot, i.e.
+ * BLAS zdotc, whose kernels keep several independent partial sums; this
+ * restatement sums blocks of 256 terms with 4 interleaved accumulators and
+ * combines the block sums pairwise, so its rounding error grows like
+ * log(n) rather than n (a plain serial loop drifts by ~1e-12 relative over
+ * the 4096 moments of a 2M-row operator). */
+static cplx zdotc_block(int64_t n, const cplx* a, const cplx* b) {
+  double sr[4] = {0.0, 0.0, 0.0, 0.0}, si[4] = {0.0, 0.0, 0.0, 0.0};
   for (int64_t i = 0; i < n; ++i) {
-    sr += a[i].re * b[i].re + a[i].im * b[i].im;
-    si += a[i].re * b[i].im - a[i].im * b[i].re;
+    const int q = (int)(i & 3);
+    sr[q] += a[i].re * b[i].re + a[i].im * b[i].im;
+    si[q] += a[i].re * b[i].im - a[i].im * b[i].re;
   }
-  cplx r = {sr, si};
+  cplx r = {(sr[0] + sr[1]) + (sr[2] + sr[3]), (si[0] + si[1]) + (si[2] + si[3])};
   return r;
+}
+
+static cplx zdotc(int64_t n, const cplx* a, const cplx* b) {
+  if (n <= 256) return zdotc_block(n, a, b);
+  const int64_t h = (n / 2 + 255) / 256 * 256;  /* split on a block boundary */
+  const cplx l = zdotc(h, a, b), r = zdotc(n - h, a + h, b + h);
+  cplx s = {l.re + r.re, l.im + r.im};
+  return s;
 }
 
 /* Equal-vector moments with the doubling trick.  Runs steps n = 2..last_n

@@ -54,8 +54,17 @@ def random_phase_vectors(rng: np.random.Generator, NH: int, NR: int) -> np.ndarr
 
 
 def columnwise_dot(A: np.ndarray, B: np.ndarray) -> np.ndarray:
-    """dot(A[:,i], B[:,i]) = sum(conj(A)*B) per column (``src/utils/vectors.jl:103-117``)."""
-    return np.einsum("ij,ij->j", A.conj(), B)
+    """dot(A[:,i], B[:,i]) = sum(conj(A)*B) per column (``src/utils/vectors.jl:103-117``).
+
+    The reference calls BLAS ``dot``; here each column's products are summed
+    along a contiguous axis, where NumPy uses pairwise summation, so the
+    rounding error grows like log(NH) as with a blocked BLAS kernel (a plain
+    running sum over NH rows drifts by ~1e-12 relative over a few hundred
+    moments)."""
+    P = np.ascontiguousarray((A.conj() * B).T)
+    if P.ndim == 1:
+        return P.sum()
+    return P.sum(axis=1)
 
 
 def cheb_step(H, Vpp: np.ndarray, Vp: np.ndarray) -> np.ndarray:
@@ -350,6 +359,87 @@ def dos(mu, a, b=0.0, E_grid=None, N_tilde=0, E_range=None, NC=0, kernel=jackson
     return E_grid, rho
 
 
+# Truncated Taylor series ("jets") f(E + h) = sum_k f[k] h^k, the arithmetic
+# that nested forward-mode derivatives perform; used to restate the
+# dE_order >= 1 branch of ``src/applications/dos.jl:128-139`` (ForwardDiff
+# through ``_dos_single``, i.e. through cos(n acos x) and a pi sqrt(1 - x^2)).
+def _jet_mul(f, g):
+    K = len(f) - 1
+    return [sum(f[j] * g[k - j] for j in range(k + 1)) for k in range(K + 1)]
+
+
+def _jet_div(f, g):
+    K = len(f) - 1
+    r = []
+    for k in range(K + 1):
+        r.append((f[k] - sum(g[j] * r[k - j] for j in range(1, k + 1))) / g[0])
+    return r
+
+
+def _jet_sqrt(u):
+    K = len(u) - 1
+    s = [np.sqrt(u[0])]
+    for k in range(1, K + 1):
+        s.append((u[k] - sum(s[j] * s[k - j] for j in range(1, k))) / (2 * s[0]))
+    return s
+
+
+def _jet_integral_from_derivative(dv, v0):
+    """v with v' = dv (jets): v[k] = dv[k-1] / k."""
+    return [v0] + [dv[k - 1] / k for k in range(1, len(dv) + 1)]
+
+
+def _jet_cos_sin(w):
+    """cos(w), sin(w) jets from c' = -s w', s' = c w'."""
+    K = len(w) - 1
+    c, s = [np.cos(w[0])], [np.sin(w[0])]
+    for k in range(1, K + 1):
+        c.append(-sum(j * w[j] * s[k - j] for j in range(1, k + 1)) / k)
+        s.append(sum(j * w[j] * c[k - j] for j in range(1, k + 1)) / k)
+    return c, s
+
+
+def dos_derivative(mu, a, b, E_grid, dE_order: int, NC=0, kernel=jackson_kernel):
+    """d^k rho/dE^k of ``dos`` at each energy (``src/applications/dos.jl:128-139``)."""
+    mu = np.asarray(mu)
+    NC = len(mu) if NC == 0 else min(NC, len(mu))
+    n = np.arange(NC)
+    mut = np.real(mu[:NC]) * kernel(n, NC) * hn(n)
+    E_grid = np.asarray(E_grid, dtype=np.float64)
+    out = np.zeros_like(E_grid)
+    K = int(dE_order)
+    for i, E in enumerate(E_grid):
+        if not abs(E - b) < a:
+            continue
+        x = [(E - b) / a, 1.0 / a] + [0.0] * (K - 1) if K >= 1 else [(E - b) / a]
+        u = _jet_mul(x, x)
+        u = [1.0 - u[0]] + [-v for v in u[1:]]
+        sq = _jet_sqrt(u)
+        # acos(x): derivative -x' / sqrt(1 - x^2)
+        dth = _jet_div([-v for v in x[1:]] + [0.0], sq)[:K] if K >= 1 else []
+        th = _jet_integral_from_derivative(dth, np.arccos(x[0]))
+        c, _ = _jet_cos_sin([n * t for t in th])          # jets of cos(n theta), vectorised in n
+        S = [float(np.dot(mut, ck)) for ck in c]
+        rho = _jet_div(S, [a * np.pi * v for v in sq])
+        out[i] = math.factorial(K) * rho[K]
+    return out
+
+
+def dos0(mu, a, NC=0, kernel=jackson_kernel, dE_order: int = 0):
+    """DOS or its second energy derivative at x = 0 from the closed forms of
+    ``src/applications/dos.jl:166-200``."""
+    mu = np.real(np.asarray(mu))
+    NC = len(mu) if NC == 0 else min(NC, len(mu))
+    n0, n2 = np.arange(0, NC, 4), np.arange(2, NC, 4)
+    t0 = mu[n0] * hn(n0) * kernel(n0, NC)
+    t2 = mu[n2] * hn(n2) * kernel(n2, NC)
+    if dE_order == 0:
+        return (t0.sum() - t2.sum()) / (a * np.pi)
+    if dE_order == 2:
+        return ((t0 * (1 - n0 ** 2.0)).sum() + (t2 * (n2 ** 2.0 - 1)).sum()) / (a ** 3 * np.pi)
+    raise ValueError(f"unimplemented for derivative of order {dE_order}.")
+
+
 def gausschebyshevt(n: int):
     """Gauss-Chebyshev (first kind) nodes cos((2k-1)pi/2n) and weights pi/n."""
     k = np.arange(n, 0, -1)
@@ -444,8 +534,18 @@ def kpm_1d_tangent(H, dH, NC: int, psi: np.ndarray) -> np.ndarray:
     """d/dt <psi_i|T_n(H + t dH)|psi_i> at t = 0, shape (NR, NC)."""
     H, dH = _csr(H), _csr(dH)
     psi = np.asarray(psi, dtype=np.complex128)
-    _, dv = _tangent_chain(H, dH, psi, np.zeros_like(psi), NC)
-    return np.stack([columnwise_dot(psi, d) for d in dv], axis=1)
+    # the dual recurrence of _tangent_chain, keeping only the last two vectors
+    out = np.zeros((psi.shape[1], NC), dtype=np.complex128)
+    v_pp, v_p = psi, H @ psi
+    dv_pp, dv_p = np.zeros_like(psi), dH @ psi
+    if NC > 1:
+        out[:, 1] = columnwise_dot(psi, dv_p)
+    for n in range(2, NC):
+        v_n = 2.0 * (H @ v_p) - v_pp
+        dv_n = 2.0 * (dH @ v_p + H @ dv_p) - dv_pp
+        out[:, n] = columnwise_dot(psi, dv_n)
+        v_pp, v_p, dv_pp, dv_p = v_p, v_n, dv_p, dv_n
+    return out
 
 
 def kpm_2d_tangent(H, dH, Ja, dJa, Jb, dJb, NC: int, psi_l, psi_r) -> np.ndarray:

@@ -76,3 +76,56 @@ def test_ensemble_operator_reuse(built_lib):
         assert np.array_equal(x, y) and np.array_equal(y, z)
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d_ensemble(ens, 48, psis[:-1])
+
+
+def test_ensemble_autotune_cache_round_trip(built_lib, tmp_path, monkeypatch):
+    """kernel="tune" times the candidate launch shapes once, writes the choice
+    to the persistent cache, and a later call (a fresh operator, as a new
+    process would build) reads it back without timing: it launches exactly as
+    many kernels as an untuned call.  Both agree with the oracle."""
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("KPMGB_TUNE_CACHE", str(cache))
+    rng = np.random.default_rng(19)
+    Hs, psis = _members(rng, 24, 6, 18)
+    ref = [ko.kpm_1d_doubling(H, 96, p) for H, p in zip(Hs, psis)]
+    for prec in ("ff", "fp64"):
+        n0 = kg.kernel_launch_count()
+        got = kg.kpm_1d_ensemble(kg.EnsembleOperator(Hs), 96, psis, precision=prec,
+                                 avg_output=False, kernel="tune")
+        n_tuned = kg.kernel_launch_count() - n0
+        lines = [l for l in cache.read_text().splitlines() if l.startswith("ensemble|")]
+        assert any(f"|prec={1 if prec == 'ff' else 0}" in l for l in lines)
+        n0 = kg.kernel_launch_count()
+        again = kg.kpm_1d_ensemble(kg.EnsembleOperator(Hs), 96, psis, precision=prec,
+                                   avg_output=False, kernel="tune")
+        n_cached = kg.kernel_launch_count() - n0
+        n0 = kg.kernel_launch_count()
+        kg.kpm_1d_ensemble(kg.EnsembleOperator(Hs), 96, psis, precision=prec, avg_output=False)
+        n_plain = kg.kernel_launch_count() - n0
+        assert n_tuned > n_cached
+        assert n_cached == n_plain
+        for m, a, r in zip(got, again, ref):
+            assert np.array_equal(m, a)
+            assert relerr(m, r) < TOL[prec]
+
+
+@pytest.mark.parametrize("threads", [256, 512, 1024])
+def test_ensemble_padded_kernel_matches_oracle(built_lib, tmp_path, monkeypatch, threads):
+    """The padded-row float-float ensemble kernel at every tuned CTA size
+    (forced through a cache entry): parity with the oracle; the doubling
+    moments' imaginary parts are exactly 0 (Hermitian members)."""
+    rng = np.random.default_rng(23 + threads)
+    Hs, psis = _members(rng, 16, 6, 20)
+    ens = kg.EnsembleOperator(Hs)
+    NH, nnz = ens.op.shape[0], ens.op.nnz
+    cache = tmp_path / "tune.txt"
+    monkeypatch.setenv("KPMGB_TUNE_CACHE", str(cache))
+    # learn the exact key from a tuning run, then pin its value
+    kg.kpm_1d_ensemble(ens, 64, psis, precision="ff", kernel="tune")
+    key = [l.rsplit(" ", 1)[0] for l in cache.read_text().splitlines()
+           if l.startswith("ensemble|") and f"|NH={NH}|nnz={nnz}|" in l and "|prec=1" in l][0]
+    cache.write_text(f"{key} {threads},1\n")
+    got = kg.kpm_1d_ensemble(ens, 128, psis, precision="ff", avg_output=False, kernel="tune")
+    for H, p, m in zip(Hs, psis, got):
+        assert relerr(m, ko.kpm_1d_doubling(H, 128, p)) < TOL["ff"]
+        assert np.all(m.imag == 0.0)

@@ -363,6 +363,79 @@ def test_padded_row_kernel_real_matches_oracle(NR, lr):
     assert relerr(got, gat) < 1e-13
 
 
+@pytest.mark.parametrize("NR", [33, 40, 64])
+@pytest.mark.parametrize("dot", ["doubling", "lr"])
+@pytest.mark.parametrize("W", [5, 7, 8])
+def test_streaming_kernel_matches_oracle(NR, dot, W):
+    """kernel variant 11 (row-streaming, real H, 33..64 columns, rows of 5..8
+    nonzeros, one anchored chunk per row, loads prefetched across rows): moments
+    against the oracle and against the register-gather kernel; the doubling
+    moments' imaginary parts are exactly 0 (Hermitian H)."""
+    rng = np.random.default_rng(NR + 11 * W)
+    if W == 7:
+        H = (models.cubic_anderson(7, W=4.0, rng=rng) / 8.2).tocsc()
+    else:
+        H = _ragged_herm(rng, 300, W, False)
+        while np.diff(H.tocsr().indptr).max() != W:       # exactly W in the longest row
+            H = _ragged_herm(rng, 300, W, False)
+    NH = H.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    if dot == "lr":
+        psr = ko.random_phase_vectors(rng, NH, NR)
+        kw = dict(psi_in_l=psi, psi_in_r=psr)
+        NC, ref = 41, ko.kpm_1d_lr(H, 41, psi, psr)
+    else:
+        kw = dict(psi_in=psi)
+        NC, ref = 96, ko.kpm_1d_doubling(H, 96, psi)
+    got = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="streaming", **kw)
+    gat = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="gather", **kw)
+    assert relerr(got, ref) < TOL["ff"]
+    assert relerr(got, gat) < 1e-12
+    if dot == "doubling":
+        assert np.all(got.imag == 0.0)
+
+
+def test_streaming_kernel_limits():
+    rng = np.random.default_rng(4)
+    H = (models.cubic_anderson(5, W=1.0, rng=rng) / 7.0).tocsc()
+    psi = ko.random_phase_vectors(rng, 125, 40)
+    with pytest.raises(kg.KPMArgumentError):   # 32 columns
+        kg.kpm_1d(H, 16, 32, psi_in=psi[:, :32], precision="ff", kernel="streaming")
+    with pytest.raises(kg.KPMArgumentError):   # FP64
+        kg.kpm_1d(H, 16, 40, psi_in=psi, precision="fp64", kernel="streaming")
+    Hc = _peierls_square(8, rng)               # complex operator
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d(Hc, 16, 40, psi_in=ko.random_phase_vectors(rng, 64, 40), precision="ff",
+                  kernel="streaming")
+    long_rows = _ragged_herm(rng, 80, 13, False)
+    long_rows = long_rows if np.diff(long_rows.tocsr().indptr).max() > 8 else None
+    if long_rows is not None:
+        with pytest.raises(kg.KPMArgumentError):
+            kg.kpm_1d(long_rows, 16, 40, psi_in=ko.random_phase_vectors(rng, 80, 40),
+                      precision="ff", kernel="streaming")
+
+
+def _ragged_herm(rng, n, max_row, complex_h):
+    """Hermitian operator with row lengths spread over 0..max_row (some rows
+    empty), scaled into the Chebyshev domain."""
+    rows, cols = [], []
+    for i in range(n):
+        k = int(rng.integers(0, max_row // 2 + 1))
+        for j in rng.choice(n, size=k, replace=False):
+            rows.append(i)
+            cols.append(int(j))
+    vals = rng.standard_normal(len(rows)) + (1j * rng.standard_normal(len(rows)) if complex_h else 0)
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    A = (A + A.conj().T).tocsc()
+    A.sum_duplicates()
+    deg = np.diff(A.indptr)
+    keep = deg <= max_row
+    A = sp.diags(keep.astype(float)) @ A @ sp.diags(keep.astype(float))
+    A = sp.csc_matrix(A)
+    A.eliminate_zeros()
+    return A / (1.05 * max(np.abs(np.linalg.eigvalsh(A.toarray())).max(), 1e-3))
+
+
 @pytest.mark.parametrize("max_row", [3, 8, 13, 16])
 @pytest.mark.parametrize("complex_h,NR", [(False, 6), (False, 12), (False, 40), (False, 64),
                                           (True, 5), (True, 16), (True, 32)])

@@ -131,4 +131,59 @@ def test_dos_argument_errors():
     with pytest.raises(kg.KPMArgumentError):
         kg.dos(np.ones(8), 1.0, E_grid=np.zeros(3), E_range=[0, 1])
     with pytest.raises(kg.KPMArgumentError):
-        kg.dos(np.ones(8), 1.0, dE_order=1)
+        kg.dos(np.ones(8), 1.0, dE_order=5)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.dos(np.ones(8), 1.0, dE_order=-1)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.dos0(np.ones(8), 1.0, dE_order=1)
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4])
+def test_dos_energy_derivatives_match_oracle(order):
+    """dos(mu, a; dE_order) (src/applications/dos.jl:128-139): the device jets
+    against the oracle's jets through cos(n acos x) (the arithmetic of the
+    reference's nested ForwardDiff), and against finite differences of the
+    dE_order - 1 curve."""
+    rng = np.random.default_rng(40 + order)
+    NC = 200
+    mu = rng.standard_normal(NC) * np.exp(-np.arange(NC) / 50)
+    mu[0] = 1.0
+    a, b = 1.7, 0.35
+    Eg = b + a * np.linspace(-0.97, 0.97, 41)
+    Eg = np.concatenate([Eg, [b - 1.5 * a, b + 1.01 * a]])   # outside: zero
+    _, d = kg.dos(mu, a, b=b, E_grid=Eg, dE_order=order)
+    ref = ko.dos_derivative(mu, a, b, Eg, order)
+    assert np.abs(d - ref).max() <= 1e-10 * np.abs(ref).max()
+    assert np.all(d[-2:] == 0)
+    h = 1e-5 * a
+    E_in = Eg[:-2]
+    _, up = kg.dos(mu, a, b=b, E_grid=E_in + h, dE_order=order - 1)
+    _, dn = kg.dos(mu, a, b=b, E_grid=E_in - h, dE_order=order - 1)
+    fd = (up - dn) / (2 * h)
+    assert np.abs(d[:-2] - fd).max() <= 1e-5 * np.abs(fd).max()
+
+
+def test_dos_derivative_reference_cases():
+    """test/dos_test.jl:143-193: dE_order = 1 against central differences
+    (rtol 1e-5), dE_order = 2 against the five-point stencil (rtol 1e-7) and
+    against dos0 at the band centre (rtol 1e-10)."""
+    rng = np.random.default_rng(23)
+    NC, a, b = 48, 1.7, 0.35
+    mu = rng.standard_normal(NC)
+    E_grid = b + a * np.array([-0.45, 0.2, 0.55])
+    h = 1e-3 * a
+
+    def rho0(E):
+        return kg.dos(mu, a, b=b, E_grid=[E], N_tilde=1)[1][0]
+
+    stencil = np.array([(-rho0(E + 2 * h) + 16 * rho0(E + h) - 30 * rho0(E)
+                         + 16 * rho0(E - h) - rho0(E - 2 * h)) / (12 * h * h) for E in E_grid])
+    _, d2 = kg.dos(mu, a, b=b, E_grid=E_grid, N_tilde=3, dE_order=2)
+    assert np.allclose(d2, stencil, rtol=1e-7, atol=0)
+    _, d2c = kg.dos(mu, a, b=b, E_grid=[b], N_tilde=1, dE_order=2)
+    assert abs(d2c[0] - kg.dos0(mu, a, dE_order=2)) <= 1e-10 * abs(d2c[0])
+    assert abs(kg.dos0(mu, a) - kg.dos(mu, a, b=b, E_grid=[b])[1][0]) <= 1e-10 * abs(kg.dos0(mu, a))
+    h1 = 1e-4 * a
+    _, d1 = kg.dos(mu, a, b=b, E_grid=E_grid, dE_order=1)
+    fd = (kg.dos(mu, a, b=b, E_grid=E_grid + h1)[1] - kg.dos(mu, a, b=b, E_grid=E_grid - h1)[1]) / (2 * h1)
+    assert np.allclose(d1, fd, rtol=1e-5, atol=0)

@@ -336,3 +336,29 @@ def test_oracle_tangent_finite_difference():
     fd1 = (ko.kpm_1d_lr(model(t2 + h)[0], NC, psr, psr)
            - ko.kpm_1d_lr(model(t2 - h)[0], NC, psr, psr)) / (2 * h)
     assert relerr(d1, fd1) < 1e-6
+
+
+def test_oracle_dos_derivatives():
+    """test/dos_test.jl:143-193 on the oracle: dE_order = 1 against central
+    differences (rtol 1e-5), dE_order = 2 against the five-point stencil
+    (rtol 1e-7) and against dos0 at the band centre (rtol 1e-10)."""
+    rng = np.random.default_rng(23)
+    NC, a, b = 48, 1.7, 0.35
+    mu = rng.standard_normal(NC)
+    E_grid = b + a * np.array([-0.45, 0.2, 0.55])
+    h = 1e-3 * a
+
+    def rho0(E):
+        return ko.dos(mu, a, b, E_grid=[E])[1][0]
+
+    stencil = np.array([(-rho0(E + 2 * h) + 16 * rho0(E + h) - 30 * rho0(E)
+                         + 16 * rho0(E - h) - rho0(E - 2 * h)) / (12 * h * h) for E in E_grid])
+    assert np.allclose(ko.dos_derivative(mu, a, b, E_grid, 2), stencil, rtol=1e-7, atol=0)
+    c = ko.dos_derivative(mu, a, b, [b], 2)[0]
+    assert abs(c - ko.dos0(mu, a, dE_order=2)) <= 1e-10 * abs(c)
+    assert abs(ko.dos0(mu, a) - ko.dos(mu, a, b, E_grid=[b])[1][0]) <= 1e-12 * abs(ko.dos0(mu, a))
+    h1 = 1e-4 * a
+    fd = (ko.dos(mu, a, b, E_grid=E_grid + h1)[1] - ko.dos(mu, a, b, E_grid=E_grid - h1)[1]) / (2 * h1)
+    assert np.allclose(ko.dos_derivative(mu, a, b, E_grid, 1), fd, rtol=1e-5, atol=0)
+    assert np.allclose(ko.dos_derivative(mu, a, b, E_grid, 0), ko.dos(mu, a, b, E_grid=E_grid)[1],
+                       rtol=1e-13, atol=0)
