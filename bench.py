@@ -668,6 +668,12 @@ def main():
     ms = float(t.item())
     value = world * NR * (NC // 2) / (ms / 1e3)
     mu_chosen = mu_t.cpu().numpy().T.copy()
+    if world > 1:
+        # every rank ran its own NR probe columns (weak scaling); one sum over
+        # the ranks assembles all world * NR columns (kpm_gb300.sharding)
+        from kpm_gb300 import sharding
+        mu_global = sharding.gather_probe_moments(mu_chosen, world * NR)
+        mu_avg = mu_global.sum(axis=0).real / (world * NR)
 
     # roofline of the dominant kernel (the fused recurrence step)
     nnz = h.H.nnz
@@ -775,6 +781,9 @@ def main():
             "kpm2d_tensor_core": cond,
             "version": kg.version(),
         }
+        if world > 1:
+            line["sharded"] = {"probe_columns": world * NR, "mu0_average": float(mu_avg[0]),
+                               "reduction": "kpm_gb300.sharding.gather_probe_moments (NCCL)"}
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

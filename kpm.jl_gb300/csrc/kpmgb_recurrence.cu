@@ -183,6 +183,13 @@ bool padded_complex() {
   return on;
 }
 
+// Automatic selection of the complex row-streaming kernel
+// (KPMGB_STREAMING_COMPLEX=0 turns it off).
+const bool kStreamingComplex = [] {
+  const char* e = std::getenv("KPMGB_STREAMING_COMPLEX");
+  return !(e && std::atoi(e) == 0);
+}();
+
 int grid_for(KernelFn fn, int64_t NH, int lpr) {
   const int per_sm = blocks_per_sm(fn);
   const int64_t groups = kThreads / lpr;
@@ -210,6 +217,9 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
                                       sizeof(double2));
         if (KernelFn fr = select_kernel_ffr(ncols, dot, H.is_real != 0, H.max_row_nnz, H.ell_w))
           worst = std::max(worst, (size_t)grid_for(fr, NH, 32) * 2 * ncols * sizeof(double2));
+        if (KernelFn fc = select_kernel_ffc(ncols, dot, H.is_real != 0, H.ell_w))
+          worst = std::max(worst, (size_t)grid_for(fc, NH, ffc_lanes(ncols)) * 2 * ncols *
+                                      sizeof(double2));
       }
     }
   }
@@ -273,10 +283,20 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
         KPMGB_TRY(launch_step_kernel(fr, grid_for(fr, a.NH, 32), s, p));
         continue;
       }
+      KernelFn fc = H.ell_w > 0 && kStreamingComplex
+                        ? select_kernel_ffc(p.ncols, a.dot, H.is_real != 0, H.ell_w)
+                        : nullptr;
+      if (a.variant == 11 && !fc && H.ell_w > 0)
+        fc = select_kernel_ffc(p.ncols, a.dot, H.is_real != 0, H.ell_w);
+      if (fc) {
+        KPMGB_TRY(launch_step_kernel(fc, grid_for(fc, a.NH, ffc_lanes(p.ncols)), s, p));
+        continue;
+      }
       if (a.variant == 11)
         return fail(KPMGB_ERR_ARGUMENT,
-                    "the row-streaming kernel serves float-float steps of real operators with "
-                    "33..64 columns and rows of 5..8 nonzeros");
+                    "the row-streaming kernels serve float-float steps of real operators with "
+                    "33..64 columns and rows of 5..8 nonzeros, and of complex operators with "
+                    "9..32 columns and rows of 5..12 nonzeros");
     }
     const bool auto_padded = a.variant == 0 && H.ell_w > 0 &&
                              ((H.is_real && p.ncols > 32) || padded_complex());
@@ -312,7 +332,8 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
       select_kernel_ffe(a0.NR, a0.dot, a0.H->is_real != 0))
     cands.push_back({9, 0});
   if (precision == KPMGB_PREC_FF &&
-      select_kernel_ffr(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz, a0.H->ell_w))
+      (select_kernel_ffr(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz, a0.H->ell_w) ||
+       select_kernel_ffc(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->ell_w)))
     cands.push_back({11, 0});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   KPMGB_CUDA(cudaEventCreate(&e0));

@@ -737,6 +737,11 @@ int ffe_lanes(int ncols);
 // stride 8 (kpmgb_step_ffe.cu): 33..64 columns (32 lanes x 2 per row), rows of
 // at most 8 nonzeros; nullptr otherwise.  Rows per block tile: 8.
 KernelFn select_kernel_ffr(int ncols, int dot, bool real, int max_row_nnz, int ell_w);
+// Row-streaming float-float kernel for complex operators over padded rows of
+// stride 8 or 12 (kpmgb_step_ffe.cu): 9..32 columns, one column per lane;
+// nullptr otherwise.  ffc_lanes: lanes per row (16 or 32).
+KernelFn select_kernel_ffc(int ncols, int dot, bool real, int ell_w);
+int ffc_lanes(int ncols);
 
 }  // namespace step
 }  // namespace kpmgb

@@ -443,6 +443,173 @@ KernelFn select_kernel_ffr(int ncols, int dot, bool real, int max_row_nnz, int e
   }
 }
 
+// ---------------------------------------------------------------------------
+// Row-streaming form for complex operators with 9..32 columns (k_step_ffc):
+// LPR lanes per row with one column each (two rows per warp for 16 columns),
+// rows padded to W <= 16 slots; the next rows' column indices and complex
+// values are staged in shared memory with cp.async while the current rows are
+// computed, and the row's z, own x (and bra) and every gather are issued
+// before the arithmetic, as in k_step_ffr.  Doubling dots: <x|x> and Re<x|y>.
+template <int LPR, int W, int DOT, bool FULL>
+__global__ void __launch_bounds__(kThreads, 2) k_step_ffc(KParams p) {
+  pdl_enter();
+  constexpr int RPW = 32 / LPR;                 // rows per warp
+  constexpr int GROUPS = kThreads / LPR;        // rows per block tile
+  constexpr int ND = NDots<DOT>::value;
+  constexpr int NDA = ND > 0 ? ND : 1;
+  constexpr int kPieces = W / 4 + W;            // 16-byte pieces of one padded row
+  const int g = threadIdx.x / LPR, lg = threadIdx.x % LPR;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / LPR;                   // row of this lane within the warp
+  const float4* __restrict__ x = static_cast<const float4*>(p.x);
+  const float4* z = static_cast<const float4*>(p.z);
+  float4* y = static_cast<float4*>(p.y);
+  const float4* __restrict__ bra = static_cast<const float4*>(p.bra);
+  const int* __restrict__ ecol = p.ell_col;
+  const float4* __restrict__ eval = static_cast<const float4*>(p.ell_val);
+  const float alpha = p.alpha_f;
+  const int beta_mode = p.beta_mode;
+  const int ld = p.ld;
+  const bool live = FULL || lg < p.ncols;
+
+  __shared__ double2 sacc[kThreads][NDA];
+  // per warp, two buffers of RPW padded rows: W indices then W values each
+  __shared__ __align__(16) float4 sidx[kThreads / 32][2][RPW][kPieces];
+  float dS[NDA][2], dC[NDA][2];
+#pragma unroll
+  for (int k = 0; k < NDA; ++k) {
+    sacc[threadIdx.x][k] = make_double2(0.0, 0.0);
+    dS[k][0] = dS[k][1] = dC[k][0] = dC[k][1] = 0.f;
+  }
+  int rows_since_flush = 0;
+  const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+  // the warp's lanes copy the RPW rows of tile t into buffer b
+  auto stage = [&](int64_t t, int b) {
+    for (int q = lane; q < RPW * kPieces; q += 32) {
+      const int rr = q / kPieces, piece = q % kPieces;
+      const int64_t r = t * GROUPS + warp * RPW + rr;
+      if (t < ntiles && r < p.NH) {
+        const char* src = piece < W / 4
+                              ? reinterpret_cast<const char*>(ecol + r * W) + piece * 16
+                              : reinterpret_cast<const char*>(eval + r * W + (piece - W / 4));
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&sidx[warp][b][rr][piece]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int buf = 0;
+  stage(blockIdx.x, 0);
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    stage(t + gridDim.x, buf ^ 1);
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncwarp();
+    const int64_t r = t * GROUPS + g;
+    const bool row_ok = r < p.NH;
+    const int* jrow = reinterpret_cast<const int*>(&sidx[warp][buf][sub][0]);
+    const float4* hrow = &sidx[warp][buf][sub][W / 4];
+    const int64_t base = r * ld + p.c0 + lg;
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 zv = zero, xo = zero, bo = zero, xv[W];
+    if (row_ok && live) {
+      if (beta_mode != 0) zv = __ldcs(z + base);
+      if (DOT == DOT_DOUBLING || DOT == DOT_LR2) xo = __ldg(x + base);
+      if (DOT == DOT_LR2 || DOT == DOT_LR1) bo = __ldg(bra + base);
+#pragma unroll
+      for (int u = 0; u < W; ++u) xv[u] = __ldg(x + (int64_t)jrow[u] * ld + p.c0 + lg);
+    } else {
+#pragma unroll
+      for (int u = 0; u < W; ++u) xv[u] = zero;
+    }
+    float R = 0.f, M = 0.f;
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      const float4 h = hrow[u];
+      R = __fadd_rn(R, habs(h));
+      M = fmaxf(M, fmaxf(fabsf(xv[u].x), fabsf(xv[u].z)));
+    }
+    const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+    const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+    float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+    for (int u = 0; u < W; ++u) ffmac(Ar, cr, Ai, ci, hrow[u], xv[u]);
+    __syncwarp();  // the buffer is restaged two tiles later
+    buf ^= 1;
+    if (row_ok && live) {
+      const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+      const float2 yr = ff_epilogue(sr, cr, alpha, beta_mode, zv.x, zv.y);
+      const float2 yi = ff_epilogue(si, ci, alpha, beta_mode, zv.z, zv.w);
+      const float4 yv = make_float4(yr.x, yr.y, yi.x, yi.y);
+      __stcs(y + base, yv);
+      if constexpr (DOT == DOT_DOUBLING) {
+        ffnorm2(dS[0], dC[0], xo);
+        ff::dacc(dS[1][0], dC[1][0], xo.x, xo.y, yv.x, yv.y);
+        ff::dacc(dS[1][0], dC[1][0], xo.z, xo.w, yv.z, yv.w);
+      } else if constexpr (DOT == DOT_LR2) {
+        ffdot(dS[0], dC[0], bo, xo);
+        ffdot(dS[1], dC[1], bo, yv);
+      } else if constexpr (DOT == DOT_LR1) {
+        ffdot(dS[0], dC[0], bo, yv);
+      }
+    }
+    if constexpr (ND > 0) {
+      if (++rows_since_flush == kFlushRows) {
+        rows_since_flush = 0;
+#pragma unroll
+        for (int k = 0; k < ND; ++k) {
+          double2 v = sacc[threadIdx.x][k];
+          v.x += ff::join(dS[k][0], dC[k][0]);
+          if (!(DOT == DOT_DOUBLING && k == 1)) v.y += ff::join(dS[k][1], dC[k][1]);
+          sacc[threadIdx.x][k] = v;
+          dS[k][0] = dS[k][1] = dC[k][0] = dC[k][1] = 0.f;
+        }
+      }
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if constexpr (ND > 0) {
+    double2 d[NDA][1];
+#pragma unroll
+    for (int k = 0; k < ND; ++k) {
+      d[k][0] = sacc[threadIdx.x][k];
+      d[k][0].x += ff::join(dS[k][0], dC[k][0]);
+      if (!(DOT == DOT_DOUBLING && k == 1)) d[k][0].y += ff::join(dS[k][1], dC[k][1]);
+    }
+    reduce_finalize<ND, LPR, 1>(d, p);
+  }
+}
+
+namespace {
+
+template <int LPR, int W, bool FULL>
+KernelFn ffc_dot(int dot) {
+  switch (dot) {
+    case DOT_DOUBLING: return k_step_ffc<LPR, W, DOT_DOUBLING, FULL>;
+    case DOT_LR2: return k_step_ffc<LPR, W, DOT_LR2, FULL>;
+    case DOT_LR1: return k_step_ffc<LPR, W, DOT_LR1, FULL>;
+    default: return k_step_ffc<LPR, W, DOT_NONE, FULL>;
+  }
+}
+
+template <int LPR>
+KernelFn ffc_w(int ncols, int dot, int ell_w) {
+  const bool full = ncols == LPR;
+  switch (ell_w) {
+    case 8: return full ? ffc_dot<LPR, 8, true>(dot) : ffc_dot<LPR, 8, false>(dot);
+    case 12: return full ? ffc_dot<LPR, 12, true>(dot) : ffc_dot<LPR, 12, false>(dot);
+    default: return nullptr;
+  }
+}
+
+}  // namespace
+
+KernelFn select_kernel_ffc(int ncols, int dot, bool real, int ell_w) {
+  if (real || ncols < 9 || ncols > 32) return nullptr;
+  return ncols <= 16 ? ffc_w<16>(ncols, dot, ell_w) : ffc_w<32>(ncols, dot, ell_w);
+}
+
+int ffc_lanes(int ncols) { return ncols <= 16 ? 16 : 32; }
+
 // 5..64 columns: 8 or 16 lanes per row with one column each up to 8 and 16
 // columns, 32 lanes with one or two columns each above.  For real operators
 // with 33..64 columns and complex ones with 9..32 (chunks of 4 in k_step_ff)

@@ -57,8 +57,7 @@ def _allreduce_sum(arr: np.ndarray, group) -> np.ndarray:
     """Sum a complex/real numpy array over the ranks of ``group``."""
     import torch
     dist = _dist()
-    world, _ = _world(group)
-    if world == 1:
+    if not dist.is_available() or not dist.is_initialized():
         return arr
     t = torch.from_numpy(np.ascontiguousarray(arr))
     if t.is_complex():
@@ -70,6 +69,21 @@ def _allreduce_sum(arr: np.ndarray, group) -> np.ndarray:
     if np.iscomplexobj(arr):
         t = torch.view_as_complex(t.contiguous())
     return t.numpy().reshape(arr.shape)
+
+
+def gather_probe_moments(mu_local: np.ndarray, NR_total: int, *, group=None) -> np.ndarray:
+    """Assemble per-rank kpm_1d moments (this rank's (NR_g, NC) block of the
+    columns ``probe_slice(NR_total, world, rank)``) into the full
+    (NR_total, NC) matrix on every rank, by one sum over the ranks."""
+    world, rank = _world(group)
+    sl = probe_slice(NR_total, world, rank)
+    mu_local = np.asarray(mu_local)
+    if mu_local.shape[0] != sl.stop - sl.start:
+        raise KPMArgumentError(f"rank {rank} holds {mu_local.shape[0]} columns; its slice has "
+                               f"{sl.stop - sl.start}")
+    full = np.zeros((int(NR_total), mu_local.shape[1]), dtype=np.complex128)
+    full[sl] = mu_local
+    return _allreduce_sum(full, group)
 
 
 def kpm_1d_sharded(H, NC: int, psi_in, *, group=None, avg_output: bool = True, compute=None,
@@ -88,9 +102,8 @@ def kpm_1d_sharded(H, NC: int, psi_in, *, group=None, avg_output: bool = True, c
     if world > NR:
         raise KPMArgumentError(f"{world} ranks for {NR} probe columns")
     sl = probe_slice(NR, world, rank)
-    mu_all = np.zeros((NR, int(NC)), dtype=np.complex128)
-    mu_all[sl] = compute(H, int(NC), np.array(psi[:, sl], dtype=np.complex128))
-    mu_all = _allreduce_sum(mu_all, group)
+    mu_all = gather_probe_moments(compute(H, int(NC), np.array(psi[:, sl], dtype=np.complex128)),
+                                  NR, group=group)
     if avg_output:
         return mu_all.sum(axis=0).real / NR
     return mu_all

@@ -395,6 +395,40 @@ def test_streaming_kernel_matches_oracle(NR, dot, W):
         assert np.all(got.imag == 0.0)
 
 
+@pytest.mark.parametrize("NR", [9, 16, 24, 32])
+@pytest.mark.parametrize("dot", ["doubling", "lr"])
+@pytest.mark.parametrize("case", ["peierls", "haldane", "ragged12", "ragged7"])
+def test_streaming_kernel_complex_matches_oracle(NR, dot, case):
+    """kernel variant 11 on complex operators (k_step_ffc: 9..32 columns, one
+    column per lane, rows padded to 8 or 12 slots)."""
+    rng = np.random.default_rng(NR + (7 if dot == "lr" else 0) + len(case))
+    if case == "peierls":
+        H = _peierls_square(16, rng)                        # 5 nonzeros per row
+    elif case == "haldane":
+        Hh, _, _, _ = models.haldane(8, 8, t2=0.2, m=0.1)   # 10 nonzeros per row
+        H = (Hh / 3.8).tocsc()
+    else:
+        w = int(case[6:])
+        H = _ragged_herm(rng, 240, w, True)
+        while np.diff(H.tocsr().indptr).max() < w - 1:
+            H = _ragged_herm(rng, 240, w, True)
+    NH = H.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    if dot == "lr":
+        psr = ko.random_phase_vectors(rng, NH, NR)
+        kw = dict(psi_in_l=psi, psi_in_r=psr)
+        NC, ref = 37, ko.kpm_1d_lr(H, 37, psi, psr)
+    else:
+        kw = dict(psi_in=psi)
+        NC, ref = 80, ko.kpm_1d_doubling(H, 80, psi)
+    got = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="streaming", **kw)
+    gat = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="gather", **kw)
+    assert relerr(got, ref) < TOL["ff"]
+    assert relerr(got, gat) < 1e-12
+    if dot == "doubling":
+        assert np.all(got.imag == 0.0)
+
+
 def test_streaming_kernel_limits():
     rng = np.random.default_rng(4)
     H = (models.cubic_anderson(5, W=1.0, rng=rng) / 7.0).tocsc()
@@ -403,9 +437,12 @@ def test_streaming_kernel_limits():
         kg.kpm_1d(H, 16, 32, psi_in=psi[:, :32], precision="ff", kernel="streaming")
     with pytest.raises(kg.KPMArgumentError):   # FP64
         kg.kpm_1d(H, 16, 40, psi_in=psi, precision="fp64", kernel="streaming")
-    Hc = _peierls_square(8, rng)               # complex operator
+    Hc = _peierls_square(8, rng)               # complex operator, 40 columns
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d(Hc, 16, 40, psi_in=ko.random_phase_vectors(rng, 64, 40), precision="ff",
+                  kernel="streaming")
+    with pytest.raises(kg.KPMArgumentError):   # complex operator, 8 columns
+        kg.kpm_1d(Hc, 16, 8, psi_in=ko.random_phase_vectors(rng, 64, 8), precision="ff",
                   kernel="streaming")
     long_rows = _ragged_herm(rng, 80, 13, False)
     long_rows = long_rows if np.diff(long_rows.tocsr().indptr).max() > 8 else None
