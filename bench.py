@@ -443,7 +443,31 @@ def workload_dsigma(args):
         out[f"{contraction}_contraction"] = {
             "forward_ms": tf, "derivative_ms": td, "derivative_over_forward": td / tf,
             "sigma_xy": res["sigma"], "dsigma_xy_dt2": res["dsigma"]}
+    # reverse mode: the gradient of sigma_xy(Ef=0) with respect to every stored
+    # entry of H, Jx and Jy at once (kpmgb_kubo_bastin_weights + kpmgb_kpm2d_grad)
+    def grad():
+        W = kg.kubo_bastin_weights(NC, h.a, 0.0, b=h.b, NH=NH, area=area)
+        res["grads"] = kg.kpm_2d_grad(h.H, Jx, Jy, NC, W, psi_in=psi)
+    tfwd = out["fp64_contraction"]["forward_ms"]
+    tg = _time_host(grad, 1, steps)
+    gH, gJx, gJy = res["grads"]
+    d_rev = _pair(gH, dH) + _pair(gJx, dJx) + _pair(gJy, dJy)
+    out["reverse_mode_gradient"] = {
+        "gradient_ms": tg, "gradient_over_forward_fp64": tg / tfwd,
+        "entries": int(gH.nnz + gJx.nnz + gJy.nnz),
+        "dsigma_xy_dt2_from_gradient": d_rev,
+        "note": "one reverse pass gives d sigma / d (every stored entry of H, Jx, Jy); "
+                "dsigma/dt2 follows by pairing with the t2 direction"}
     return out
+
+
+def _pair(G, D):
+    """sum_k Re(conj(G_k) D_k) over the stored entries of D (G: a gradient on a
+    pattern that contains D's)."""
+    import scipy.sparse as sp
+    g, d = sp.coo_matrix(G), sp.coo_matrix(D)
+    gd = {(i, j): v for i, j, v in zip(g.row, g.col, g.data)}
+    return float(sum((np.conj(gd.get((i, j), 0.0)) * v).real for i, j, v in zip(d.row, d.col, d.data)))
 
 
 def _square_lattice(L):
@@ -547,9 +571,13 @@ def workload_ensemble(args):
     ens = kg.EnsembleOperator(Hs)
     out["ensemble_operator_build_ms"] = (time.perf_counter() - t0) * 1e3
     for prec in ("fp64", "ff"):
-        ms = _time_host(lambda: kg.kpm_1d_ensemble(ens, NC, psis, precision=prec), 1,
-                        max(args.steps, 3))
-        out[f"ensemble_{prec}"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+        for kernel in ("auto", "tune"):
+            ms = _time_host(lambda: kg.kpm_1d_ensemble(ens, NC, psis, precision=prec,
+                                                       kernel=kernel), 1, max(args.steps, 3))
+            key = f"ensemble_{prec}" + ("_tuned" if kernel == "tune" else "")
+            out[key] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+    out["ff_tuned_over_fp64_tuned"] = (out["ensemble_fp64_tuned"]["ms_per_call"]
+                                       / out["ensemble_ff_tuned"]["ms_per_call"])
     ops = [kg.GB300Operator(H) for H in Hs]
     def loop():
         for op, p in zip(ops, psis):

@@ -424,7 +424,9 @@ def test_streaming_kernel_complex_matches_oracle(NR, dot, case):
     got = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="streaming", **kw)
     gat = kg.kpm_1d(H, NC, NR, avg_output=False, precision="ff", kernel="gather", **kw)
     assert relerr(got, ref) < TOL["ff"]
-    assert relerr(got, gat) < 1e-12
+    # both float-float; one anchored chunk per row here against chunks of 8
+    # (+ the rest) in the CSR kernel: different roundings at ~1e-12
+    assert relerr(got, gat) < 1e-11
     if dot == "doubling":
         assert np.all(got.imag == 0.0)
 
