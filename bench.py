@@ -553,7 +553,8 @@ def workload_published(args):
 
 def workload_ensemble(args):
     """256 realisations of the 2D Anderson model, L ~ U{24..96}, W ~ U[1, 8],
-    NC=512, NR=8: one persistent ensemble launch against per-member calls."""
+    NC=512, NR=8: the ensemble call (per-step schedule, persistent schedule,
+    autotuned) against per-member calls."""
     import kpm_gb300 as kg
     from kpm_gb300 import models
     rng = np.random.default_rng(42)
@@ -570,12 +571,38 @@ def workload_ensemble(args):
     t0 = time.perf_counter()
     ens = kg.EnsembleOperator(Hs)
     out["ensemble_operator_build_ms"] = (time.perf_counter() - t0) * 1e3
+    suffix = {"auto": "", "single": "_persistent", "tune": "_tuned"}
     for prec in ("fp64", "ff"):
-        for kernel in ("auto", "tune"):
+        for kernel in ("auto", "single", "tune"):
             ms = _time_host(lambda: kg.kpm_1d_ensemble(ens, NC, psis, precision=prec,
                                                        kernel=kernel), 1, max(args.steps, 3))
-            key = f"ensemble_{prec}" + ("_tuned" if kernel == "tune" else "")
-            out[key] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+            out[f"ensemble_{prec}{suffix[kernel]}"] = {"ms_per_call": ms, "value": vs / (ms / 1e3)}
+    out["ff_over_fp64"] = out["ensemble_fp64"]["ms_per_call"] / out["ensemble_ff"]["ms_per_call"]
+    # device-resident form: probes and moments stay in HBM, CUDA events on the
+    # launching stream (the GPU time of the call)
+    import torch
+    psi_t = torch.from_numpy(np.ascontiguousarray(np.vstack(psis).T)).cuda()
+    mu_t = torch.zeros((len(Hs), NC, NR), dtype=torch.complex128, device="cuda")
+    stream = torch.cuda.current_stream()
+    for prec in ("fp64", "ff"):
+        for kernel in ("auto", "single"):
+            def call():
+                kg.kpm_1d_ensemble_device(ens, NC, psi_t, mu_t, precision=prec, kernel=kernel)
+            call()
+            kg.sync(ens.op)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = max(args.steps, 3)
+            e0.record(stream)
+            for _ in range(reps):
+                call()
+            e1.record(stream)
+            kg.sync(ens.op)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            out[f"ensemble_{prec}{suffix[kernel]}_device"] = {"ms_per_call": ms,
+                                                             "value": vs / (ms / 1e3)}
+    out["ff_over_fp64_device"] = (out["ensemble_fp64_device"]["ms_per_call"]
+                                  / out["ensemble_ff_device"]["ms_per_call"])
     out["ff_tuned_over_fp64_tuned"] = (out["ensemble_fp64_tuned"]["ms_per_call"]
                                        / out["ensemble_ff_tuned"]["ms_per_call"])
     ops = [kg.GB300Operator(H) for H in Hs]

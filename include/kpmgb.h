@@ -182,16 +182,30 @@ int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb,
                        const kpmgb_kpm2d_options* opts, void* stream);
 
 /* Batched ensemble: doubling kpm_1d moments of nseg independent members in one
- * persistent launch (no reference counterpart as a single call; it replaces
- * nseg calls of kpm_1d! on disorder realisations of uneven size).  H is the
- * block-diagonal stack of the members; rows seg[i] .. seg[i+1]-1 belong to
- * member i (seg[0] = 0, seg[nseg] = NH) and H must not couple members.  psi:
- * host NH x NR column-major (member i's probes are its rows); mu_all: host,
- * member i's NR x NC column-major moments at offset i*NR*NC complex values.
- * Probe columns run in batches of 32 (one launch per batch).  Blocking call. */
+ * call (no reference counterpart as a single call; it replaces nseg calls of
+ * kpm_1d! on disorder realisations of uneven size).  H is the block-diagonal
+ * stack of the members; rows seg[i] .. seg[i+1]-1 belong to member i
+ * (seg[0] = 0, seg[nseg] = NH) and H must not couple members.  psi: host
+ * NH x NR column-major (member i's probes are its rows); mu_all: host, member
+ * i's NR x NC column-major moments at offset i*NR*NC complex values.  Probe
+ * columns run in batches of 32.  opts->kernel_variant: 0 automatic (= 9 where
+ * it applies, else 1); 1 one launch per recurrence step over all members,
+ * CTAs of at most 512 rows of one member, CSR rows; 9 the same over padded
+ * float-float rows (float-float, at most 8 nonzeros per row); 6 one
+ * persistent launch in which each CTA runs whole members; 4 autotune (the
+ * schedules, CTA sizes and row formats timed once per ensemble shape and
+ * device, the choice kept in the persistent tuning cache); other values fail
+ * with KPMGB_ERR_ARGUMENT.  Blocking call. */
 int kpmgb_kpm1d_ensemble(kpmgb_operator H, int32_t nseg, const int64_t* seg,
                          int64_t NC, int64_t NR, const double* psi,
                          double* mu_all, const kpmgb_kpm1d_options* opts);
+/* Device-resident form: psi and mu_all are device addresses with the layouts
+ * above (seg stays a host table); enqueued on `stream`, returns without
+ * waiting (kpmgb_operator_sync waits and reports deferred failures). */
+int kpmgb_kpm1d_ensemble_device(kpmgb_operator H, int32_t nseg,
+                                const int64_t* seg, int64_t NC, int64_t NR,
+                                const void* psi, void* mu_all,
+                                const kpmgb_kpm1d_options* opts, void* stream);
 
 /* kpm_1d_current!: mu_all[i, n] = <psi_i| J_a T_n(H) |psi_i>
  * = <J_a^dagger psi_i | T_n(H) psi_i>, n = 0 .. NC-1, no doubling

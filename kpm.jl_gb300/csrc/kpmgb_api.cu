@@ -738,8 +738,8 @@ static int host_kpm1d(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, cons
   KPMGB_TRY(op->ws.psi_in.ensure(lr ? 2 * slot : slot));
   KPMGB_TRY(op->ws.mu.ensure((size_t)NR * std::max<int64_t>(NC, 1) * 16));
   char* in = op->ws.psi_in.as<char>();
-  KPMGB_CUDA(cudaMemcpyAsync(in, psi_r, slot, cudaMemcpyHostToDevice, s));
-  if (lr) KPMGB_CUDA(cudaMemcpyAsync(in + slot, psi_l, slot, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(copy_to_device(in, psi_r, slot, s));
+  if (lr) KPMGB_TRY(copy_to_device(in + slot, psi_l, slot, s));
   KPMGB_TRY(run_kpm1d(op, NC, NR, NH, lr ? in + slot : nullptr, in, op->ws.mu.as<double2>(), opts,
                       s, lr));
   KPMGB_CUDA(cudaMemcpyAsync(mu_all, op->ws.mu.ptr, (size_t)NR * NC * 16, cudaMemcpyDeviceToHost, s));
@@ -786,8 +786,8 @@ int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t 
   KPMGB_TRY(op->ws.psi_in.ensure(2 * slot));
   KPMGB_TRY(op->ws.mu.ensure((size_t)NC * NC * 16));
   char* in = op->ws.psi_in.as<char>();
-  KPMGB_CUDA(cudaMemcpyAsync(in, psi_l, slot, cudaMemcpyHostToDevice, s));
-  KPMGB_CUDA(cudaMemcpyAsync(in + slot, psi_r, slot, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(copy_to_device(in, psi_l, slot, s));
+  KPMGB_TRY(copy_to_device(in + slot, psi_r, slot, s));
   KPMGB_TRY(run_kpm2d(op, as_op(Ja), as_op(Jb), NC, NR, NH, in, in + slot, op->ws.mu.as<double2>(),
                       opts, s));
   KPMGB_CUDA(cudaMemcpyAsync(mu, op->ws.mu.ptr, (size_t)NC * NC * 16, cudaMemcpyDeviceToHost, s));
@@ -797,16 +797,17 @@ int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t 
 }  // extern "C"
 
 // ------------------------------------------------------------ ensemble
-namespace kpmgb {
-int launch_ensemble(const DeviceCSR& H, const int64_t* d_seg, const int* d_order, int nseg, int NR,
-                    int64_t NC, void* slot0, void* slot1, double2* mu, const double* scale,
-                    unsigned* next, unsigned* status, int precision, cudaStream_t s,
-                    const EnsembleShape& shape);
-}
+// Rows per CTA of the per-step ensemble schedule: the default and the
+// autotuner's candidates (the smallest sizes the scratch).
+constexpr int kEnsRows = 512;
+constexpr int kEnsRowsCand[] = {256, 512, 1024, 2048};
+constexpr int kEnsRowsMin = 256;
 
-extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_t* seg,
-                                    int64_t NC, int64_t NR, const double* psi, double* mu_all,
-                                    const kpmgb_kpm1d_options* opts) {
+// The ensemble call on host buffers (psi copied in, moments copied out,
+// blocking) or on device buffers (device = true: enqueued on s).
+static int run_ensemble(kpmgb_operator h, int32_t nseg, const int64_t* seg, int64_t NC,
+                        int64_t NR, const double* psi, double* mu_all,
+                        const kpmgb_kpm1d_options* opts, void* stream, bool device) {
   clear_error();
   if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   if (nseg < 1 || !seg || !psi || !mu_all) return fail(KPMGB_ERR_ARGUMENT, "invalid ensemble arguments");
@@ -824,46 +825,66 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
     if (seg[i + 1] <= seg[i]) return fail(KPMGB_ERR_ARGUMENT, "segment %d is empty or unordered", i);
     order[i] = i;
   }
+  const bool ff = precision == KPMGB_PREC_FF;
+  const bool ell_ok = ff && op->csr.ell_w > 0 && op->csr.max_row_nnz <= 8;
+  const int variant = opts ? opts->kernel_variant : 0;
+  if (variant != 0 && variant != 1 && variant != 4 && variant != 6 && variant != 9)
+    return fail(KPMGB_ERR_ARGUMENT,
+                "the ensemble takes kernel_variant 0 (automatic), 1 (one launch per step, CSR "
+                "rows), 4 (autotune), 6 (one persistent launch) or 9 (one launch per step, "
+                "padded float-float rows)");
+  if (variant == 9 && !ell_ok)
+    return fail(KPMGB_ERR_ARGUMENT, "the padded-row ensemble kernel serves float-float members "
+                                    "with at most 8 nonzeros per row");
   // largest members first: the persistent grid drains the queue evenly
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     return seg[a + 1] - seg[a] > seg[b + 1] - seg[b];
   });
   Guard g(op);
-  cudaStream_t s = op->stream;
+  cudaStream_t s = device ? pick_stream(op, stream) : op->stream;
   Workspace& ws = op->ws;
   // probe columns in batches of at most 32 (one lane per column in the
-  // ensemble kernel); the moments of each column are independent
+  // ensemble kernels); the moments of each column are independent
   constexpr int64_t kBatch = 32;
   const int64_t nb_max = std::min<int64_t>(NR, kBatch);
   const size_t slot = (size_t)NH * nb_max * 16;
-  KPMGB_TRY(ws.psi_in.ensure(slot));
+  if (!device) KPMGB_TRY(ws.psi_in.ensure(slot));
   KPMGB_TRY(ws.slots.ensure(2 * slot));
   KPMGB_TRY(ws.mu.ensure((size_t)nseg * NC * nb_max * 16));
   KPMGB_TRY(ws.scales.ensure((size_t)(3 * nb_max + 2) * sizeof(double)));
-  // segment table + order + work counter in the partials buffer (small)
-  const size_t meta = (size_t)(nseg + 1) * sizeof(int64_t) + (size_t)nseg * sizeof(int) + 64;
-  KPMGB_TRY(ws.partials.ensure(std::max(meta, ws.partials.bytes)));
+  // segment table + order, then the per-step schedule's block table and
+  // partial dots, in the partials buffer
+  const size_t meta = ((size_t)(nseg + 1) * sizeof(int64_t) + (size_t)nseg * sizeof(int) + 15) &
+                      ~(size_t)15;
+  const size_t step_scratch = ensemble_step_scratch_bytes(seg, nseg, (int)nb_max, kEnsRowsMin);
+  KPMGB_TRY(ws.partials.ensure(std::max(meta + step_scratch, ws.partials.bytes)));
   KPMGB_TRY(ensure_sync(op, s));
   char* mp = ws.partials.as<char>();
-  int64_t* d_seg = reinterpret_cast<int64_t*>(mp);
-  int* d_order = reinterpret_cast<int*>(mp + (size_t)(nseg + 1) * sizeof(int64_t));
-  unsigned* next = ws.sync.as<unsigned>() + 2;
-  KPMGB_CUDA(cudaMemcpyAsync(d_seg, seg, (size_t)(nseg + 1) * sizeof(int64_t),
+  EnsembleArgs ea;
+  ea.seg_host = seg;
+  ea.d_seg = reinterpret_cast<int64_t*>(mp);
+  ea.d_order = reinterpret_cast<int*>(mp + (size_t)(nseg + 1) * sizeof(int64_t));
+  ea.nseg = nseg;
+  ea.next = ws.sync.as<unsigned>() + 2;
+  ea.status = ws.sync.as<unsigned>() + 1;
+  ea.scratch = mp + meta;
+  ea.scratch_bytes = ws.partials.bytes - meta;
+  KPMGB_CUDA(cudaMemcpyAsync((void*)ea.d_seg, seg, (size_t)(nseg + 1) * sizeof(int64_t),
                              cudaMemcpyHostToDevice, s));
-  KPMGB_CUDA(cudaMemcpyAsync(d_order, order.data(), (size_t)nseg * sizeof(int),
+  KPMGB_CUDA(cudaMemcpyAsync((void*)ea.d_order, order.data(), (size_t)nseg * sizeof(int),
                              cudaMemcpyHostToDevice, s));
   char* slots = ws.slots.as<char>();
   double* sc = ws.scales.as<double>();
-  const bool ff = precision == KPMGB_PREC_FF;
-  const int variant = opts ? opts->kernel_variant : 0;
-  if (variant != 0 && variant != 4)
-    return fail(KPMGB_ERR_ARGUMENT, "the ensemble kernel takes kernel_variant 0 or 4 (autotune)");
   // load column batch c0 into slot 0 (probes scaled for the float-float path)
   auto load = [&](int64_t c0, int nb, const double** scale) -> int {
     const size_t bb = (size_t)NH * nb * 16;
-    KPMGB_CUDA(cudaMemsetAsync(next, 0, sizeof(unsigned), s));
-    KPMGB_CUDA(cudaMemcpyAsync(ws.psi_in.ptr, psi + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
-    KPMGB_TRY(launch_load_block(ws.psi_in.ptr, slots, NH, nb, precision, sc, false, s));
+    KPMGB_CUDA(cudaMemsetAsync(ea.next, 0, sizeof(unsigned), s));
+    const double* src = psi + 2 * c0 * NH;
+    if (!device) {
+      KPMGB_TRY(copy_to_device(ws.psi_in.ptr, src, bb, s));
+      src = ws.psi_in.as<double>();
+    }
+    KPMGB_TRY(launch_load_block(src, slots, NH, nb, precision, sc, false, s));
     *scale = nullptr;
     if (ff) {
       KPMGB_TRY(launch_scale_product(sc, sc, sc + 2 * nb, nb, s));
@@ -871,12 +892,20 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
     }
     return KPMGB_OK;
   };
-  // Launch shape: the default (1024 threads per CTA, CSR rows), or with
-  // kernel_variant 4 the fastest of the candidate shapes timed on a short
-  // recurrence of the first column batch, kept per (device, ensemble shape)
-  // in the persistent autotuning cache.
+  // Schedule and launch shape.  Automatic: one launch per step over CTAs of
+  // at most 512 rows of a member, padded rows where the float-float members
+  // allow them (256 2D Anderson realisations L = 24..96, NR = 8, NC = 512 on
+  // GB300: see the tuning record).  kernel_variant 4 times the candidates on
+  // a short recurrence of the first column batch and keeps the fastest per
+  // (device, ensemble shape) in the persistent autotuning cache.
   EnsembleShape shape;
-  if (variant == 4) {
+  if (variant == 6) {
+    shape = EnsembleShape{1024, false, 0};
+  } else if (variant == 1) {
+    shape = EnsembleShape{256, false, kEnsRows};
+  } else if (variant == 9 || variant == 0) {
+    shape = EnsembleShape{256, ell_ok, kEnsRows};
+  } else {
     const int nb0 = (int)nb_max;
     const std::string key = "ensemble|" + device_tag() + "|nseg=" + std::to_string(nseg) +
                             "|NH=" + std::to_string(NH) + "|nnz=" + std::to_string(op->csr.nnz) +
@@ -884,16 +913,22 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
                             std::to_string(op->csr.is_real) + "|NR=" + std::to_string(nb0) +
                             "|prec=" + std::to_string(precision);
     std::string cached;
-    int th = 0, pad = 0;
-    if (tune_cache_get(key, &cached) && std::sscanf(cached.c_str(), "%d,%d", &th, &pad) == 2 &&
-        th >= 32 && th <= 1024 && th % 32 == 0 && (pad == 0 || pad == 1)) {
-      shape.threads = th;
-      shape.padded = pad != 0;
+    int th = 0, pad = 0, rows = 0;
+    const int nf = tune_cache_get(key, &cached)
+                       ? std::sscanf(cached.c_str(), "%d,%d,%d", &th, &pad, &rows)
+                       : 0;
+    if (nf == 3 && th >= 32 && th <= 1024 && th % 32 == 0 && (pad == 0 || (pad == 1 && ell_ok)) &&
+        (rows == 0 || rows >= kEnsRowsMin)) {
+      shape = EnsembleShape{th, pad != 0, rows};
     } else {
       std::vector<EnsembleShape> cands;
       for (int t : {256, 512, 1024}) {
-        cands.push_back({t, false});
-        if (ff && op->csr.ell_w > 0 && op->csr.max_row_nnz <= 8) cands.push_back({t, true});
+        cands.push_back({t, false, 0});
+        if (ell_ok) cands.push_back({t, true, 0});
+      }
+      for (int r : kEnsRowsCand) {
+        cands.push_back({256, false, r});
+        if (ell_ok) cands.push_back({256, true, r});
       }
       const int64_t NCt = std::min<int64_t>(NC, 64);
       cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -905,9 +940,8 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
         const double* scale = nullptr;
         if ((rc = load(0, nb0, &scale)) != KPMGB_OK) break;
         cudaEventRecord(e0, s);
-        rc = launch_ensemble(op->csr, d_seg, d_order, nseg, nb0, NCt, slots,
-                             slots + (size_t)NH * nb0 * 16, ws.mu.as<double2>(), scale, next,
-                             ws.sync.as<unsigned>() + 1, precision, s, c);
+        rc = launch_ensemble(op->csr, ea, nb0, NCt, slots, slots + (size_t)NH * nb0 * 16,
+                             ws.mu.as<double2>(), scale, precision, s, c);
         cudaEventRecord(e1, s);
         if (rc != KPMGB_OK) break;
         if (cudaEventSynchronize(e1) != cudaSuccess) {
@@ -925,7 +959,8 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       KPMGB_TRY(rc);
-      tune_cache_put(key, std::to_string(shape.threads) + "," + (shape.padded ? "1" : "0"));
+      tune_cache_put(key, std::to_string(shape.threads) + "," + (shape.padded ? "1" : "0") + "," +
+                              std::to_string(shape.rows));
     }
   }
   for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
@@ -933,14 +968,27 @@ extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_
     const size_t bb = (size_t)NH * nb * 16;
     const double* scale = nullptr;
     KPMGB_TRY(load(c0, nb, &scale));
-    KPMGB_TRY(launch_ensemble(op->csr, d_seg, d_order, nseg, nb, NC, slots, slots + bb,
-                              ws.mu.as<double2>(), scale, next, ws.sync.as<unsigned>() + 1,
+    KPMGB_TRY(launch_ensemble(op->csr, ea, nb, NC, slots, slots + bb, ws.mu.as<double2>(), scale,
                               precision, s, shape));
     // [nseg][NC][nb] -> columns c0 .. c0+nb of the caller's [nseg][NC][NR]
     KPMGB_CUDA(cudaMemcpy2DAsync(mu_all + 2 * c0, (size_t)NR * 16, ws.mu.ptr, (size_t)nb * 16,
-                                 (size_t)nb * 16, (size_t)nseg * NC, cudaMemcpyDeviceToHost, s));
+                                 (size_t)nb * 16, (size_t)nseg * NC,
+                                 device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
   }
-  return check_status(op, s);
+  return device ? KPMGB_OK : check_status(op, s);
+}
+
+extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_t* seg,
+                                    int64_t NC, int64_t NR, const double* psi, double* mu_all,
+                                    const kpmgb_kpm1d_options* opts) {
+  return run_ensemble(h, nseg, seg, NC, NR, psi, mu_all, opts, nullptr, false);
+}
+
+extern "C" int kpmgb_kpm1d_ensemble_device(kpmgb_operator h, int32_t nseg, const int64_t* seg,
+                                           int64_t NC, int64_t NR, const void* psi, void* mu_all,
+                                           const kpmgb_kpm1d_options* opts, void* stream) {
+  return run_ensemble(h, nseg, seg, NC, NR, static_cast<const double*>(psi),
+                      static_cast<double*>(mu_all), opts, stream, true);
 }
 
 // ------------------------------------------------------------ adjoint
@@ -979,7 +1027,7 @@ extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_
   for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
     const int64_t nb = std::min<int64_t>(kBatch, NR - c0);
     const size_t bb = (size_t)NH * nb * 16;
-    KPMGB_CUDA(cudaMemcpyAsync(in, psi + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
+    KPMGB_TRY(copy_to_device(in, psi + 2 * c0 * NH, bb, s));
     KPMGB_TRY(launch_load_block(in, in + blk, NH, (int)nb, KPMGB_PREC_FP64, nullptr, false, s));
     KPMGB_TRY(run_kpm1d_grad(op->csr, op->csr.perm, NC, (int)nb, NH,
                              reinterpret_cast<const double2*>(in + blk), g, checkpoint_every,
@@ -1077,8 +1125,8 @@ extern "C" int kpmgb_kpm2d_grad(kpmgb_operator h, kpmgb_operator ja, kpmgb_opera
   for (int64_t c0 = 0; c0 < NR; c0 += kBatch) {
     const int64_t nb = std::min<int64_t>(kBatch, NR - c0);
     const size_t bb = (size_t)NH * nb * 16;
-    KPMGB_CUDA(cudaMemcpyAsync(in, psi_l + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
-    KPMGB_CUDA(cudaMemcpyAsync(in + blk, psi_r + 2 * c0 * NH, bb, cudaMemcpyHostToDevice, s));
+    KPMGB_TRY(copy_to_device(in, psi_l + 2 * c0 * NH, bb, s));
+    KPMGB_TRY(copy_to_device(in + blk, psi_r + 2 * c0 * NH, bb, s));
     KPMGB_TRY(launch_load_block(in, in + 2 * blk, NH, (int)nb, KPMGB_PREC_FP64, nullptr, false, s));
     KPMGB_TRY(launch_load_block(in + blk, in + 3 * blk, NH, (int)nb, KPMGB_PREC_FP64, nullptr,
                                 false, s));
@@ -1142,7 +1190,7 @@ extern "C" int kpmgb_chebyshev_action(kpmgb_operator h, int64_t NH, int64_t NR, 
   KPMGB_TRY(ws.right.ensure((size_t)K * blk));
   KPMGB_TRY(ws.gemm.ensure(std::max(ws.gemm.bytes, ct.size() * sizeof(double))));
   KPMGB_TRY(ensure_sync(op, s));
-  KPMGB_CUDA(cudaMemcpyAsync(ws.psi_in.ptr, V, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(copy_to_device(ws.psi_in.ptr, V, blk, s));
   KPMGB_CUDA(cudaMemcpyAsync(ws.gemm.ptr, ct.data(), ct.size() * sizeof(double),
                              cudaMemcpyHostToDevice, s));
   KPMGB_TRY(run_chebyshev_action(op, NH, NR, ws.psi_in.as<double2>(), NC, K,
@@ -1175,7 +1223,7 @@ extern "C" int kpmgb_kpm1d_current(kpmgb_operator h, kpmgb_operator jadj, int64_
   KPMGB_TRY(ws.mu.ensure((size_t)NR * NC * 16));
   char* in = ws.psi_in.as<char>();
   // J^dagger psi (FP64, row-major) -> column-major bra
-  KPMGB_CUDA(cudaMemcpyAsync(in, psi, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(copy_to_device(in, psi, blk, s));
   KPMGB_TRY(launch_load_block(in, in + blk, NH, (int)NR, KPMGB_PREC_FP64, nullptr, false, s));
   StepArgs a;
   a.H = &jo->csr;
@@ -1221,8 +1269,8 @@ extern "C" int kpmgb_kpm3d(kpmgb_operator h, kpmgb_operator ja, kpmgb_operator j
   char* in = ws.psi_in.as<char>();
   char* sl = ws.slots.as<char>();
   auto ring = [&](int64_t n1) { return sl + (1 + (n1 - 1) % 3) * blk; };
-  KPMGB_CUDA(cudaMemcpyAsync(in, psi_l, blk, cudaMemcpyHostToDevice, s));
-  KPMGB_CUDA(cudaMemcpyAsync(in + blk, psi_r, blk, cudaMemcpyHostToDevice, s));
+  KPMGB_TRY(copy_to_device(in, psi_l, blk, s));
+  KPMGB_TRY(copy_to_device(in + blk, psi_r, blk, s));
   KPMGB_TRY(launch_load_block(in + blk, sl, NH, (int)NR, KPMGB_PREC_FP64, nullptr, false, s));
   StepArgs a;
   a.NH = NH;

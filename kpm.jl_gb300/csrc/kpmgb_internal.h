@@ -263,12 +263,41 @@ int launch_kpm1d_cluster(const DeviceCSR& H, int64_t NH, int NR, int64_t NC, boo
                          const double* mom_scale, double growth_limit, unsigned* status,
                          cudaStream_t s);
 
-// Launch shape of the persistent ensemble kernel (chosen by its autotuner):
-// threads per CTA and CSR rows or the padded-row float-float kernel.
+// Launch shape of the ensemble kernels (chosen by their autotuner): threads
+// per CTA, CSR rows or padded float-float rows, and the schedule -- rows == 0:
+// one persistent launch, each CTA runs whole members; rows > 0: one launch
+// per recurrence step over the stacked operator, each CTA takes at most
+// `rows` rows of one member and the last CTA of a member to finish sums the
+// member's partial dots.
 struct EnsembleShape {
   int threads = 1024;
   bool padded = false;
+  int rows = 0;
 };
+
+// Tables of an ensemble call (kpmgb_ensemble.cu): the segment table on the
+// host and on the device, the persistent kernel's work order and counter,
+// and scratch for the per-step kernel's block table and partial dots
+// (ensemble_step_scratch_bytes).
+struct EnsembleArgs {
+  const int64_t* seg_host = nullptr;
+  const int64_t* d_seg = nullptr;
+  const int* d_order = nullptr;
+  int nseg = 0;
+  unsigned* next = nullptr;
+  unsigned* status = nullptr;
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+};
+// Host -> device copy of an input block (kpmgb_hostio.cu): pinned host
+// memory of 1 MiB or more is read by a copy kernel through its device
+// address, anything else goes through cudaMemcpyAsync.
+int copy_to_device(void* dst, const void* src, size_t bytes, cudaStream_t s);
+
+size_t ensemble_step_scratch_bytes(const int64_t* seg, int nseg, int NR, int rows);
+int launch_ensemble(const DeviceCSR& H, const EnsembleArgs& e, int NR, int64_t NC, void* slot0,
+                    void* slot1, double2* mu, const double* scale, int precision, cudaStream_t s,
+                    const EnsembleShape& shape);
 
 namespace step {
 // Fixed-width padded rows of the float-float values (kpmgb_step_ffe.cu):

@@ -34,6 +34,7 @@ EXPORTED_SYMBOLS = (
     "kpmgb_kernel_launch_count",
     "kpmgb_kpm1d_noalloc",
     "kpmgb_kpm1d_ensemble",
+    "kpmgb_kpm1d_ensemble_device",
     "kpmgb_kpm1d_grad",
     "kpmgb_kubo_bastin",
     "kpmgb_dos",
@@ -100,6 +101,8 @@ def _declare(lib):
                                        C.POINTER(Kpm2dOptions), vp]
     lib.kpmgb_operator_sync.argtypes = [vp, vp]
     lib.kpmgb_kpm1d_ensemble.argtypes = [vp, i32, vp, i64, i64, vp, vp, C.POINTER(Kpm1dOptions)]
+    lib.kpmgb_kpm1d_ensemble_device.argtypes = [vp, i32, vp, i64, i64, vp, vp,
+                                                C.POINTER(Kpm1dOptions), vp]
     lib.kpmgb_kubo_bastin.argtypes = [vp, i64, i64, f64, f64, vp, i64, i64, f64, f64, vp, i64,
                                       f64, vp]
     lib.kpmgb_kpm1d_current.argtypes = [vp, vp, i64, i64, i64, vp, vp, C.POINTER(Kpm1dOptions)]

@@ -37,6 +37,7 @@ SOURCES = [
     "kpmgb_action.cu",
     "kpmgb_timing.cu",
     "kpmgb_tune.cu",
+    "kpmgb_hostio.cu",
 ]
 
 

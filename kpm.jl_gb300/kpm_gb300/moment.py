@@ -487,7 +487,7 @@ class EnsembleOperator:
 
 def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: bool = True,
                     kernel: str = "auto"):
-    """Doubling moments of many independent members in one persistent launch.
+    """Doubling moments of many independent members in one call.
 
     ``Hs``: list of (rescaled) sparse operators of any sizes, or an
     :class:`EnsembleOperator` built from them; ``psis``: list of probe blocks
@@ -495,10 +495,15 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     Equivalent to
     ``[kpm_1d(H_i, NC, NR, psi_in=psi_i) for ...]`` (``src/moment.jl:339-492``
     per member).  Returns a list of length-NC real averages, or of (NR, NC)
-    matrices with ``avg_output=False``.  ``kernel="tune"`` picks the launch
-    shape (threads per CTA; CSR or padded float-float rows) by timing the
-    candidates once per ensemble shape and device, and keeps the choice in the
-    persistent autotuning cache (``KPMGB_TUNE_CACHE``, default
+    matrices with ``avg_output=False``.
+
+    ``kernel``: ``"auto"`` (one launch per step over the stacked members,
+    padded float-float rows where the members allow them); ``"gather"`` (one
+    launch per step, CSR rows); ``"padded"`` (one launch per step, padded
+    float-float rows, at most 8 nonzeros per row); ``"single"`` (one
+    persistent launch, each CTA runs whole members); ``"tune"`` (times the
+    schedules and shapes once per ensemble shape and device and keeps the
+    choice in the persistent autotuning cache, ``KPMGB_TUNE_CACHE``, default
     ``~/.cache/kpmgb/tune.txt``).
     """
     ens = Hs if isinstance(Hs, EnsembleOperator) else None
@@ -519,10 +524,14 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     if ens is None:
         ens = EnsembleOperator(Hs)
     op, seg = ens.op, ens.seg
-    psi = np.asfortranarray(np.vstack([np.asarray(p, dtype=np.complex128) for p in psis]))
+    # one pass into the stacked column-major probe block
+    psi = np.empty((int(seg[-1]), NR), dtype=np.complex128, order="F")
+    for i, p in enumerate(psis):
+        psi[int(seg[i]):int(seg[i + 1])] = p
     out = np.empty((len(sizes), NC, NR), dtype=np.complex128)
-    if kernel not in ("auto", "tune"):
-        raise KPMArgumentError("kernel must be 'auto' or 'tune' for the ensemble")
+    if kernel not in ("auto", "tune", "gather", "padded", "single"):
+        raise KPMArgumentError("kernel must be 'auto', 'tune', 'gather', 'padded' or 'single' "
+                               "for the ensemble")
     opts = _opts1d(precision, False, kernel)
     lib = _native.load()
     rc = lib.kpmgb_kpm1d_ensemble(op.handle, len(sizes), seg.ctypes.data, NC, NR, psi.ctypes.data,
@@ -532,6 +541,36 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     if avg_output:
         return [m.sum(axis=0).real / NR for m in res]
     return res
+
+
+def kpm_1d_ensemble_device(ens: "EnsembleOperator", NC: int, psi_t, mu_t, *,
+                           precision: str = "fp64", kernel: str = "auto", stream=None) -> None:
+    """Enqueue the ensemble call on torch CUDA tensors without host copies.
+
+    ``psi_t``: complex128 tensor of shape (NR, sum NH_i) (row-contiguous, i.e.
+    the column-major stacked probe block, member i's probes in its rows);
+    ``mu_t``: complex128 (nseg, NC, NR), member i's moments mu_t[i, n, r].
+    Runs on ``stream`` (default: torch's current stream) and returns
+    immediately; :func:`sync` waits and raises deferred failures.
+    """
+    lib = _native.load()
+    NR, NH = psi_t.shape
+    nseg = len(ens.sizes)
+    for t, name in ((psi_t, "psi"), (mu_t, "mu")):
+        if not t.is_contiguous():
+            raise KPMArgumentError(f"{name} tensor must be contiguous")
+    if NH != int(ens.seg[-1]):
+        raise KPMArgumentError("psi must hold the stacked rows of every member")
+    if tuple(mu_t.shape) != (nseg, NC, NR):
+        raise KPMArgumentError(f"mu tensor must have shape ({nseg}, {NC}, {NR})")
+    if kernel not in ("auto", "tune", "gather", "padded", "single"):
+        raise KPMArgumentError("kernel must be 'auto', 'tune', 'gather', 'padded' or 'single' "
+                               "for the ensemble")
+    opts = _opts1d(precision, False, kernel)
+    rc = lib.kpmgb_kpm1d_ensemble_device(ens.op.handle, nseg, ens.seg.ctypes.data, NC, NR,
+                                         C.c_void_p(psi_t.data_ptr()), C.c_void_p(mu_t.data_ptr()),
+                                         C.byref(opts), _stream_ptr(stream))
+    _native.check(rc)
 
 
 def kpm_1d_grad(H, NC: int, psi_in, g, *, checkpoint_every: int = 0):

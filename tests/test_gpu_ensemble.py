@@ -1,7 +1,10 @@
-"""Batched ensemble (one persistent launch for many realisations) against the
-per-member kpm_1d and the oracle."""
+"""Batched ensemble (many realisations in one call) against the per-member
+kpm_1d and the oracle, for both schedules: one launch per step over CTAs of
+at most 512 rows of a member ("gather", "padded", the default "auto") and one
+persistent launch in which each CTA runs whole members ("single")."""
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 from conftest import relerr
 import kpm_gb300 as kg
@@ -24,13 +27,46 @@ def _members(rng, count, lo, hi):
     return Hs, psis
 
 
-@pytest.mark.parametrize("prec", ["fp64", "ff"])
-def test_ensemble_matches_oracle(built_lib, prec):
+KERNELS = [("fp64", "auto"), ("fp64", "gather"), ("fp64", "single"), ("ff", "auto"),
+           ("ff", "gather"), ("ff", "padded"), ("ff", "single")]
+
+
+@pytest.mark.parametrize("prec,kernel", KERNELS)
+def test_ensemble_matches_oracle(built_lib, prec, kernel):
     rng = np.random.default_rng(4)
     Hs, psis = _members(rng, 12, 6, 20)
-    got = kg.kpm_1d_ensemble(Hs, 128, psis, precision=prec, avg_output=False)
+    got = kg.kpm_1d_ensemble(Hs, 128, psis, precision=prec, avg_output=False, kernel=kernel)
     for H, psi, m in zip(Hs, psis, got):
         assert relerr(m, ko.kpm_1d_doubling(H, 128, psi)) < TOL[prec]
+
+
+@pytest.mark.parametrize("prec,kernel", KERNELS)
+def test_ensemble_members_over_many_ctas(built_lib, prec, kernel):
+    """Members of 1..10 CTAs of the per-step schedule (512 rows each), with
+    sizes at the CTA boundary (512, 513 rows: a 1-row CTA) and a 1-row member;
+    every member against the oracle, and the two schedules against each
+    other."""
+    rng = np.random.default_rng(77)
+    Hs, psis = [], []
+    for n in (2304, 512, 513, 1, 4900, 1024, 37, 1025):
+        if n == 1:
+            H = sp.csc_matrix(np.array([[0.3 + 0j]]))
+        else:
+            L = int(round(np.sqrt(n))) if n in (2304, 4900, 1024) else None
+            H = (models.square_anderson(L, W=3.0, rng=rng) / 5.6).tocsc() if L else \
+                ((models.ring(n) + sp.diags(rng.uniform(-0.5, 0.5, n))) / 2.6).tocsc()
+        Hs.append(H)
+        psis.append(ko.random_phase_vectors(rng, H.shape[0], 8))
+    got = kg.kpm_1d_ensemble(Hs, 64, psis, precision=prec, avg_output=False, kernel=kernel)
+    other = kg.kpm_1d_ensemble(Hs, 64, psis, precision=prec, avg_output=False,
+                               kernel="single" if kernel != "single" else "auto")
+    for H, psi, m, o in zip(Hs, psis, got, other):
+        assert relerr(m, ko.kpm_1d_doubling(H, 64, psi)) < TOL[prec]
+        assert relerr(m, o) < TOL[prec]
+    # the schedule is a pure function of the shape: repeated calls agree bitwise
+    again = kg.kpm_1d_ensemble(Hs, 64, psis, precision=prec, avg_output=False, kernel=kernel)
+    for m, a in zip(got, again):
+        assert np.array_equal(m, a)
 
 
 def test_ensemble_matches_single_calls(built_lib):
@@ -49,6 +85,11 @@ def test_ensemble_validation(built_lib):
         kg.kpm_1d_ensemble(Hs, 63, psis)
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d_ensemble(Hs, 64, [psis[0], psis[1][:, :4]])
+    # padded rows are float-float only
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_ensemble(Hs, 64, psis, kernel="padded")
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_ensemble(Hs, 64, psis, kernel="cluster")
 
 
 @pytest.mark.parametrize("prec", ["fp64", "ff"])
@@ -79,10 +120,11 @@ def test_ensemble_operator_reuse(built_lib):
 
 
 def test_ensemble_autotune_cache_round_trip(built_lib, tmp_path, monkeypatch):
-    """kernel="tune" times the candidate launch shapes once, writes the choice
-    to the persistent cache, and a later call (a fresh operator, as a new
-    process would build) reads it back without timing: it launches exactly as
-    many kernels as an untuned call.  Both agree with the oracle."""
+    """kernel="tune" times the candidate schedules and shapes once, writes
+    the choice to the persistent cache, and later calls (fresh operators, as
+    a new process would build) read it back without timing: they launch the
+    same number of kernels as each other and fewer than the tuning call.  All
+    agree with the oracle."""
     cache = tmp_path / "tune.txt"
     monkeypatch.setenv("KPMGB_TUNE_CACHE", str(cache))
     rng = np.random.default_rng(19)
@@ -100,21 +142,24 @@ def test_ensemble_autotune_cache_round_trip(built_lib, tmp_path, monkeypatch):
                                    avg_output=False, kernel="tune")
         n_cached = kg.kernel_launch_count() - n0
         n0 = kg.kernel_launch_count()
-        kg.kpm_1d_ensemble(kg.EnsembleOperator(Hs), 96, psis, precision=prec, avg_output=False)
-        n_plain = kg.kernel_launch_count() - n0
+        kg.kpm_1d_ensemble(kg.EnsembleOperator(Hs), 96, psis, precision=prec, avg_output=False,
+                           kernel="tune")
+        n_third = kg.kernel_launch_count() - n0
         assert n_tuned > n_cached
-        assert n_cached == n_plain
+        assert n_cached == n_third
         for m, a, r in zip(got, again, ref):
             assert np.array_equal(m, a)
             assert relerr(m, r) < TOL[prec]
 
 
-@pytest.mark.parametrize("threads", [256, 512, 1024])
-def test_ensemble_padded_kernel_matches_oracle(built_lib, tmp_path, monkeypatch, threads):
-    """The padded-row float-float ensemble kernel at every tuned CTA size
-    (forced through a cache entry): parity with the oracle; the doubling
-    moments' imaginary parts are exactly 0 (Hermitian members)."""
-    rng = np.random.default_rng(23 + threads)
+@pytest.mark.parametrize("shape", ["256,1,0", "512,1,0", "1024,1,0", "256,1,256", "256,1,2048",
+                                   "256,0,1024"])
+def test_ensemble_tuned_shapes_match_oracle(built_lib, tmp_path, monkeypatch, shape):
+    """Every tuned shape (threads per CTA, padded rows, rows per CTA of the
+    per-step schedule or 0 for the persistent one; forced through a cache
+    entry): parity with the oracle; the doubling moments' imaginary parts are
+    exactly 0 with padded rows (Hermitian members)."""
+    rng = np.random.default_rng(23 + sum(map(int, shape.split(","))))
     Hs, psis = _members(rng, 16, 6, 20)
     ens = kg.EnsembleOperator(Hs)
     NH, nnz = ens.op.shape[0], ens.op.nnz
@@ -124,8 +169,37 @@ def test_ensemble_padded_kernel_matches_oracle(built_lib, tmp_path, monkeypatch,
     kg.kpm_1d_ensemble(ens, 64, psis, precision="ff", kernel="tune")
     key = [l.rsplit(" ", 1)[0] for l in cache.read_text().splitlines()
            if l.startswith("ensemble|") and f"|NH={NH}|nnz={nnz}|" in l and "|prec=1" in l][0]
-    cache.write_text(f"{key} {threads},1\n")
+    cache.write_text(f"{key} {shape}\n")
+    n0 = kg.kernel_launch_count()
     got = kg.kpm_1d_ensemble(ens, 128, psis, precision="ff", avg_output=False, kernel="tune")
+    launches = kg.kernel_launch_count() - n0
+    # the per-step schedule launches once per step (64), the persistent once
+    assert (launches > 64) == (not shape.endswith(",0"))
     for H, p, m in zip(Hs, psis, got):
         assert relerr(m, ko.kpm_1d_doubling(H, 128, p)) < TOL["ff"]
-        assert np.all(m.imag == 0.0)
+        if shape.split(",")[1] == "1":
+            assert np.all(m.imag == 0.0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_ensemble_device_entry_matches_host_entry(built_lib, prec):
+    """kpmgb_kpm1d_ensemble_device on torch tensors (stacked column-major
+    probes in, (nseg, NC, NR) moments out) gives the host entry's moments
+    bitwise."""
+    import torch
+    rng = np.random.default_rng(52)
+    Hs, psis = _members(rng, 10, 20, 40)
+    ens = kg.EnsembleOperator(Hs)
+    NC, NR = 96, 8
+    host = kg.kpm_1d_ensemble(ens, NC, psis, precision=prec, avg_output=False)
+    stacked = np.vstack(psis)                     # (sum NH, NR)
+    psi_t = torch.from_numpy(np.ascontiguousarray(stacked.T)).cuda()
+    mu_t = torch.zeros((len(Hs), NC, NR), dtype=torch.complex128, device="cuda")
+    kg.kpm_1d_ensemble_device(ens, NC, psi_t, mu_t, precision=prec)
+    kg.sync(ens.op)
+    torch.cuda.synchronize()
+    got = mu_t.cpu().numpy()
+    for i, m in enumerate(host):
+        assert np.array_equal(got[i].T, m)
+    with pytest.raises(kg.KPMArgumentError):
+        kg.kpm_1d_ensemble_device(ens, NC, psi_t, mu_t[:, :64], precision=prec)

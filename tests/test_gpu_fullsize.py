@@ -9,7 +9,8 @@ rebuilt from seeds by fullsize_cases.py):
       blocked NumPy kpm_2d (src/moment.jl:987-1088) for the FP64 and the
       split tensor-core contraction, and sigma_xy at 201 Fermi energies
       against the oracle's kubo_bastin_cond;
-  c4  all 256 ensemble members against the oracle's doubling recurrence;
+  c4  all 256 ensemble members against the oracle's doubling recurrence
+      (FP64 and float-float per-step schedule, float-float persistent);
   c5  graphene 128x128, NC=1024, NR=16, checkpoints every 64: the adjoint
       gradient of the DOS-window loss along an onsite and a hopping direction
       against the oracle's exact directional derivative and against central
@@ -123,6 +124,7 @@ def test_c4_every_member_against_oracle():
     ens = kg.EnsembleOperator(Hs)
     got = kg.kpm_1d_ensemble(ens, 512, psis, avg_output=False)
     got_ff = kg.kpm_1d_ensemble(ens, 512, psis, avg_output=False, precision="ff")
+    got_ps = kg.kpm_1d_ensemble(ens, 512, psis, avg_output=False, precision="ff", kernel="single")
     ctx = mp.get_context("spawn")
     with ctx.Pool(max(1, min(16, os.cpu_count() or 1))) as pool:
         refs = pool.starmap(ko.kpm_1d_doubling, [(H, 512, p) for H, p in zip(Hs, psis)],
@@ -130,6 +132,7 @@ def test_c4_every_member_against_oracle():
     for i in range(256):
         assert relerr(got[i], refs[i]) < 1e-12, i
         assert relerr(got_ff[i], refs[i]) < 1e-9, i
+        assert relerr(got_ps[i], refs[i]) < 1e-9, i
 
 
 def test_c5_dos_window_gradient_against_oracle():

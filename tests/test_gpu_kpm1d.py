@@ -560,3 +560,28 @@ def test_cluster_kernel_growth_and_capacity():
     ok = (models.square_anderson(12, W=1.0, rng=rng) / 5.0).tocsc()
     got = kg.kpm_1d(ok, 32, 4, psi_in=psi, avg_output=False, kernel="cluster")
     assert relerr(got, ko.kpm_1d_doubling(ok, 32, psi)) < TOL["fp64"]
+
+
+@pytest.mark.parametrize("lr", [False, True])
+def test_pinned_host_probes_match_pageable(lr):
+    """Probe blocks in pinned host memory are read by the copy kernel (from
+    1 MiB up), pageable ones by cudaMemcpyAsync: the moments agree bitwise."""
+    import torch
+    rng = np.random.default_rng(61)
+    H = (models.square_anderson(96, W=2.0, rng=rng) / 5.1).tocsc()
+    NH, NR, NC = H.shape[0], 16, 64
+    psi = ko.random_phase_vectors(rng, NH, NR)          # 2.4 MB
+    op = kg.GB300Operator(H)
+    pinned = torch.empty((NR, NH), dtype=torch.complex128, pin_memory=True)
+    pinned.numpy()[...] = psi.T
+    host_psi = pinned.numpy().T
+    a = np.zeros((NR, NC), dtype=np.complex128)
+    b = np.zeros((NR, NC), dtype=np.complex128)
+    if lr:
+        kg.kpm_1d_bang(op, NC, NR, NH, a, np.asfortranarray(psi), np.asfortranarray(psi))
+        kg.kpm_1d_bang(op, NC, NR, NH, b, host_psi, host_psi)
+    else:
+        kg.kpm_1d_bang(op, NC, NR, NH, a, np.asfortranarray(psi))
+        kg.kpm_1d_bang(op, NC, NR, NH, b, host_psi)
+    assert np.array_equal(a, b)
+    assert relerr(a, ko.kpm_1d_lr(H, NC, psi, psi) if lr else ko.kpm_1d_doubling(H, NC, psi)) < 1e-12
