@@ -443,9 +443,48 @@ struct EnsStep {
   double2* part;       // [CTA][2][NR] partial dots
   const int* ecol;     // padded rows (ELL kernels)
   const void* evalv;
-  int ew, w;
+  int ew;
   int n;               // recurrence step 1 .. NC/2
 };
+
+// Row r of y = alpha H x - [!first] z over W padded slots whose column
+// indices and values are already in registers (jj, hv); returns y and x[r].
+template <bool REALH, int W>
+__device__ __forceinline__ void ell_row_staged(
+    const int (&jj)[W], const typename std::conditional<REALH, float2, float4>::type (&hv)[W],
+    const float4* x, float4* y, int64_t r, int NR, int cc, float alpha, bool first, float4& xo,
+    float4& yv) {
+  const int64_t idx = r * NR + cc;
+  const float4 zz = first ? make_float4(0.f, 0.f, 0.f, 0.f) : y[idx];
+  xo = x[idx];
+  float4 xg[W];
+#pragma unroll
+  for (int u = 0; u < W; ++u) xg[u] = x[(int64_t)jj[u] * NR + cc];
+  float R = 0.f, M = 0.f;
+#pragma unroll
+  for (int u = 0; u < W; ++u) {
+    R = __fadd_rn(R, ens_habs(hv[u]));
+    M = fmaxf(M, fmaxf(fabsf(xg[u].x), fabsf(xg[u].z)));
+  }
+  const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+  const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+  float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
+#pragma unroll
+  for (int u = 0; u < W; ++u) ens_ffmac(Ar, cr, Ai, ci, hv[u], xg[u]);
+  const float sr = __fsub_rn(Ar, sig), si = __fsub_rn(Ai, sig);
+  const float2 yr = ens_epi(sr, cr, alpha, !first, zz.x, zz.y);
+  const float2 yi = ens_epi(si, ci, alpha, !first, zz.z, zz.w);
+  yv = make_float4(yr.x, yr.y, yi.x, yi.y);
+  y[idx] = yv;
+}
+
+__device__ __forceinline__ float2 shfl_v(unsigned m, float2 v, int src, int width) {
+  return make_float2(__shfl_sync(m, v.x, src, width), __shfl_sync(m, v.y, src, width));
+}
+__device__ __forceinline__ float4 shfl_v(unsigned m, float4 v, int src, int width) {
+  return make_float4(__shfl_sync(m, v.x, src, width), __shfl_sync(m, v.y, src, width),
+                     __shfl_sync(m, v.z, src, width), __shfl_sync(m, v.w, src, width));
+}
 
 // One doubling step n of every member: CTA b applies the step to its rows
 // (y = H x for n = 1, else y = 2 H x - y in place; x and y alternate between
@@ -453,7 +492,12 @@ struct EnsStep {
 // and stores them; the last CTA of the member to finish (ticket counter) adds
 // the member's partials in CTA order and writes mu_{2n-2}, mu_{2n-1} by the
 // doubling identities.  The moments are independent of the CTA schedule.
-template <bool FF, bool REALH, int LPR, bool ELL>
+// W = 0: CSR rows; W = 4..8: float-float padded rows with W live slots,
+// fetched one row ahead: lane k of a row's lane group loads slots k, k + LPR,
+// ... of the next row while the current row is computed, and the group's
+// lanes exchange them with shuffles, so the gathers of a row wait on no
+// index load.
+template <bool FF, bool REALH, int LPR, int W>
 __global__ void __launch_bounds__(kEnsStepThreads) k_ensemble_step(EnsParams p, EnsStep q) {
   asm volatile("griddepcontrol.wait;" ::: "memory");
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -471,51 +515,84 @@ __global__ void __launch_bounds__(kEnsStepThreads) k_ensemble_step(EnsParams p, 
   void* xv = odd ? p.slot0 : p.slot1;
   void* yv = odd ? p.slot1 : p.slot0;
   double2 d0 = make_double2(0.0, 0.0), d1 = make_double2(0.0, 0.0);
-  if (cc < p.NR) {
-    if constexpr (ELL) {
-      using HV = typename std::conditional<REALH, float2, float4>::type;
-      const HV* __restrict__ eval = static_cast<const HV*>(q.evalv);
-      float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
-      for (int64_t r = rows.x + g; r < rows.y; r += groups) {
+  if constexpr (W > 0) {
+    using HV = typename std::conditional<REALH, float2, float4>::type;
+    const HV* __restrict__ eval = static_cast<const HV*>(q.evalv);
+    const int* __restrict__ ecol = q.ecol;
+    constexpr int SL = (W + LPR - 1) / LPR;  // slots held per lane
+    const unsigned gmask =
+        LPR == 32 ? 0xffffffffu : (((1u << LPR) - 1u) << (lane & ~(LPR - 1)));
+    const bool active = cc < p.NR;
+    const float4* x = static_cast<const float4*>(xv);
+    float4* y = static_cast<float4*>(yv);
+    float S0 = 0.f, C0 = 0.f, S1 = 0.f, C1 = 0.f;
+    int pc[SL];
+    HV pv[SL];
+    auto fetch = [&](int64_t rr) {
+#pragma unroll
+      for (int s = 0; s < SL; ++s) {
+        const int k = cc + s * LPR;
+        if (k < W) {
+          pc[s] = __ldg(ecol + rr * q.ew + k);
+          pv[s] = __ldg(eval + rr * q.ew + k);
+        }
+      }
+    };
+#pragma unroll
+    for (int s = 0; s < SL; ++s) {
+      pc[s] = 0;
+      if constexpr (REALH) pv[s] = make_float2(0.f, 0.f);
+      else pv[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    int64_t r = rows.x + g;
+    if (r < rows.y) fetch(r);
+    for (; r < rows.y; r += groups) {
+      int jj[W];
+      HV hv[W];
+#pragma unroll
+      for (int u = 0; u < W; ++u) {
+        jj[u] = __shfl_sync(gmask, pc[u / LPR], u % LPR, LPR);
+        hv[u] = shfl_v(gmask, pv[u / LPR], u % LPR, LPR);
+      }
+      if (r + groups < rows.y) fetch(r + groups);
+      if (active) {
         float4 xo, yo;
-        ell_row<REALH>(q.ecol, eval, q.ew, q.w, static_cast<const float4*>(xv),
-                       static_cast<float4*>(yv), r, p.NR, cc, first ? 1.f : 2.f, first, xo, yo);
+        ell_row_staged<REALH, W>(jj, hv, x, y, r, p.NR, cc, first ? 1.f : 2.f, first, xo, yo);
         ffdacc(S0, C0, xo.x, xo.y, xo.x, xo.y);
         ffdacc(S0, C0, xo.z, xo.w, xo.z, xo.w);
         ffdacc(S1, C1, xo.x, xo.y, yo.x, yo.y);
         ffdacc(S1, C1, xo.z, xo.w, yo.z, yo.w);
       }
-      d0.x = ff::join(S0, C0);
-      d1.x = ff::join(S1, C1);
-    } else {
-      float S[3] = {0.f, 0.f, 0.f}, C[3] = {0.f, 0.f, 0.f};
-      const double alpha = first ? 1.0 : 2.0;
-      for (int64_t r = rows.x + g; r < rows.y; r += groups) {
-        double2 xo, yo;
-        float4 xf, yf;
-        row_value<FF, REALH, 8>(p, xv, r, cc, (float)alpha, alpha, !first, yv, yv, xo, yo, xf,
-                                yf);
-        if constexpr (!FF) {
-          d0.x = fma(xo.x, xo.x, d0.x);
-          d0.x = fma(xo.y, xo.y, d0.x);
-          d1.x = fma(xo.x, yo.x, d1.x);
-          d1.x = fma(xo.y, yo.y, d1.x);
-          d1.y = fma(xo.x, yo.y, d1.y);
-          d1.y = fma(-xo.y, yo.x, d1.y);
-        } else {
-          ffdacc(S[0], C[0], xf.x, xf.y, xf.x, xf.y);
-          ffdacc(S[0], C[0], xf.z, xf.w, xf.z, xf.w);
-          ffdacc(S[1], C[1], xf.x, xf.y, yf.x, yf.y);
-          ffdacc(S[1], C[1], xf.z, xf.w, yf.z, yf.w);
-          ffdacc(S[2], C[2], xf.x, xf.y, yf.z, yf.w);
-          ffdacc(S[2], C[2], -xf.z, -xf.w, yf.x, yf.y);
-        }
+    }
+    d0.x = ff::join(S0, C0);
+    d1.x = ff::join(S1, C1);
+  } else if (cc < p.NR) {
+    float S[3] = {0.f, 0.f, 0.f}, C[3] = {0.f, 0.f, 0.f};
+    const double alpha = first ? 1.0 : 2.0;
+    for (int64_t r = rows.x + g; r < rows.y; r += groups) {
+      double2 xo, yo;
+      float4 xf, yf;
+      row_value<FF, REALH, 8>(p, xv, r, cc, (float)alpha, alpha, !first, yv, yv, xo, yo, xf, yf);
+      if constexpr (!FF) {
+        d0.x = fma(xo.x, xo.x, d0.x);
+        d0.x = fma(xo.y, xo.y, d0.x);
+        d1.x = fma(xo.x, yo.x, d1.x);
+        d1.x = fma(xo.y, yo.y, d1.x);
+        d1.y = fma(xo.x, yo.y, d1.y);
+        d1.y = fma(-xo.y, yo.x, d1.y);
+      } else {
+        ffdacc(S[0], C[0], xf.x, xf.y, xf.x, xf.y);
+        ffdacc(S[0], C[0], xf.z, xf.w, xf.z, xf.w);
+        ffdacc(S[1], C[1], xf.x, xf.y, yf.x, yf.y);
+        ffdacc(S[1], C[1], xf.z, xf.w, yf.z, yf.w);
+        ffdacc(S[2], C[2], xf.x, xf.y, yf.z, yf.w);
+        ffdacc(S[2], C[2], -xf.z, -xf.w, yf.x, yf.y);
       }
-      if constexpr (FF) {
-        d0.x = ff::join(S[0], C[0]);
-        d1.x = ff::join(S[1], C[1]);
-        d1.y = ff::join(S[2], C[2]);
-      }
+    }
+    if constexpr (FF) {
+      d0.x = ff::join(S[0], C[0]);
+      d1.x = ff::join(S[1], C[1]);
+      d1.y = ff::join(S[2], C[2]);
     }
   }
 #pragma unroll
@@ -615,22 +692,34 @@ void* pick_ensemble(bool ff, bool real, int NR) {
   return nullptr;
 }
 
-template <bool FF, bool REALH, bool ELL>
+template <bool FF, bool REALH, int W>
 void* pick_step_lanes(int NR) {
   switch (lanes_for(NR)) {
-    case 1: return (void*)k_ensemble_step<FF, REALH, 1, ELL>;
-    case 2: return (void*)k_ensemble_step<FF, REALH, 2, ELL>;
-    case 4: return (void*)k_ensemble_step<FF, REALH, 4, ELL>;
-    case 8: return (void*)k_ensemble_step<FF, REALH, 8, ELL>;
-    case 16: return (void*)k_ensemble_step<FF, REALH, 16, ELL>;
-    default: return (void*)k_ensemble_step<FF, REALH, 32, ELL>;
+    case 1: return (void*)k_ensemble_step<FF, REALH, 1, W>;
+    case 2: return (void*)k_ensemble_step<FF, REALH, 2, W>;
+    case 4: return (void*)k_ensemble_step<FF, REALH, 4, W>;
+    case 8: return (void*)k_ensemble_step<FF, REALH, 8, W>;
+    case 16: return (void*)k_ensemble_step<FF, REALH, 16, W>;
+    default: return (void*)k_ensemble_step<FF, REALH, 32, W>;
   }
 }
 
-void* pick_ensemble_step(bool ff, bool real, bool ell, int NR) {
-  if (ell) return real ? pick_step_lanes<true, true, true>(NR) : pick_step_lanes<true, false, true>(NR);
-  if (ff) return real ? pick_step_lanes<true, true, false>(NR) : pick_step_lanes<true, false, false>(NR);
-  return real ? pick_step_lanes<false, true, false>(NR) : pick_step_lanes<false, false, false>(NR);
+template <bool REALH>
+void* pick_step_ell(int NR, int max_row) {
+  switch (max_row <= 4 ? 4 : max_row) {
+    case 4: return pick_step_lanes<true, REALH, 4>(NR);
+    case 5: return pick_step_lanes<true, REALH, 5>(NR);
+    case 6: return pick_step_lanes<true, REALH, 6>(NR);
+    case 7: return pick_step_lanes<true, REALH, 7>(NR);
+    default: return pick_step_lanes<true, REALH, 8>(NR);
+  }
+}
+
+// ell: padded rows of at most 8 nonzeros (float-float)
+void* pick_ensemble_step(bool ff, bool real, bool ell, int NR, int max_row) {
+  if (ell) return real ? pick_step_ell<true>(NR, max_row) : pick_step_ell<false>(NR, max_row);
+  if (ff) return real ? pick_step_lanes<true, true, 0>(NR) : pick_step_lanes<true, false, 0>(NR);
+  return real ? pick_step_lanes<false, true, 0>(NR) : pick_step_lanes<false, false, 0>(NR);
 }
 
 size_t align16(size_t b) { return (b + 15) & ~(size_t)15; }
@@ -678,7 +767,6 @@ int launch_ensemble_steps(const DeviceCSR& H, const EnsembleArgs& e, EnsParams p
   q.ecol = H.ell_col;
   q.evalv = H.ell_val;
   q.ew = H.ell_w;
-  q.w = H.max_row_nnz;
   KPMGB_CUDA(cudaMemcpyAsync((void*)q.blk, blk.data(), blk.size() * sizeof(int2),
                              cudaMemcpyHostToDevice, s));
   KPMGB_CUDA(cudaMemcpyAsync((void*)q.blk_seg, bseg.data(), bseg.size() * sizeof(int),
@@ -686,7 +774,7 @@ int launch_ensemble_steps(const DeviceCSR& H, const EnsembleArgs& e, EnsParams p
   KPMGB_CUDA(cudaMemcpyAsync((void*)q.seg_b0, b0.data(), b0.size() * sizeof(int),
                              cudaMemcpyHostToDevice, s));
   KPMGB_CUDA(cudaMemsetAsync(q.ticket, 0, (size_t)nseg * sizeof(unsigned), s));
-  void* fn = pick_ensemble_step(ff, H.is_real != 0, ell, p.NR);
+  void* fn = pick_ensemble_step(ff, H.is_real != 0, ell, p.NR, H.max_row_nnz);
   // programmatic dependent launch on created streams: step n+1's CTAs are
   // scheduled while step n drains and wait (griddepcontrol.wait) for its
   // completion
