@@ -11,21 +11,27 @@
 // p_i = d_i 2^(-8i) (exact), so that
 //     v = 2^(e-7) * sum_i p_i          (rounding <= 2^-39 of the row max)
 // and every plane product carries its own weight.  The 15 plane pairs with
-// i + j <= 4 feed four TMEM accumulators (128 x 64 FP32 each): level 0
-// (p_0 q_0, integers), level 1 (p_0 q_1 + p_1 q_0, multiples of 2^-8),
-// level 2 (multiples of 2^-16) and levels 3-4 together.  Over a chunk of 256
-// K' elements the first three stay below 2^22, 2^15 and 2^8, i.e. within 24
-// significant bits of their granularity, and are therefore exact in the
-// tensor core's FP32 accumulation; the fourth stays below ~1, so its FP32
-// rounding is below 2^-24 (2^-38 of one leading digit product).  After each
-// chunk the epilogue warps fold the four accumulators into one int64 per
-// output in units of 2^-24 (exact for levels 0-3, level 4 rounded to 2^-25)
-// and the chunk accumulators are reused.  A K split holds at most 2^24 K'
-// elements, so the int64 stays below 2^62.
+// i + j <= 4 feed five TMEM accumulators (128 x 48 FP32 each), one per digit
+// level i + j: level l holds multiples of 2^-8l and stays below
+// (l+1) 2^22 of them over a chunk of 256 K' elements, so levels 0-3
+// accumulate exactly in the tensor core's FP32 and level 4 (2^-32 of the
+// leading products) rounds at most to its own last bit.  After each chunk the
+// epilogue warps fold the five accumulators into one int64 per output in
+// units of 2^-24 (exact for levels 0-3, level 4 rounded to 2^-25) and the
+// chunk accumulators are reused.  A K split holds at most 2^24 K' elements,
+// so the int64 stays below 2^62.
+//
+// MMA shape: the five B planes of a stage lie one after another along N, so
+// A plane i meets B planes 0..4-i in ONE tcgen05.mma of N = 48 (5 - i)
+// whose output columns land on the accumulators of levels i..4 (the level
+// blocks are adjacent in TMEM): 5 MMAs per 16 K' elements instead of 15, with
+// N up to 240 (the tensor pipe's issue cost per instruction was the limit of
+// the 15 x N=64 form: 77 % tc-pipe activity at 40 % tensor math).
 //
 // Data movement: the digit planes are pre-tiled in global memory in the
-// canonical no-swizzle K-major UMMA layout, so each pipeline stage is two
-// bulk copies (cp.async.bulk, 40 KiB of A planes and 20 KiB of B planes)
+// canonical no-swizzle K-major UMMA layout, each k-tile's five planes of one
+// operand as one (5 x rows) x 32 block, so each pipeline stage is two bulk
+// copies (cp.async.bulk, 40 KiB of A planes and 15 KiB of B planes)
 // completed on an mbarrier.  Warp roles per CTA: 0 producer, 1 MMA issuer
 // (one thread), 2-5 epilogue (one TMEM lane each).  All waits are bounded.
 #include <cuda_bf16.h>
@@ -42,20 +48,20 @@ namespace kpmgb {
 namespace {
 
 constexpr int TC_M = 128;      // A rows per tile
-constexpr int TC_N = 64;       // B rows per tile
+constexpr int TC_N = 48;       // B rows per tile
 constexpr int TC_KT = 32;      // real K' elements per k-tile
 constexpr int TC_SLICES = 5;   // digit planes per operand
-constexpr int TC_ACC = 4;      // TMEM accumulators: levels 0, 1, 2 and 3-4
+constexpr int TC_ACC = 5;      // TMEM accumulators: one per digit level 0..4
 constexpr int TC_CHUNK = 8;    // k-tiles per exact chunk (256 K' elements)
-constexpr int TC_STAGES = 3;
+constexpr int TC_STAGES = 4;
 constexpr uint32_t A_TILE = TC_M * TC_KT * 2;  // 8 KiB per plane
-constexpr uint32_t B_TILE = TC_N * TC_KT * 2;  // 4 KiB per plane
+constexpr uint32_t B_TILE = TC_N * TC_KT * 2;  // 3 KiB per plane
 constexpr uint32_t A_STAGE = A_TILE * TC_SLICES;
 constexpr uint32_t B_STAGE = B_TILE * TC_SLICES;
 constexpr uint32_t STAGE_BYTES = A_STAGE + B_STAGE;
-constexpr int TMEM_COLS = 512;  // 2 buffers x 4 accumulators x 64 columns
+constexpr int TMEM_COLS = 512;  // 2 buffers of 256 columns (5 levels x 48 used)
 constexpr int64_t kMaxKtPerSplit = (int64_t)1 << 19;  // 2^24 K' elements: int64 headroom
-constexpr int TMEM_BUF = TC_ACC * TC_N;
+constexpr int TMEM_BUF = 256;
 constexpr int kSpin = 1 << 22;
 constexpr int kThreadsTC = 192;  // 6 warps
 
@@ -103,15 +109,21 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr) {
   d |= (uint64_t)1 << 46;
   return d;
 }
-// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
-                            ((uint32_t)(TC_M >> 4) << 24);
+// kind::f16 instruction descriptor: D = F32, A = B = BF16, both K-major,
+// M = TC_M, N = n (a multiple of 16 up to 256).
+__host__ __device__ constexpr uint32_t idesc_for(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(TC_M >> 4) << 24);
+}
+static_assert(TC_N * TC_SLICES <= 256 && (TC_N * TC_SLICES) % 16 == 0 && TC_N % 16 == 0,
+              "one MMA covers up to five B planes");
 
-__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                     uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
       " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(kIdesc), "r"(acc)
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
       : "memory");
 }
 __device__ __forceinline__ void umma_commit(uint32_t bar) {
@@ -119,22 +131,24 @@ __device__ __forceinline__ void umma_commit(uint32_t bar) {
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
       : "memory");
 }
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+// 16 consecutive TMEM columns of this thread's lane (no wait).
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* v) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
       : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
         "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-        "=r"(v[14]), "=r"(v[15]), "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]),
-        "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]), "=r"(v[25]),
-        "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        "=r"(v[14]), "=r"(v[15])
       : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // --------------------------------------------------------------- pre-passes
-// Byte offset of element (r, k) inside a ROWS x TC_KT tile (canonical layout).
+// Byte offset of element (r, k) inside a ROWS x TC_KT tile (canonical layout);
+// the five planes of a k-tile form one (5 ROWS) x TC_KT tile, plane i in rows
+// i ROWS .. (i+1) ROWS - 1.
 template <int ROWS>
 __host__ __device__ __forceinline__ uint32_t tile_off(int r, int k) {
   return (uint32_t)((k >> 4) * (ROWS * 32) + (r >> 3) * 256 + ((k >> 3) & 1) * 128 + (r & 7) * 16 +
@@ -241,13 +255,13 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
     const int kin = (int)(kp0 % TC_KT);
     auto store = [&](int row, float (&dd)[8][TC_SLICES]) {
       const int tile = row / ROWS, r = row % ROWS;
-      uint8_t* tbase = planes + ((size_t)(tile * ktiles + kt) * TC_SLICES) * TILE;
+      uint8_t* tbase = planes + (size_t)(tile * ktiles + kt) * (TC_SLICES * TILE);
 #pragma unroll
       for (int i = 0; i < TC_SLICES; ++i) {
         __nv_bfloat16 h[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(ldexpf(dd[q][i], -8 * i));
-        *reinterpret_cast<uint4*>(tbase + (size_t)i * TILE + tile_off<ROWS>(r, kin)) =
+        *reinterpret_cast<uint4*>(tbase + tile_off<TC_SLICES * ROWS>(i * ROWS + r, kin)) =
             *reinterpret_cast<const uint4*>(h);
       }
     };
@@ -272,16 +286,16 @@ __global__ void k_zero_rows(uint8_t* planes, int nrows, int rows_pad, int64_t kt
     const int64_t kt = q / (TC_KT / 8);
     const int kin = (int)(q % (TC_KT / 8)) * 8;
     const int tile = row / ROWS, r = row % ROWS;
-    uint8_t* tbase = planes + ((size_t)(tile * ktiles + kt) * TC_SLICES) * TILE;
-    *reinterpret_cast<uint4*>(tbase + (size_t)i * TILE + tile_off<ROWS>(r, kin)) =
+    uint8_t* tbase = planes + (size_t)(tile * ktiles + kt) * (TC_SLICES * TILE);
+    *reinterpret_cast<uint4*>(tbase + tile_off<TC_SLICES * ROWS>(i * ROWS + r, kin)) =
         make_uint4(0, 0, 0, 0);
   }
 }
 
 // --------------------------------------------------------------- GEMM
 struct TcArgs {
-  const uint8_t* A;      // planes [mtiles][ktiles][4][A_TILE]
-  const uint8_t* B;      // planes [ntiles][ktiles][4][B_TILE]
+  const uint8_t* A;      // planes [mtiles][ktiles][A_STAGE]
+  const uint8_t* B;      // planes [ntiles][ktiles][B_STAGE]
   int64_t ktiles;
   int64_t kt_per_split;
   int nr, ncols;         // real rows of A, real rows of B (2 nl)
@@ -337,12 +351,10 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
         }
         const int64_t kt = kt0 + i;
         bar_expect(full0 + 8 * s, STAGE_BYTES);
-        bulk_copy(sm0 + s * STAGE_BYTES,
-                  p.A + ((size_t)(mt * p.ktiles + kt) * TC_SLICES) * A_TILE, A_STAGE,
+        bulk_copy(sm0 + s * STAGE_BYTES, p.A + (size_t)(mt * p.ktiles + kt) * A_STAGE, A_STAGE,
                   full0 + 8 * s);
-        bulk_copy(sm0 + s * STAGE_BYTES + A_STAGE,
-                  p.B + ((size_t)(nt * p.ktiles + kt) * TC_SLICES) * B_TILE, B_STAGE,
-                  full0 + 8 * s);
+        bulk_copy(sm0 + s * STAGE_BYTES + A_STAGE, p.B + (size_t)(nt * p.ktiles + kt) * B_STAGE,
+                  B_STAGE, full0 + 8 * s);
       }
     }
   } else if (warp == 1) {
@@ -357,7 +369,6 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        bool started[TC_ACC] = {false, false, false, false};
         const int64_t rem = nkt - c * TC_CHUNK;
         const int64_t tiles = rem < TC_CHUNK ? rem : TC_CHUNK;
         for (int64_t t = 0; t < tiles; ++t, ++i) {
@@ -370,16 +381,18 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
           const uint32_t a0 = sm0 + s * STAGE_BYTES, b0 = a0 + A_STAGE;
 #pragma unroll
           for (int ks = 0; ks < TC_KT / 16; ++ks) {
+            // B planes 0..4 of this K step: rows 0 .. 5 TC_N - 1 of one tile
+            const uint64_t bd = umma_desc(b0 + ks * (TC_SLICES * TC_N * 32));
 #pragma unroll
-            for (int ia = 0; ia < TC_SLICES; ++ia)
-#pragma unroll
-              for (int ib = 0; ib < TC_SLICES - ia; ++ib) {
-                const int acc = ia + ib < 3 ? ia + ib : 3;
-                const uint64_t ad = umma_desc(a0 + ia * A_TILE + ks * (TC_M * 32));
-                const uint64_t bd = umma_desc(b0 + ib * B_TILE + ks * (TC_N * 32));
-                umma(tmem + buf * TMEM_BUF + acc * TC_N, ad, bd, started[acc] ? 1u : 0u);
-                started[acc] = true;
-              }
+            for (int ia = 0; ia < TC_SLICES; ++ia) {
+              // A plane ia x B planes 0 .. 4-ia -> level blocks ia .. 4; the
+              // chunk's first MMA (ia = 0 covers every block) initialises
+              const uint64_t ad =
+                  umma_desc(a0 + ks * (TC_SLICES * TC_M * 32) + ia * (TC_M / 8) * 256);
+              const bool init = t == 0 && ks == 0 && ia == 0;
+              umma(tmem + buf * TMEM_BUF + ia * TC_N, ad, bd, idesc_for(TC_N * (TC_SLICES - ia)),
+                   init ? 0u : 1u);
+            }
           }
           umma_commit(empty0 + 8 * s);  // stage free once these MMAs retire
         }
@@ -404,20 +417,21 @@ __global__ void __launch_bounds__(kThreadsTC, 1) k_contract_tc(TcArgs p) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int ac = 0; ac < TC_ACC; ++ac) {
-        // in units of 2^-24: level 0 is an integer, level 1 a multiple of
-        // 2^-8, level 2 of 2^-16 (all exact), levels 3-4 (|.| < ~1.01, so
-        // below 2^25 units) rounded to 2^-24
-        const float unit = ac == 0 ? 1.f : (ac == 1 ? 256.f : (ac == 2 ? 65536.f : 16777216.f));
-        const int shift = 24 - 8 * ac;
+        // in units of 2^-24: level l < 4 is a multiple of 2^-8l below
+        // (l+1) 2^22 of them (exact), level 4 (below 5 2^-10) is rounded to
+        // 2^-24
+        const float unit = ac == 4 ? 16777216.f : (float)(1 << (8 * ac));
+        const int shift = ac == 4 ? 0 : 24 - 8 * ac;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          uint32_t v[32];
-          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + buf * TMEM_BUF + ac * TC_N + h * 32, v);
+        for (int h = 0; h < TC_N / 16; ++h) {
+          uint32_t v[16];
+          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + buf * TMEM_BUF + ac * TC_N + h * 16, v);
+          tmem_wait_ld();
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
+          for (int j = 0; j < 16; ++j) {
             const long long iv =
                 (long long)__float2int_rn(__fmul_rn(__uint_as_float(v[j]), unit));
-            acc[h * 32 + j] += iv << shift;
+            acc[h * 16 + j] += iv << shift;
           }
         }
       }
@@ -522,8 +536,8 @@ TcPlan plan_for(int64_t K, int nr, int nl) {
   pl.kt_per_split = (pl.kt_per_split + TC_CHUNK - 1) / TC_CHUNK * TC_CHUNK;
   pl.kt_per_split = std::min(pl.kt_per_split, kMaxKtPerSplit);
   pl.nsplit = (int)((pl.ktiles + pl.kt_per_split - 1) / pl.kt_per_split);
-  pl.a_bytes = (size_t)pl.mtiles * pl.ktiles * TC_SLICES * A_TILE;
-  pl.b_bytes = (size_t)pl.ntiles * pl.ktiles * TC_SLICES * B_TILE;
+  pl.a_bytes = (size_t)pl.mtiles * pl.ktiles * A_STAGE;
+  pl.b_bytes = (size_t)pl.ntiles * pl.ktiles * B_STAGE;
   pl.exp_bytes = ((size_t)(nr + nl) * sizeof(int) + 255) & ~size_t(255);
   pl.part_bytes = (size_t)pl.nsplit * nr * 2 * nl * sizeof(double);
   return pl;
