@@ -182,13 +182,6 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   void* sl[2] = {slots, slots + slot};
   double* sc = ws.scales.as<double>();
   const bool ff = precision == KPMGB_PREC_FF;
-  KPMGB_TRY(launch_load_block(psi_r, sl[0], NH, (int)NR, precision, sc, false, s));
-  if (lr) KPMGB_TRY(launch_load_block(psi_l, ws.bra.ptr, NH, (int)NR, precision, sc + NR, false, s));
-  const double* mom_scale = nullptr;
-  if (ff) {
-    KPMGB_TRY(launch_scale_product(sc, lr ? sc + NR : sc, sc + 2 * NR, (int)NR, s));
-    mom_scale = sc + 2 * NR;
-  }
   // kernel_variant 10: one thread-block cluster per probe column, the
   // recurrence resident in distributed shared memory.  Automatic selection
   // takes it for small operators, where it measured faster on GB300 than
@@ -211,6 +204,23 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       (precision == KPMGB_PREC_FF
            ? NH <= 16384 && NH * NR <= 131072
            : (NH <= 16384 && NH * NR <= 524288) || (NH <= 32768 && NR <= 4));
+  // Float-float doubling calls with 64 columns on real operators of at most
+  // 8 nonzeros per row keep their vectors in the paired element layout and
+  // run every step on packed FP32 pairs (k_step_ffpk; KPMGB_PAIRED=0 keeps
+  // the standard layout and k_step_ffr).
+  static const bool paired_on = [] {
+    const char* e = std::getenv("KPMGB_PAIRED");
+    return !(e && std::atoi(e) == 0);
+  }();
+  const bool paired = paired_on && ff && !lr && !auto_cluster && (variant == 0 || variant == 11) &&
+                      packed_step_applies(op->csr, (int)NR);
+  KPMGB_TRY(launch_load_block(psi_r, sl[0], NH, (int)NR, precision, sc, false, s, paired));
+  if (lr) KPMGB_TRY(launch_load_block(psi_l, ws.bra.ptr, NH, (int)NR, precision, sc + NR, false, s));
+  const double* mom_scale = nullptr;
+  if (ff) {
+    KPMGB_TRY(launch_scale_product(sc, lr ? sc + NR : sc, sc + 2 * NR, (int)NR, s));
+    mom_scale = sc + 2 * NR;
+  }
   if (variant == 10 || auto_cluster) {
     const int rc = launch_kpm1d_cluster(op->csr, NH, (int)NR, NC, lr, precision, sl[0],
                                         lr ? ws.bra.ptr : nullptr, mu, mom_scale,
@@ -286,6 +296,7 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   a.bra = lr ? ws.bra.ptr : nullptr;
   a.variant = chosen_variant;
   a.shape = chosen_shape;
+  a.paired = paired;
   // alpha_1 = H alpha_0 with mu_0, mu_1 (src/moment.jl:440-449, :521-527)
   a.x = sl[0];
   a.z = nullptr;

@@ -183,10 +183,15 @@ struct StepArgs {
   int variant = 0;           // 0 auto, 1 register-gather kernel, 9 padded-row kernel
   int shape = 0;             // lanes-per-row * 10 + columns-per-lane of the
                              // register-gather kernel; 0 = automatic
+  bool paired = false;       // float-float vectors in the paired element layout
+                             // (re.hi, im.hi, re.lo, im.lo): the packed kernel
 };
 
 // precision: KPMGB_PREC_FP64 or KPMGB_PREC_FF.  Returns KPMGB_OK or an error.
 int launch_step(const StepArgs& a, int precision, cudaStream_t s);
+// Whether float-float doubling steps of NR columns on H can run on packed
+// FP32 pairs over the paired vector layout (StepArgs::paired).
+bool packed_step_applies(const DeviceCSR& H, int NR);
 // Autotuning: times every (variant, shape) candidate of the step `a` (which
 // must not write its own inputs: y aliasing neither x nor z) with CUDA events
 // on `s`, after one warm launch each, and returns the fastest in
@@ -203,7 +208,7 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
 // col_scale[0..NR] and col_scale[NR]).
 int launch_load_block(const void* psi_colmajor, void* slot, int64_t NH, int NR,
                       int precision, double* col_scale, bool uniform,
-                      cudaStream_t s);
+                      cudaStream_t s, bool paired = false);
 
 // Whole kpm_1d recurrence in one cooperative launch (kpmgb_small.cu); sync[2]
 // must be zero.  small_partials_bytes: the partials it needs for NR columns.

@@ -221,9 +221,16 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
           worst = std::max(worst, (size_t)grid_for(fc, NH, ffc_lanes(ncols)) * 2 * ncols *
                                       sizeof(double2));
       }
+      if (KernelFn fp = select_kernel_ffpk(ncols, H.is_real != 0, H.max_row_nnz, H.ell_w))
+        worst = std::max(worst, (size_t)grid_for(fp, NH, 32) * 2 * ncols * sizeof(double2));
     }
   }
   return worst;
+}
+
+bool packed_step_applies(const DeviceCSR& H, int NR) {
+  return NR <= cols_per_launch() &&
+         select_kernel_ffpk(NR, H.is_real != 0, H.max_row_nnz, H.ell_w) != nullptr;
 }
 
 int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
@@ -275,6 +282,16 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     // NR=16, kpm_2d 183 ms against 189 ms (exact-length last chunk); the
     // L2-resident 2D Anderson L=64, NR=12, 7.4 ms against 8.3 ms per call
     // (4 lanes x 3 columns against 16 x 1).
+    if (a.paired) {
+      // the call keeps its vectors in the paired layout: only the packed
+      // kernel reads them
+      KernelFn fp = precision == KPMGB_PREC_FF && a.dot == DOT_DOUBLING
+                        ? select_kernel_ffpk(p.ncols, H.is_real != 0, H.max_row_nnz, H.ell_w)
+                        : nullptr;
+      if (!fp) return fail(KPMGB_ERR_CUDA, "internal: paired layout without the packed kernel");
+      KPMGB_TRY(launch_step_kernel(fp, grid_for(fp, a.NH, 32), s, p));
+      continue;
+    }
     if (a.variant == 11 && precision != KPMGB_PREC_FF)
       return fail(KPMGB_ERR_ARGUMENT, "the row-streaming kernel is float-float only");
     if (precision == KPMGB_PREC_FF && (a.variant == 11 || a.variant == 0)) {
@@ -409,7 +426,8 @@ __global__ void __launch_bounds__(256) k_colnorm2(const double2* __restrict__ ps
 template <bool FF>
 __global__ void __launch_bounds__(256) k_transpose_in(const double2* __restrict__ psi, void* out,
                                                       int64_t NH, int NR,
-                                                      const double* __restrict__ col_scale) {
+                                                      const double* __restrict__ col_scale,
+                                                      bool paired) {
   __shared__ double2 tile[32][33];
   const int64_t r0 = (int64_t)blockIdx.x * 32;
   const int c0 = blockIdx.y * 32;
@@ -431,7 +449,8 @@ __global__ void __launch_bounds__(256) k_transpose_in(const double2* __restrict_
         const double f = 1.0 / col_scale[c];
         const float2 re = ff::split_double(v.x * f);
         const float2 im = ff::split_double(v.y * f);
-        static_cast<float4*>(out)[r * NR + c] = make_float4(re.x, re.y, im.x, im.y);
+        static_cast<float4*>(out)[r * NR + c] = paired ? make_float4(re.x, im.x, re.y, im.y)
+                                                       : make_float4(re.x, re.y, im.x, im.y);
       } else {
         static_cast<double2*>(out)[r * NR + c] = v;
       }
@@ -461,7 +480,7 @@ __global__ void k_copy2(const double2* src, double2* dst, int64_t n) {
 }  // namespace
 
 int launch_load_block(const void* psi, void* slot, int64_t NH, int NR, int precision,
-                      double* col_scale, bool uniform, cudaStream_t s) {
+                      double* col_scale, bool uniform, cudaStream_t s, bool paired) {
   const bool ff = precision == KPMGB_PREC_FF;
   if (ff) {
     k_colnorm2<<<NR, 256, 0, s>>>(static_cast<const double2*>(psi), NH, col_scale);
@@ -474,10 +493,10 @@ int launch_load_block(const void* psi, void* slot, int64_t NH, int NR, int preci
   dim3 grid((unsigned)((NH + 31) / 32), (unsigned)((NR + 31) / 32));
   if (ff)
     k_transpose_in<true><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
-                                              col_scale);
+                                              col_scale, paired);
   else
     k_transpose_in<false><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
-                                               nullptr);
+                                               nullptr, false);
   KPMGB_LAUNCHED();
   return KPMGB_OK;
 }

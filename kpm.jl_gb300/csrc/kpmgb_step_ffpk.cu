@@ -1,0 +1,277 @@
+// Row-streaming float-float step on packed FP32 pairs (k_step_ffpk): real
+// operators, 64 columns, doubling dots.
+//
+// Blackwell executes `fma/add/sub/mul.rn.f32x2` on a 64-bit register pair:
+// one instruction for two correctly rounded FP32 operations.  For real H the
+// real and imaginary parts of a float-float complex value go through
+// identical operation sequences, so this kernel runs k_step_ffr's row
+// arithmetic once on the pair {re, im}: 6 packed operations per nonzero and
+// column for the anchored products instead of 12, and likewise for the
+// epilogue and the compensated dots.  The pairs come straight from memory:
+// the call stores its recurrence vectors as (re.hi, im.hi, re.lo, im.lo) per
+// element ("paired" layout, written by the load kernel), so a 16-byte load
+// yields the {hi} and {lo} pairs in register pairs and no packing is needed
+// except for broadcasting the operator values.  Each lane of a pair performs
+// exactly the scalar sequence of k_step_ffr (A - A_new stands for
+// -(A_new - A), both exact), so y is bitwise k_step_ffr's; the dots add the
+// real and imaginary terms in separate accumulators and join them at the
+// FP64 fold.
+//
+// Layout and pipeline as k_step_ffr: a warp owns a row, each lane the two
+// columns lane and lane + 32; the next row's 8 column indices and values are
+// staged in the warp's shared memory with cp.async; all loads of a row are
+// issued before its arithmetic; 2 blocks per SM.
+#include <cuda_runtime.h>
+
+#include "kpmgb_step.cuh"
+
+namespace kpmgb {
+namespace step {
+
+namespace {
+
+using f2 = unsigned long long;  // {first, second} FP32 pair in one 64-bit register
+
+__device__ __forceinline__ f2 pk(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void upk(f2 v, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// TwoSum (Knuth / Moller) on both lanes: s + e = a + b exactly.
+__device__ __forceinline__ void two_sum2(f2 a, f2 b, f2& s, f2& e) {
+  s = add2(a, b);
+  const f2 bb = sub2(s, a);
+  e = add2(sub2(a, sub2(s, bb)), sub2(b, bb));
+}
+
+// Anchored multiply-accumulate of the real float-float h (broadcast to both
+// lanes) times x = {re, im} (ff::amac on each lane).
+__device__ __forceinline__ void amac2(f2& A, f2& C, f2 hh, f2 hl, f2 xh, f2 xl) {
+  const f2 An = fma2(hh, xh, A);
+  const f2 nq = sub2(A, An);
+  C = add2(C, fma2(hh, xh, nq));
+  C = fma2(hh, xl, C);
+  C = fma2(hl, xh, C);
+  A = An;
+}
+
+// Compensated accumulation of a*b on both lanes (ff::dacc per lane); nah is
+// -a_h, so nah*b_h + p = p - a_h b_h is the negated (exact) TwoProd error,
+// subtracted instead of added (the same rounded value).
+__device__ __forceinline__ void dacc2(f2& S, f2& C, f2 ah, f2 nah, f2 al, f2 bh, f2 bl) {
+  const f2 p = mul2(ah, bh);
+  const f2 ne = fma2(nah, bh, p);
+  f2 s, t;
+  two_sum2(S, p, s, t);
+  C = add2(C, sub2(t, ne));
+  C = fma2(ah, bl, C);
+  C = fma2(al, bh, C);
+  S = s;
+}
+
+__device__ __forceinline__ double join2(f2 S, f2 C) {
+  float s0, s1, c0, c1;
+  upk(S, s0, s1);
+  upk(C, c0, c1);
+  return ((double)s0 + (double)c0) + ((double)s1 + (double)c1);
+}
+
+}  // namespace
+
+template <int W>
+__global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
+  pdl_enter();
+  constexpr int GROUPS = kThreads / 32;  // rows per block tile
+  constexpr int CPL = 2;
+  constexpr int kStride = 8;  // padded row stride (ints / float2 values)
+  const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const ulonglong2* __restrict__ x = static_cast<const ulonglong2*>(p.x);
+  const ulonglong2* z = static_cast<const ulonglong2*>(p.z);
+  ulonglong2* y = static_cast<ulonglong2*>(p.y);
+  const int* __restrict__ ecol = p.ell_col;
+  const float2* __restrict__ eval = static_cast<const float2*>(p.ell_val);
+  const f2 alpha2 = pk(p.alpha_f, p.alpha_f);
+  const int beta_mode = p.beta_mode;
+  const int ld = p.ld;
+
+  __shared__ double2 sacc[kThreads][2 * CPL];
+  // per warp, two buffers of one padded row: 8 column indices, 8 values
+  __shared__ __align__(16) int sidx[GROUPS][2][3 * kStride];
+  // dot accumulators per column: norm {sum re^2, sum im^2}, cross
+  // {sum re x re y, sum im x im y}
+  f2 nS[CPL], nC[CPL], xS[CPL], xC[CPL];
+  const f2 zero2 = pk(0.f, 0.f);
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) {
+    sacc[threadIdx.x][c] = make_double2(0.0, 0.0);
+    sacc[threadIdx.x][CPL + c] = make_double2(0.0, 0.0);
+    nS[c] = nC[c] = xS[c] = xC[c] = zero2;
+  }
+  int rows_since_flush = 0;
+
+  auto stage = [&](int64_t r, int b) {
+    if (lane < 6) {
+      const char* src = lane < 2 ? reinterpret_cast<const char*>(ecol + r * kStride) + lane * 16
+                                 : reinterpret_cast<const char*>(eval + r * kStride) + (lane - 2) * 16;
+      const unsigned dst = (unsigned)__cvta_generic_to_shared(&sidx[g][b][lane * 4]);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+  int buf = 0;
+  {
+    const int64_t r0 = (int64_t)blockIdx.x * GROUPS + g;
+    if ((int64_t)blockIdx.x < ntiles && r0 < p.NH) stage(r0, 0);
+    else asm volatile("cp.async.commit_group;" ::: "memory");
+  }
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t r = t * GROUPS + g;
+    if (r >= p.NH) continue;
+    {
+      const int64_t rn = r + (int64_t)gridDim.x * GROUPS;
+      if (t + gridDim.x < ntiles && rn < p.NH) stage(rn, buf ^ 1);
+      else asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncwarp();
+    const int* jrow = &sidx[g][buf][0];
+    const float4* hrow = reinterpret_cast<const float4*>(&sidx[g][buf][kStride]);
+    const int64_t base = r * ld + p.c0;
+    // every load of the row, before any arithmetic
+    ulonglong2 zv[CPL], xo[CPL], xv[CPL][W];
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      const int64_t e = base + lane + 32 * c;
+      zv[c] = beta_mode != 0 ? __ldcs(z + e) : make_ulonglong2(0ull, 0ull);
+      xo[c] = __ldg(x + e);
+    }
+    {
+      const int4 j0 = reinterpret_cast<const int4*>(jrow)[0];
+      const int4 j1 = reinterpret_cast<const int4*>(jrow)[1];
+      const int jj[8] = {j0.x, j0.y, j0.z, j0.w, j1.x, j1.y, j1.z, j1.w};
+#pragma unroll
+      for (int c = 0; c < CPL; ++c)
+#pragma unroll
+        for (int u = 0; u < W; ++u) xv[c][u] = __ldg(x + (int64_t)jj[u] * ld + p.c0 + lane + 32 * c);
+    }
+    float hh[8], hl[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 v = hrow[q];
+      hh[2 * q] = v.x;
+      hl[2 * q] = v.y;
+      hh[2 * q + 1] = v.z;
+      hl[2 * q + 1] = v.w;
+    }
+    __syncwarp();  // the buffer is restaged two rows later
+    buf ^= 1;
+    float R = 0.f;
+#pragma unroll
+    for (int u = 0; u < W; ++u) R = __fadd_rn(R, fabsf(hh[u]));
+    f2 hh2[W], hl2[W];
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      hh2[u] = pk(hh[u], hh[u]);
+      hl2[u] = pk(hl[u], hl[u]);
+    }
+#pragma unroll
+    for (int c = 0; c < CPL; ++c) {
+      float M = 0.f;
+#pragma unroll
+      for (int u = 0; u < W; ++u) {
+        float re, im;
+        upk(xv[c][u].x, re, im);
+        M = fmaxf(M, fmaxf(fabsf(re), fabsf(im)));
+      }
+      // anchor 1.5 * 2^E with 2^E = 4P, P <= R*M (1 + tiny) < 2P (k_step_ffr)
+      const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
+      const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
+      const f2 sig2 = pk(sig, sig);
+      f2 A = sig2, C = zero2;
+#pragma unroll
+      for (int u = 0; u < W; ++u) amac2(A, C, hh2[u], hl2[u], xv[c][u].x, xv[c][u].y);
+      const f2 S = sub2(A, sig2);
+      // y = alpha (S + C) + beta z, normalised (ff_epilogue on both lanes)
+      const f2 u2 = mul2(alpha2, S);  // alpha is a power of two: exact
+      const f2 c2 = mul2(alpha2, C);
+      f2 yh, yl;
+      if (beta_mode == 0) {
+        two_sum2(u2, c2, yh, yl);
+      } else {
+        f2 s, e;
+        if (beta_mode > 0) {
+          two_sum2(u2, zv[c].x, s, e);
+          two_sum2(s, add2(e, add2(c2, zv[c].y)), yh, yl);
+        } else {
+          // two_sum(u, -zh) and e + (c - zl): the negations are exact
+          s = sub2(u2, zv[c].x);
+          const f2 bb = sub2(s, u2);
+          e = sub2(sub2(u2, sub2(s, bb)), add2(zv[c].x, bb));
+          two_sum2(s, add2(e, sub2(c2, zv[c].y)), yh, yl);
+        }
+      }
+      __stcs(y + base + lane + 32 * c, make_ulonglong2(yh, yl));
+      const f2 nxh = sub2(zero2, xo[c].x);  // exact negation
+      dacc2(nS[c], nC[c], xo[c].x, nxh, xo[c].y, xo[c].x, xo[c].y);
+      dacc2(xS[c], xC[c], xo[c].x, nxh, xo[c].y, yh, yl);
+    }
+    if (++rows_since_flush == kFlushRows) {
+      rows_since_flush = 0;
+#pragma unroll
+      for (int c = 0; c < CPL; ++c) {
+        sacc[threadIdx.x][c].x += join2(nS[c], nC[c]);
+        sacc[threadIdx.x][CPL + c].x += join2(xS[c], xC[c]);
+        nS[c] = nC[c] = xS[c] = xC[c] = zero2;
+      }
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  double2 d[2][CPL];
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) {
+    d[0][c] = sacc[threadIdx.x][c];
+    d[0][c].x += join2(nS[c], nC[c]);
+    d[1][c] = sacc[threadIdx.x][CPL + c];
+    d[1][c].x += join2(xS[c], xC[c]);
+  }
+  reduce_finalize<2, 32, CPL>(d, p);
+}
+
+KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {
+  if (!real || ell_w != 8 || ncols != 64 || max_row_nnz > 8) return nullptr;
+  switch (max_row_nnz) {
+    case 5: return k_step_ffpk<5>;
+    case 6: return k_step_ffpk<6>;
+    case 7: return k_step_ffpk<7>;
+    case 8: return k_step_ffpk<8>;
+    default: return nullptr;
+  }
+}
+
+}  // namespace step
+}  // namespace kpmgb

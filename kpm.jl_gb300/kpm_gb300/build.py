@@ -38,6 +38,7 @@ SOURCES = [
     "kpmgb_timing.cu",
     "kpmgb_tune.cu",
     "kpmgb_hostio.cu",
+    "kpmgb_step_ffpk.cu",
 ]
 
 
