@@ -197,6 +197,32 @@ int grid_for(KernelFn fn, int64_t NH, int lpr) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)per_sm * num_sms()));
 }
 
+// Grid of a packed step: resident blocks per SM (with its threads and
+// dynamic shared memory) times the SM count, capped by the row tiles.
+int grid_packed(const PackedStep& ps, int64_t NH) {
+  static std::mutex m;
+  static std::unordered_map<const void*, int> cache;
+  int per_sm = 1;
+  {
+    std::lock_guard<std::mutex> lk(m);
+    auto it = cache.find((const void*)ps.fn);
+    if (it != cache.end()) {
+      per_sm = it->second;
+    } else {
+      if (ps.smem > 48 * 1024)
+        cudaFuncSetAttribute(ps.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ps.smem);
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ps.fn, ps.threads, ps.smem) !=
+          cudaSuccess)
+        per_sm = 1;
+      per_sm = std::max(per_sm, 1);
+      cudaGetLastError();
+      cache.emplace((const void*)ps.fn, per_sm);
+    }
+  }
+  const int64_t tiles = (NH + ps.rows_per_block - 1) / ps.rows_per_block;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(tiles, (int64_t)per_sm * num_sms()));
+}
+
 }  // namespace
 
 size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision) {
@@ -221,8 +247,8 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
           worst = std::max(worst, (size_t)grid_for(fc, NH, ffc_lanes(ncols)) * 2 * ncols *
                                       sizeof(double2));
       }
-      if (KernelFn fp = select_kernel_ffpk(ncols, H.is_real != 0, H.max_row_nnz, H.ell_w))
-        worst = std::max(worst, (size_t)grid_for(fp, NH, 32) * 2 * ncols * sizeof(double2));
+      const PackedStep ps = select_packed_step(ncols, H.is_real != 0, H.max_row_nnz, H.ell_w);
+      if (ps.fn) worst = std::max(worst, (size_t)grid_packed(ps, NH) * 2 * ncols * sizeof(double2));
     }
   }
   return worst;
@@ -285,11 +311,12 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     if (a.paired) {
       // the call keeps its vectors in the paired layout: only the packed
       // kernel reads them
-      KernelFn fp = precision == KPMGB_PREC_FF && a.dot == DOT_DOUBLING
-                        ? select_kernel_ffpk(p.ncols, H.is_real != 0, H.max_row_nnz, H.ell_w)
-                        : nullptr;
-      if (!fp) return fail(KPMGB_ERR_CUDA, "internal: paired layout without the packed kernel");
-      KPMGB_TRY(launch_step_kernel(fp, grid_for(fp, a.NH, 32), s, p));
+      const PackedStep ps =
+          precision == KPMGB_PREC_FF && a.dot == DOT_DOUBLING
+              ? select_packed_step(p.ncols, H.is_real != 0, H.max_row_nnz, H.ell_w)
+              : PackedStep{};
+      if (!ps.fn) return fail(KPMGB_ERR_CUDA, "internal: paired layout without the packed kernel");
+      KPMGB_TRY(launch_step_kernel(ps.fn, grid_packed(ps, a.NH), s, p, ps.threads, ps.smem));
       continue;
     }
     if (a.variant == 11 && precision != KPMGB_PREC_FF)

@@ -747,6 +747,15 @@ int ffc_lanes(int ncols);
 // vectors in the paired element layout (re.hi, im.hi, re.lo, im.lo);
 // nullptr otherwise.  Rows per block tile: 8.
 KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w);
+// The packed step to launch for such a call (fn = nullptr when none applies):
+// threads per block, dynamic shared memory, rows per block tile.
+struct PackedStep {
+  KernelFn fn = nullptr;
+  int threads = 0;
+  size_t smem = 0;
+  int rows_per_block = 0;
+};
+PackedStep select_packed_step(int ncols, bool real, int max_row_nnz, int ell_w);
 
 }  // namespace step
 }  // namespace kpmgb
