@@ -23,8 +23,6 @@
 // issued before its arithmetic; 2 blocks per SM.
 #include <cuda_runtime.h>
 
-#include <cstdlib>
-
 #include "kpmgb_step.cuh"
 
 namespace kpmgb {
@@ -264,215 +262,6 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
   reduce_finalize<2, 32, CPL>(d, p);
 }
 
-// ---------------------------------------------------------------------------
-// Gathers staged in shared memory (k_step_ffpks): the W neighbour loads of the
-// NEXT row go out as cp.async copies into a per-warp shared-memory buffer
-// while the current row is computed from the other buffer, so the gather
-// latency overlaps a whole row of arithmetic without holding the loads in
-// registers.  z and the row's own x are plain loads issued at the start of
-// the row and consumed at its end.  6 warps per block, 2 blocks per SM; the
-// arithmetic is k_step_ffpk's, so y is bitwise the same.
-namespace {
-constexpr int kPkWarps = 6;
-constexpr int kPkThreads = kPkWarps * 32;
-}  // namespace
-
-template <int W>
-__global__ void __launch_bounds__(kPkThreads, 2) k_step_ffpks(KParams p) {
-  pdl_enter();
-  constexpr int CPL = 2;
-  constexpr int kStride = 8;
-  // per warp: 2 buffers x W neighbours x 2 column slots x 32 lanes x 16 bytes
-  extern __shared__ __align__(16) unsigned char pk_dyn[];
-  __shared__ __align__(16) int sidx[kPkWarps][3][3 * kStride];
-  const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  ulonglong2* gbuf = reinterpret_cast<ulonglong2*>(pk_dyn) + (size_t)g * 2 * W * CPL * 32;
-  const ulonglong2* __restrict__ x = static_cast<const ulonglong2*>(p.x);
-  const ulonglong2* z = static_cast<const ulonglong2*>(p.z);
-  ulonglong2* y = static_cast<ulonglong2*>(p.y);
-  const int* __restrict__ ecol = p.ell_col;
-  const float2* __restrict__ eval = static_cast<const float2*>(p.ell_val);
-  const f2 alpha2 = pk(p.alpha_f, p.alpha_f);
-  const int beta_mode = p.beta_mode;
-  const int ld = p.ld;
-  const f2 zero2 = pk(0.f, 0.f);
-  f2 nS[CPL], nC[CPL], xS[CPL], xC[CPL];
-  double dn[CPL], dx[CPL];
-#pragma unroll
-  for (int c = 0; c < CPL; ++c) {
-    nS[c] = nC[c] = xS[c] = xC[c] = zero2;
-    dn[c] = dx[c] = 0.0;
-  }
-  int rows_since_flush = 0;
-
-  auto stage_idx = [&](int64_t r, int b) {
-    if (lane < 6) {
-      const char* src = lane < 2 ? reinterpret_cast<const char*>(ecol + r * kStride) + lane * 16
-                                 : reinterpret_cast<const char*>(eval + r * kStride) + (lane - 2) * 16;
-      const unsigned dst = (unsigned)__cvta_generic_to_shared(&sidx[g][b][lane * 4]);
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-    }
-  };
-  // the W gathers of both column slots of row r into buffer b
-  auto stage_rows = [&](int64_t r, int bi, int b) {
-    const int* jr = &sidx[g][bi][0];
-#pragma unroll
-    for (int u = 0; u < W; ++u) {
-      const int j = jr[u];
-#pragma unroll
-      for (int c = 0; c < CPL; ++c) {
-        const ulonglong2* src = x + (int64_t)j * ld + p.c0 + lane + 32 * c;
-        const unsigned dst =
-            (unsigned)__cvta_generic_to_shared(gbuf + ((size_t)(b * W + u) * CPL + c) * 32 + lane);
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-      }
-    }
-    (void)r;
-  };
-  const int64_t rstride = (int64_t)gridDim.x * kPkWarps;
-  int64_t r = (int64_t)blockIdx.x * kPkWarps + g;
-  if (r < p.NH) {
-    stage_idx(r, 0);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    if (r + rstride < p.NH) stage_idx(r + rstride, 1);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    asm volatile("cp.async.wait_group 1;" ::: "memory");
-    __syncwarp();
-    stage_rows(r, 0, 0);
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    int bi = 0, b = 0;
-    for (;;) {
-      const int64_t rn = r + rstride;
-      const bool has_next = rn < p.NH;
-      // this row's gathers and the next row's indices have landed
-      asm volatile("cp.async.wait_group 0;" ::: "memory");
-      __syncwarp();
-      const int bin = bi == 2 ? 0 : bi + 1;
-      if (has_next) stage_rows(rn, bin, b ^ 1);
-      if (rn + rstride < p.NH) stage_idx(rn + rstride, bin == 2 ? 0 : bin + 1);
-      asm volatile("cp.async.commit_group;" ::: "memory");
-      const int64_t base = r * ld + p.c0 + lane;
-      ulonglong2 zv[CPL], xo[CPL];
-#pragma unroll
-      for (int c = 0; c < CPL; ++c) {
-        zv[c] = beta_mode != 0 ? __ldcs(z + base + 32 * c) : make_ulonglong2(0ull, 0ull);
-        xo[c] = __ldg(x + base + 32 * c);
-      }
-      float hh[8], hl[8];
-      {
-        const float4* hrow = reinterpret_cast<const float4*>(&sidx[g][bi][kStride]);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float4 v = hrow[q];
-          hh[2 * q] = v.x;
-          hl[2 * q] = v.y;
-          hh[2 * q + 1] = v.z;
-          hl[2 * q + 1] = v.w;
-        }
-      }
-      float R = 0.f;
-#pragma unroll
-      for (int u = 0; u < W; ++u) R = __fadd_rn(R, fabsf(hh[u]));
-      f2 hh2[W], hl2[W];
-#pragma unroll
-      for (int u = 0; u < W; ++u) {
-        hh2[u] = pk(hh[u], hh[u]);
-        hl2[u] = pk(hl[u], hl[u]);
-      }
-#pragma unroll
-      for (int c = 0; c < CPL; ++c) {
-        ulonglong2 xv[W];
-#pragma unroll
-        for (int u = 0; u < W; ++u) xv[u] = gbuf[((size_t)(b * W + u) * CPL + c) * 32 + lane];
-        float M = 0.f;
-#pragma unroll
-        for (int u = 0; u < W; ++u) {
-          float re, im;
-          upk(xv[u].x, re, im);
-          M = fmaxf(M, fmaxf(fabsf(re), fabsf(im)));
-        }
-        const float B = __fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f);
-        const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
-        const f2 sig2 = pk(sig, sig);
-        f2 A = sig2, C = zero2;
-#pragma unroll
-        for (int u = 0; u < W; ++u) amac2(A, C, hh2[u], hl2[u], xv[u].x, xv[u].y);
-        const f2 S = sub2(A, sig2);
-        const f2 u2 = mul2(alpha2, S);
-        const f2 c2 = mul2(alpha2, C);
-        f2 yh, yl;
-        if (beta_mode == 0) {
-          two_sum2(u2, c2, yh, yl);
-        } else {
-          f2 s2, e2;
-          if (beta_mode > 0) {
-            two_sum2(u2, zv[c].x, s2, e2);
-            two_sum2(s2, add2(e2, add2(c2, zv[c].y)), yh, yl);
-          } else {
-            s2 = sub2(u2, zv[c].x);
-            const f2 bb = sub2(s2, u2);
-            e2 = sub2(sub2(u2, sub2(s2, bb)), add2(zv[c].x, bb));
-            two_sum2(s2, add2(e2, sub2(c2, zv[c].y)), yh, yl);
-          }
-        }
-        __stcs(y + base + 32 * c, make_ulonglong2(yh, yl));
-        const f2 nxh = sub2(zero2, xo[c].x);
-        dacc2(nS[c], nC[c], xo[c].x, nxh, xo[c].y, xo[c].x, xo[c].y);
-        dacc2(xS[c], xC[c], xo[c].x, nxh, xo[c].y, yh, yl);
-      }
-      if (++rows_since_flush == kFlushRows) {
-        rows_since_flush = 0;
-#pragma unroll
-        for (int c = 0; c < CPL; ++c) {
-          dn[c] += join2(nS[c], nC[c]);
-          dx[c] += join2(xS[c], xC[c]);
-          nS[c] = nC[c] = xS[c] = xC[c] = zero2;
-        }
-      }
-      __syncwarp();  // buffer b and index buffer bi are restaged next row
-      if (!has_next) break;
-      r = rn;
-      bi = bin;
-      b ^= 1;
-    }
-  }
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
-  double2 d[2][CPL];
-#pragma unroll
-  for (int c = 0; c < CPL; ++c) {
-    d[0][c] = make_double2(dn[c] + join2(nS[c], nC[c]), 0.0);
-    d[1][c] = make_double2(dx[c] + join2(xS[c], xC[c]), 0.0);
-  }
-  reduce_finalize<2, 32, CPL, kPkWarps>(d, p);
-}
-
-PackedStep select_packed_step(int ncols, bool real, int max_row_nnz, int ell_w) {
-  PackedStep ps;
-  if (!real || ell_w != 8 || ncols != 64 || max_row_nnz > 8) return ps;
-  static const bool staged = [] {
-    const char* e = std::getenv("KPMGB_PACKED_STAGED");
-    return !(e && std::atoi(e) == 0);
-  }();
-  if (!staged) {
-    ps.fn = select_kernel_ffpk(ncols, real, max_row_nnz, ell_w);
-    ps.threads = kThreads;
-    ps.rows_per_block = kThreads / 32;
-    ps.smem = 0;
-    return ps;
-  }
-  const int W = max_row_nnz <= 5 ? 5 : max_row_nnz;
-  switch (W) {
-    case 5: ps.fn = k_step_ffpks<5>; break;
-    case 6: ps.fn = k_step_ffpks<6>; break;
-    case 7: ps.fn = k_step_ffpks<7>; break;
-    default: ps.fn = k_step_ffpks<8>; break;
-  }
-  ps.threads = kPkThreads;
-  ps.rows_per_block = kPkWarps;
-  ps.smem = (size_t)kPkWarps * 2 * W * 2 * 32 * sizeof(ulonglong2);
-  return ps;
-}
-
 KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {
   if (!real || ell_w != 8 || ncols != 64 || max_row_nnz > 8) return nullptr;
   switch (max_row_nnz) {
@@ -482,6 +271,15 @@ KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {
     case 8: return k_step_ffpk<8>;
     default: return nullptr;
   }
+}
+
+PackedStep select_packed_step(int ncols, bool real, int max_row_nnz, int ell_w) {
+  PackedStep ps;
+  ps.fn = select_kernel_ffpk(ncols, real, max_row_nnz, ell_w);
+  ps.threads = kThreads;
+  ps.rows_per_block = kThreads / 32;
+  ps.smem = 0;
+  return ps;
 }
 
 }  // namespace step
