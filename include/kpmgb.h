@@ -92,15 +92,18 @@ typedef struct kpmgb_kpm1d_options {
                               per probe column with the recurrence resident
                               in distributed shared memory (one launch per
                               call; NH up to ~100k rows); 11: row-streaming
-                              padded-row kernel (float-float, real operators,
-                              33..64 columns, rows of 5..8 nonzeros).  Other
-                              values fail with KPMGB_ERR_ARGUMENT.
+                              padded-row kernels (float-float; real operators
+                              with 33..64 columns and rows of 5..8 nonzeros,
+                              on packed FP32 pairs for exactly 64 columns in
+                              the doubling path; complex operators with 9..32
+                              columns).  Other values fail with
+                              KPMGB_ERR_ARGUMENT.
                               Automatic selection (0) is the cluster kernel
                               (10) for small operators (float-float:
                               NH <= 16384, NH * NR <= 131072; FP64:
                               NH <= 16384, NH * NR <= 524288, or NH <= 32768
                               with NR <= 4), else per-step launches of the
-                              row-streaming kernel (11) where it applies,
+                              row-streaming kernels (11) where they apply,
                               else of the padded-row kernel for real
                               operators with 33..64 columns, else of the
                               register-gather kernel with the default shape. */
@@ -369,6 +372,14 @@ int kpmgb_operator_sync(kpmgb_operator op, void* stream);
 /* Number of CUDA kernels the library launched since the process started
  * (instrumentation for benchmarks). */
 int64_t kpmgb_kernel_launch_count(void);
+
+/* Page-locked host memory for input blocks.  The host entry points read
+ * pinned inputs of 1 MiB or more with a copy kernel through the buffer's
+ * device address (about 210 GB/s over NVLink-C2C on GB300 in every state of
+ * the link), pageable ones through the staged copy engine.  kpmgb_host_free
+ * releases a buffer from kpmgb_host_alloc. */
+int kpmgb_host_alloc(int64_t bytes, void** out);
+int kpmgb_host_free(void* ptr);
 
 #ifdef __cplusplus
 }

@@ -583,6 +583,20 @@ const char* kpmgb_last_error(void) { return t_last_error.c_str(); }
 
 int64_t kpmgb_kernel_launch_count(void) { return g_launches.load(); }
 
+int kpmgb_host_alloc(int64_t bytes, void** out) {
+  clear_error();
+  if (!out || bytes < 1) return fail(KPMGB_ERR_ARGUMENT, "invalid host allocation");
+  *out = nullptr;
+  KPMGB_CUDA(cudaMallocHost(out, (size_t)bytes));
+  return KPMGB_OK;
+}
+
+int kpmgb_host_free(void* ptr) {
+  clear_error();
+  if (ptr) KPMGB_CUDA(cudaFreeHost(ptr));
+  return KPMGB_OK;
+}
+
 int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const int64_t* rowval,
                           const double* nzval, int32_t index_base, kpmgb_operator* out) {
   clear_error();

@@ -23,8 +23,6 @@
 // issued before its arithmetic; 2 blocks per SM.
 #include <cuda_runtime.h>
 
-#include <cstdlib>
-
 #include "kpmgb_step.cuh"
 
 namespace kpmgb {
@@ -104,7 +102,7 @@ __device__ __forceinline__ double join2(f2 S, f2 C) {
 
 }  // namespace
 
-template <int W, bool CHUNKED>
+template <int W>
 __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
   pdl_enter();
   constexpr int GROUPS = kThreads / 32;  // rows per block tile
@@ -144,25 +142,23 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
     }
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
+  // row tiles of this block: every gridDim.x-th tile, so that the rows in
+  // flight on the whole GPU lie in one window and their distant neighbours
+  // (the ±L^2 planes of a 3D lattice) are still in L2 (contiguous ranges of
+  // tiles per block measured 2.18 ms per step against 1.57 ms)
   const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
-  // row tiles of this block: every gridDim.x-th tile, or (CHUNKED) one
-  // contiguous range of tiles
-  const int64_t per_block = (ntiles + gridDim.x - 1) / gridDim.x;
-  const int64_t t_first = CHUNKED ? (int64_t)blockIdx.x * per_block : (int64_t)blockIdx.x;
-  const int64_t t_end = CHUNKED ? min(ntiles, t_first + per_block) : ntiles;
-  const int64_t t_step = CHUNKED ? 1 : (int64_t)gridDim.x;
   int buf = 0;
   {
-    const int64_t r0 = t_first * GROUPS + g;
-    if (t_first < t_end && r0 < p.NH) stage(r0, 0);
+    const int64_t r0 = (int64_t)blockIdx.x * GROUPS + g;
+    if ((int64_t)blockIdx.x < ntiles && r0 < p.NH) stage(r0, 0);
     else asm volatile("cp.async.commit_group;" ::: "memory");
   }
-  for (int64_t t = t_first; t < t_end; t += t_step) {
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int64_t r = t * GROUPS + g;
     if (r >= p.NH) continue;
     {
-      const int64_t rn = r + t_step * GROUPS;
-      if (t + t_step < t_end && rn < p.NH) stage(rn, buf ^ 1);
+      const int64_t rn = r + (int64_t)gridDim.x * GROUPS;
+      if (t + gridDim.x < ntiles && rn < p.NH) stage(rn, buf ^ 1);
       else asm volatile("cp.async.commit_group;" ::: "memory");
     }
     asm volatile("cp.async.wait_group 1;" ::: "memory");
@@ -270,24 +266,15 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
   reduce_finalize<2, 32, CPL>(d, p);
 }
 
-template <bool CHUNKED>
-KernelFn ffpk_rows(int max_row_nnz) {
-  switch (max_row_nnz) {
-    case 5: return k_step_ffpk<5, CHUNKED>;
-    case 6: return k_step_ffpk<6, CHUNKED>;
-    case 7: return k_step_ffpk<7, CHUNKED>;
-    case 8: return k_step_ffpk<8, CHUNKED>;
-    default: return nullptr;
-  }
-}
-
 KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {
   if (!real || ell_w != 8 || ncols != 64 || max_row_nnz > 8) return nullptr;
-  static const bool chunked = [] {
-    const char* e = std::getenv("KPMGB_ROW_CHUNKS");
-    return e && std::atoi(e) != 0;
-  }();
-  return chunked ? ffpk_rows<true>(max_row_nnz) : ffpk_rows<false>(max_row_nnz);
+  switch (max_row_nnz) {
+    case 5: return k_step_ffpk<5>;
+    case 6: return k_step_ffpk<6>;
+    case 7: return k_step_ffpk<7>;
+    case 8: return k_step_ffpk<8>;
+    default: return nullptr;
+  }
 }
 
 PackedStep select_packed_step(int ncols, bool real, int max_row_nnz, int ell_w) {

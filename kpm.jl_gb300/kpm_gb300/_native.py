@@ -10,6 +10,8 @@ import ctypes as C
 import threading
 from pathlib import Path
 
+import numpy as np
+
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libkpmgb.so"
 
 # status classes (include/kpmgb.h)
@@ -48,6 +50,8 @@ EXPORTED_SYMBOLS = (
     "kpmgb_timing_enable",
     "kpmgb_timing_read",
     "kpmgb_measure_fp64_peak",
+    "kpmgb_host_alloc",
+    "kpmgb_host_free",
 )
 
 
@@ -118,6 +122,8 @@ def _declare(lib):
     lib.kpmgb_timing_enable.argtypes = [i32]
     lib.kpmgb_timing_read.argtypes = [i32, dp, C.POINTER(i64)]
     lib.kpmgb_measure_fp64_peak.argtypes = [dp]
+    lib.kpmgb_host_alloc.argtypes = [i64, C.POINTER(vp)]
+    lib.kpmgb_host_free.argtypes = [vp]
     for name in EXPORTED_SYMBOLS:
         if name not in ("kpmgb_version", "kpmgb_last_error", "kpmgb_kernel_launch_count"):
             getattr(lib, name).restype = C.c_int
@@ -153,6 +159,22 @@ def check(rc: int) -> None:
     if rc == ERR_NUMERICAL:
         raise KPMNumericalError(msg)
     raise KPMDeviceError(f"status {rc}: {msg}")
+
+
+def pinned_empty(shape, dtype=np.complex128, order="C"):
+    """An uninitialised NumPy array in page-locked host memory
+    (kpmgb_host_alloc), freed when the array is collected."""
+    import weakref
+    lib = load()
+    dt = np.dtype(dtype)
+    n = int(np.prod(shape)) * dt.itemsize
+    ptr = C.c_void_p()
+    check(lib.kpmgb_host_alloc(max(n, 1), C.byref(ptr)))
+    buf = (C.c_char * max(n, 1)).from_address(ptr.value)
+    arr = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape)))
+    arr = arr.reshape(shape, order=order)
+    weakref.finalize(buf, lib.kpmgb_host_free, C.c_void_p(ptr.value))
+    return arr
 
 
 def version() -> str:

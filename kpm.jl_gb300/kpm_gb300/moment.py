@@ -111,10 +111,10 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
 
     ``kernel`` picks the recurrence kernel (``include/kpmgb.h``,
     ``kernel_variant``): ``"auto"`` (one thread-block-cluster launch per call
-    for small operators, else per-step launches of the padded-row kernel for
-    real operators with 33..64 columns or of the register-gather kernel),
-    ``"gather"``, ``"padded"``, ``"streaming"``, ``"cluster"``, ``"single"``,
-    ``"tune"``.
+    for small operators, else per-step launches of the row-streaming kernels
+    -- on packed FP32 pairs for real operators with 64 columns, float-float --
+    where they apply, else of the register-gather kernel), ``"gather"``,
+    ``"padded"``, ``"streaming"``, ``"cluster"``, ``"single"``, ``"tune"``.
     ``use_graph`` replays the per-step launches from a CUDA graph.  With
     ``NR_parallel=False`` the columns run one call each, with the same
     options.
@@ -480,6 +480,16 @@ class EnsembleOperator:
         self.op = GB300Operator(Hb)
         self.seg = np.zeros(len(Hs) + 1, dtype=np.int64)
         self.seg[1:] = np.cumsum(self.sizes)
+        self._staging = None
+
+    def staging(self, NR: int):
+        """The stacked column-major probe block (sum NH_i, NR) in page-locked
+        host memory, kept between calls (the library reads it with its copy
+        kernel instead of staging pageable memory)."""
+        if self._staging is None or self._staging.shape[1] != NR:
+            self._staging = None
+            self._staging = _native.pinned_empty((int(self.seg[-1]), NR), np.complex128, "F")
+        return self._staging
 
     def __len__(self):
         return len(self.sizes)
@@ -524,8 +534,8 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     if ens is None:
         ens = EnsembleOperator(Hs)
     op, seg = ens.op, ens.seg
-    # one pass into the stacked column-major probe block
-    psi = np.empty((int(seg[-1]), NR), dtype=np.complex128, order="F")
+    # one pass into the stacked column-major probe block (pinned, reused)
+    psi = ens.staging(NR)
     for i, p in enumerate(psis):
         psi[int(seg[i]):int(seg[i + 1])] = p
     out = np.empty((len(sizes), NC, NR), dtype=np.complex128)
