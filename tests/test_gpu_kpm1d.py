@@ -585,3 +585,12 @@ def test_pinned_host_probes_match_pageable(lr):
         kg.kpm_1d_bang(op, NC, NR, NH, b, host_psi)
     assert np.array_equal(a, b)
     assert relerr(a, ko.kpm_1d_lr(H, NC, psi, psi) if lr else ko.kpm_1d_doubling(H, NC, psi)) < 1e-12
+    # the library's own page-locked buffers (kpmgb_host_alloc)
+    own = kg.pinned_empty((NH, NR), np.complex128, "F")
+    own[...] = psi
+    c = np.zeros((NR, NC), dtype=np.complex128)
+    if lr:
+        kg.kpm_1d_bang(op, NC, NR, NH, c, own, own)
+    else:
+        kg.kpm_1d_bang(op, NC, NR, NH, c, own)
+    assert np.array_equal(a, c)
