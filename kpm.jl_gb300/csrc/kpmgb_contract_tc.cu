@@ -270,28 +270,6 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
   }
 }
 
-// Zero the padding rows nrows..rows_pad-1 of a plane array (every k-tile and
-// digit plane), leaving the rows k_slice writes untouched.
-template <int ROWS>
-__global__ void k_zero_rows(uint8_t* planes, int nrows, int rows_pad, int64_t ktiles) {
-  constexpr uint32_t TILE = ROWS == TC_N ? B_TILE : A_TILE;
-  const int64_t per_row = ktiles * (TC_KT / 8) * TC_SLICES;
-  const int64_t total = (int64_t)(rows_pad - nrows) * per_row;
-  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int row = nrows + (int)(idx / per_row);
-    int64_t q = idx % per_row;
-    const int i = (int)(q % TC_SLICES);
-    q /= TC_SLICES;
-    const int64_t kt = q / (TC_KT / 8);
-    const int kin = (int)(q % (TC_KT / 8)) * 8;
-    const int tile = row / ROWS, r = row % ROWS;
-    uint8_t* tbase = planes + (size_t)(tile * ktiles + kt) * (TC_SLICES * TILE);
-    *reinterpret_cast<uint4*>(tbase + tile_off<TC_SLICES * ROWS>(i * ROWS + r, kin)) =
-        make_uint4(0, 0, 0, 0);
-  }
-}
-
 // --------------------------------------------------------------- GEMM
 struct TcArgs {
   const uint8_t* A;      // planes [mtiles][ktiles][A_STAGE]
@@ -586,10 +564,10 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
   const int64_t groupsB = (int64_t)a.nl * pl.ktiles * (TC_KT / 8);
   const int gA = (int)std::min<int64_t>((groupsA + 255) / 256, 65535 * 16);
   const int gB = (int)std::min<int64_t>((groupsB + 255) / 256, 65535 * 16);
-  auto zero_grid = [&](int64_t rows) {
-    const int64_t n = rows * pl.ktiles * (TC_KT / 8) * TC_SLICES;
-    return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 65535 * 16));
-  };
+  // The padding rows of the last A and B tiles (rows nr.. and 2 nl.. of the
+  // plane arrays) are not written: the MMAs multiply them only into output
+  // rows and columns that the epilogue discards, each output being its own
+  // dot product.
   if (!a.reuse_l) {
     if (ff) {
       k_vec_exp<true><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
@@ -597,10 +575,6 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
       k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
     }
     KPMGB_LAUNCHED();
-    if (rowsB > 2 * a.nl) {
-      k_zero_rows<TC_N><<<zero_grid(rowsB - 2 * a.nl), 256, 0, s>>>(B, 2 * a.nl, rowsB, pl.ktiles);
-      KPMGB_LAUNCHED();
-    }
     if (ff) {
       k_slice<true, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
     } else {
@@ -614,10 +588,6 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
     k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
   }
   KPMGB_LAUNCHED();
-  if (rowsA > a.nr) {
-    k_zero_rows<TC_M><<<zero_grid(rowsA - a.nr), 256, 0, s>>>(A, a.nr, rowsA, pl.ktiles);
-    KPMGB_LAUNCHED();
-  }
   if (ff) {
     k_slice<true, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A);
   } else {

@@ -243,7 +243,7 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
                                       sizeof(double2));
         if (KernelFn fr = select_kernel_ffr(ncols, dot, H.is_real != 0, H.max_row_nnz, H.ell_w))
           worst = std::max(worst, (size_t)grid_for(fr, NH, 32) * 2 * ncols * sizeof(double2));
-        if (KernelFn fc = select_kernel_ffc(ncols, dot, H.is_real != 0, H.ell_w))
+        if (KernelFn fc = select_kernel_ffc(ncols, dot, H.is_real != 0, H.ell_w, H.max_row_nnz))
           worst = std::max(worst, (size_t)grid_for(fc, NH, ffc_lanes(ncols)) * 2 * ncols *
                                       sizeof(double2));
       }
@@ -328,10 +328,10 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
         continue;
       }
       KernelFn fc = H.ell_w > 0 && kStreamingComplex
-                        ? select_kernel_ffc(p.ncols, a.dot, H.is_real != 0, H.ell_w)
+                        ? select_kernel_ffc(p.ncols, a.dot, H.is_real != 0, H.ell_w, H.max_row_nnz)
                         : nullptr;
       if (a.variant == 11 && !fc && H.ell_w > 0)
-        fc = select_kernel_ffc(p.ncols, a.dot, H.is_real != 0, H.ell_w);
+        fc = select_kernel_ffc(p.ncols, a.dot, H.is_real != 0, H.ell_w, H.max_row_nnz);
       if (fc) {
         KPMGB_TRY(launch_step_kernel(fc, grid_for(fc, a.NH, ffc_lanes(p.ncols)), s, p));
         continue;
@@ -377,7 +377,7 @@ int tune_step(const StepArgs& a0, int precision, cudaStream_t s, int* variant, i
     cands.push_back({9, 0});
   if (precision == KPMGB_PREC_FF &&
       (select_kernel_ffr(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->max_row_nnz, a0.H->ell_w) ||
-       select_kernel_ffc(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->ell_w)))
+       select_kernel_ffc(a0.NR, a0.dot, a0.H->is_real != 0, a0.H->ell_w, a0.H->max_row_nnz)))
     cands.push_back({11, 0});
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   KPMGB_CUDA(cudaEventCreate(&e0));

@@ -740,7 +740,7 @@ KernelFn select_kernel_ffr(int ncols, int dot, bool real, int max_row_nnz, int e
 // Row-streaming float-float kernel for complex operators over padded rows of
 // stride 8 or 12 (kpmgb_step_ffe.cu): 9..32 columns, one column per lane;
 // nullptr otherwise.  ffc_lanes: lanes per row (16 or 32).
-KernelFn select_kernel_ffc(int ncols, int dot, bool real, int ell_w);
+KernelFn select_kernel_ffc(int ncols, int dot, bool real, int ell_w, int max_row_nnz);
 int ffc_lanes(int ncols);
 // Row-streaming float-float kernel on packed FP32 pairs (kpmgb_step_ffpk.cu):
 // real operators, exactly 64 columns, doubling dots, rows of 5..8 nonzeros,

@@ -450,7 +450,9 @@ KernelFn select_kernel_ffr(int ncols, int dot, bool real, int max_row_nnz, int e
 // values are staged in shared memory with cp.async while the current rows are
 // computed, and the row's z, own x (and bra) and every gather are issued
 // before the arithmetic, as in k_step_ffr.  Doubling dots: <x|x> and Re<x|y>.
-template <int LPR, int W, int DOT, bool FULL>
+// WL: slots that may hold nonzeros (the operator's longest row), the rest of
+// the W-slot row is padding that every row shares and that is skipped.
+template <int LPR, int W, int DOT, bool FULL, int WL = W>
 __global__ void __launch_bounds__(kThreads, 2) k_step_ffc(KParams p) {
   pdl_enter();
   constexpr int RPW = 32 / LPR;                 // rows per warp
@@ -510,20 +512,20 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffc(KParams p) {
     const float4* hrow = &sidx[warp][buf][sub][W / 4];
     const int64_t base = r * ld + p.c0 + lg;
     const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-    float4 zv = zero, xo = zero, bo = zero, xv[W];
+    float4 zv = zero, xo = zero, bo = zero, xv[WL];
     if (row_ok && live) {
       if (beta_mode != 0) zv = __ldcs(z + base);
       if (DOT == DOT_DOUBLING || DOT == DOT_LR2) xo = __ldg(x + base);
       if (DOT == DOT_LR2 || DOT == DOT_LR1) bo = __ldg(bra + base);
 #pragma unroll
-      for (int u = 0; u < W; ++u) xv[u] = __ldg(x + (int64_t)jrow[u] * ld + p.c0 + lg);
+      for (int u = 0; u < WL; ++u) xv[u] = __ldg(x + (int64_t)jrow[u] * ld + p.c0 + lg);
     } else {
 #pragma unroll
-      for (int u = 0; u < W; ++u) xv[u] = zero;
+      for (int u = 0; u < WL; ++u) xv[u] = zero;
     }
     float R = 0.f, M = 0.f;
 #pragma unroll
-    for (int u = 0; u < W; ++u) {
+    for (int u = 0; u < WL; ++u) {
       const float4 h = hrow[u];
       R = __fadd_rn(R, habs(h));
       M = fmaxf(M, fmaxf(fabsf(xv[u].x), fabsf(xv[u].z)));
@@ -532,7 +534,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffc(KParams p) {
     const float sig = __fmul_rn(6.0f, ff::pow2_floor(B));
     float Ar = sig, Ai = sig, cr = 0.f, ci = 0.f;
 #pragma unroll
-    for (int u = 0; u < W; ++u) ffmac(Ar, cr, Ai, ci, hrow[u], xv[u]);
+    for (int u = 0; u < WL; ++u) ffmac(Ar, cr, Ai, ci, hrow[u], xv[u]);
     __syncwarp();  // the buffer is restaged two tiles later
     buf ^= 1;
     if (row_ok && live) {
@@ -591,21 +593,39 @@ KernelFn ffc_dot(int dot) {
   }
 }
 
+// Steps without dots (kpm_2d's chains and current applications) on full
+// lane groups skip the padding slots past the longest row.
+template <int LPR, int W>
+KernelFn ffc_live(int live) {
+  switch (W - live) {
+    case 0: return k_step_ffc<LPR, W, DOT_NONE, true, W>;
+    case 1: return k_step_ffc<LPR, W, DOT_NONE, true, W - 1>;
+    case 2: return k_step_ffc<LPR, W, DOT_NONE, true, W - 2>;
+    default: return k_step_ffc<LPR, W, DOT_NONE, true, W - 3>;
+  }
+}
+
 template <int LPR>
-KernelFn ffc_w(int ncols, int dot, int ell_w) {
+KernelFn ffc_w(int ncols, int dot, int ell_w, int max_row_nnz) {
   const bool full = ncols == LPR;
+  const bool live = full && dot == DOT_NONE && max_row_nnz >= 1 && max_row_nnz <= ell_w;
   switch (ell_w) {
-    case 8: return full ? ffc_dot<LPR, 8, true>(dot) : ffc_dot<LPR, 8, false>(dot);
-    case 12: return full ? ffc_dot<LPR, 12, true>(dot) : ffc_dot<LPR, 12, false>(dot);
+    case 8:
+      if (live) return ffc_live<LPR, 8>(std::max(max_row_nnz, 5));
+      return full ? ffc_dot<LPR, 8, true>(dot) : ffc_dot<LPR, 8, false>(dot);
+    case 12:
+      if (live) return ffc_live<LPR, 12>(std::max(max_row_nnz, 9));
+      return full ? ffc_dot<LPR, 12, true>(dot) : ffc_dot<LPR, 12, false>(dot);
     default: return nullptr;
   }
 }
 
 }  // namespace
 
-KernelFn select_kernel_ffc(int ncols, int dot, bool real, int ell_w) {
+KernelFn select_kernel_ffc(int ncols, int dot, bool real, int ell_w, int max_row_nnz) {
   if (real || ncols < 9 || ncols > 32) return nullptr;
-  return ncols <= 16 ? ffc_w<16>(ncols, dot, ell_w) : ffc_w<32>(ncols, dot, ell_w);
+  return ncols <= 16 ? ffc_w<16>(ncols, dot, ell_w, max_row_nnz)
+                     : ffc_w<32>(ncols, dot, ell_w, max_row_nnz);
 }
 
 int ffc_lanes(int ncols) { return ncols <= 16 ? 16 : 32; }
