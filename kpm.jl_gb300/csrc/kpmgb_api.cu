@@ -214,7 +214,8 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
   }();
   const bool paired = paired_on && ff && !lr && !auto_cluster && (variant == 0 || variant == 11) &&
                       packed_step_applies(op->csr, (int)NR);
-  KPMGB_TRY(launch_load_block(psi_r, sl[0], NH, (int)NR, precision, sc, false, s, paired));
+  KPMGB_TRY(launch_load_block(psi_r, sl[0], NH, (int)NR, precision, sc, false, s,
+                              paired ? VEC_PAIRED : VEC_STD));
   if (lr) KPMGB_TRY(launch_load_block(psi_l, ws.bra.ptr, NH, (int)NR, precision, sc + NR, false, s));
   const double* mom_scale = nullptr;
   if (ff) {
@@ -462,10 +463,25 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
   auto R = [&](int64_t i) { return (void*)(ws.right.as<char>() + i * block); };
   auto RING = [&](int64_t i) { return (void*)(ws.ring.as<char>() + i * block); };
   double* sc = ws.scales.as<double>();
+  // Float-float calls with the split contraction on complex H, Ja, Jb of at
+  // most 12 nonzeros per row and 16 or 32 probe columns keep their vectors in
+  // the column-pair layout and run every step on column pairs
+  // (k_step_ffcp); the contraction sums over memory order, the same
+  // permutation of K on both sides.  KPMGB_COLPAIR=0 keeps the standard
+  // layout.
+  static const bool colpair_on = [] {
+    const char* e = std::getenv("KPMGB_COLPAIR");
+    return !(e && std::atoi(e) == 0);
+  }();
+  const bool colpair = colpair_on && ff && opt.contraction == KPMGB_CONTRACT_SPLIT &&
+                       colpair_step_applies(H->csr, (int)NR) &&
+                       colpair_step_applies(Ja->csr, (int)NR) &&
+                       colpair_step_applies(Jb->csr, (int)NR);
+  const int layout = colpair ? VEC_COLPAIR : VEC_STD;
   // ff: one power-of-two factor per probe block (the contraction sums over
   // columns, so all columns of a block share it)
-  KPMGB_TRY(launch_load_block(psi_l, L(0), NH, (int)NR, precision, sc, true, s));
-  KPMGB_TRY(launch_load_block(psi_r, R(0), NH, (int)NR, precision, sc + NR + 1, true, s));
+  KPMGB_TRY(launch_load_block(psi_l, L(0), NH, (int)NR, precision, sc, true, s, layout));
+  KPMGB_TRY(launch_load_block(psi_r, R(0), NH, (int)NR, precision, sc + NR + 1, true, s, layout));
   const double* dscale = nullptr;
   if (ff) {
     k_mul_scalar<<<1, 1, 0, s>>>(sc + NR, sc + 2 * NR + 1, sc + 2 * NR + 4);
@@ -486,6 +502,7 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
     a.sync = ws.sync.as<unsigned>();
     a.partials = ws.partials.ptr;
     a.partials_bytes = ws.partials.bytes;
+    a.colpair = colpair;
     return launch_step(a, precision, s);
   };
   // right seed Ja psi_r -> ring slot 3 (src/moment.jl:1021)
@@ -555,6 +572,7 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
       c.scratch = ws.gemm.ptr;
       c.scratch_bytes = ws.gemm.bytes;
       c.reuse_l = n1 > 0;  // same left block as the previous contraction of this rep
+      c.colpair = colpair;
       KPMGB_TRY(launch_contract(c, precision, opt.contraction, s));
     }
     if (rep < reps - 1) {

@@ -168,16 +168,49 @@ __device__ __forceinline__ void load_pair(const void* base, int64_t idx, float& 
   }
 }
 
+// Four consecutive complex elements kc0..kc0+3 (kc0 a multiple of 4) of a
+// float-float block in the column-pair layout, taken in memory order: two
+// 32-byte blocks, element 2b + s at floats 8b + s + {0, 2, 4, 6}.  Elements
+// at or past `count` read as 0 (count is even).
+__device__ __forceinline__ void load4_colpair(const void* base, int64_t e0, int64_t count,
+                                              float (&rh)[4], float (&rl)[4], float (&ih)[4],
+                                              float (&il)[4]) {
+  const float4* f = static_cast<const float4*>(base);
+#pragma unroll
+  for (int b = 0; b < 2; ++b) {
+    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+    if (2 * b < count) {
+      lo = __ldg(f + (e0 / 2 + b) * 2);      // re.hi, re.hi', re.lo, re.lo'
+      hi = __ldg(f + (e0 / 2 + b) * 2 + 1);  // im.hi, im.hi', im.lo, im.lo'
+    }
+    rh[2 * b] = lo.x; rh[2 * b + 1] = lo.y;
+    rl[2 * b] = lo.z; rl[2 * b + 1] = lo.w;
+    ih[2 * b] = hi.x; ih[2 * b + 1] = hi.y;
+    il[2 * b] = hi.z; il[2 * b + 1] = hi.w;
+  }
+}
+
 // Exponent e of each vector with max |entry| < 2^e (0 for a zero vector).
+// colpair: float-float vectors in the column-pair layout (the high parts are
+// the first two floats of every 16 bytes).
 template <bool FF>
-__global__ void __launch_bounds__(256) k_vec_exp(const void* vecs, int64_t K, int nvec, int* exps) {
+__global__ void __launch_bounds__(256) k_vec_exp(const void* vecs, int64_t K, int nvec, int* exps,
+                                                 bool colpair) {
   const int v = blockIdx.x;
   if (v >= nvec) return;
   float m = 0.f;
-  for (int64_t k = threadIdx.x; k < K; k += 256) {
-    float rh, rl, ih, il;
-    load_pair<FF>(vecs, (int64_t)v * K + k, rh, rl, ih, il);
-    m = fmaxf(m, fmaxf(fabsf(rh), fabsf(ih)));
+  if (FF && colpair) {
+    const float4* f = static_cast<const float4*>(vecs) + (int64_t)v * K;  // K float4 per vector
+    for (int64_t k = threadIdx.x; k < K; k += 256) {
+      const float4 q = __ldg(f + k);
+      m = fmaxf(m, fmaxf(fabsf(q.x), fabsf(q.y)));
+    }
+  } else {
+    for (int64_t k = threadIdx.x; k < K; k += 256) {
+      float rh, rl, ih, il;
+      load_pair<FF>(vecs, (int64_t)v * K + k, rh, rl, ih, il);
+      m = fmaxf(m, fmaxf(fabsf(rh), fabsf(ih)));
+    }
   }
   __shared__ float red[256];
   red[threadIdx.x] = m;
@@ -220,7 +253,7 @@ __device__ __forceinline__ void digits(float vh, float vl, int e, float (&d)[TC_
 template <bool FF, bool IS_B>
 __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int nvec,
                                                const int* exps, int64_t ktiles, int rows_pad,
-                                               uint8_t* planes) {
+                                               uint8_t* planes, bool colpair) {
   constexpr int ROWS = IS_B ? TC_N : TC_M;
   constexpr uint32_t TILE = IS_B ? B_TILE : A_TILE;
   const int64_t groups = ktiles * (TC_KT / 8);
@@ -236,11 +269,20 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
     const int e = exps[v];
     float d[8][TC_SLICES];
     float dq[8][TC_SLICES];  // B' digits (IS_B only)
+    float rh4[4], rl4[4], ih4[4], il4[4];
+    if (FF && colpair) {
+      load4_colpair(vecs, (int64_t)v * K + kp0 / 2, K - kp0 / 2, rh4, rl4, ih4, il4);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t kc = kp0 / 2 + j;  // complex element
+        rh4[j] = rl4[j] = ih4[j] = il4[j] = 0.f;
+        if (kc < K) load_pair<FF>(vecs, (int64_t)v * K + kc, rh4[j], rl4[j], ih4[j], il4[j]);
+      }
+    }
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      const int64_t kc = kp0 / 2 + j;  // complex element
-      float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-      if (kc < K) load_pair<FF>(vecs, (int64_t)v * K + kc, rh, rl, ih, il);
+      const float rh = rh4[j], rl = rl4[j], ih = ih4[j], il = il4[j];
       digits(rh, rl, e, d[2 * j]);
       digits(ih, il, e, d[2 * j + 1]);
       if constexpr (IS_B) {
@@ -570,28 +612,32 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
   // dot product.
   if (!a.reuse_l) {
     if (ff) {
-      k_vec_exp<true><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
+      k_vec_exp<true><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB, a.colpair);
     } else {
-      k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB);
+      k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB, false);
     }
     KPMGB_LAUNCHED();
     if (ff) {
-      k_slice<true, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
+      k_slice<true, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B,
+                                              a.colpair);
     } else {
-      k_slice<false, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B);
+      k_slice<false, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B,
+                                               false);
     }
     KPMGB_LAUNCHED();
   }
   if (ff) {
-    k_vec_exp<true><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
+    k_vec_exp<true><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA, a.colpair);
   } else {
-    k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA);
+    k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA, false);
   }
   KPMGB_LAUNCHED();
   if (ff) {
-    k_slice<true, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A);
+    k_slice<true, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A,
+                                             a.colpair);
   } else {
-    k_slice<false, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A);
+    k_slice<false, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A,
+                                              false);
   }
   KPMGB_LAUNCHED();
   // GEMM

@@ -185,13 +185,25 @@ struct StepArgs {
                              // register-gather kernel; 0 = automatic
   bool paired = false;       // float-float vectors in the paired element layout
                              // (re.hi, im.hi, re.lo, im.lo): the packed kernel
+  bool colpair = false;      // float-float vectors in the column-pair layout
+                             // (VEC_COLPAIR): the column-pair kernel
 };
+
+// Float-float vector layouts of the row-major probe blocks: the standard one
+// (re.hi, re.lo, im.hi, im.lo) per element; the paired one (re.hi, im.hi,
+// re.lo, im.lo) per element; the column-pair one, per row and p < NR/2 a
+// 32-byte block (re.hi, re.hi', re.lo, re.lo', im.hi, im.hi', im.lo, im.lo')
+// of columns p and p + NR/2.
+enum VecLayout : int { VEC_STD = 0, VEC_PAIRED = 1, VEC_COLPAIR = 2 };
 
 // precision: KPMGB_PREC_FP64 or KPMGB_PREC_FF.  Returns KPMGB_OK or an error.
 int launch_step(const StepArgs& a, int precision, cudaStream_t s);
 // Whether float-float doubling steps of NR columns on H can run on packed
 // FP32 pairs over the paired vector layout (StepArgs::paired).
 bool packed_step_applies(const DeviceCSR& H, int NR);
+// Whether float-float steps without dots of NR columns on H can run on
+// column pairs over the column-pair vector layout (StepArgs::colpair).
+bool colpair_step_applies(const DeviceCSR& H, int NR);
 // Autotuning: times every (variant, shape) candidate of the step `a` (which
 // must not write its own inputs: y aliasing neither x nor z) with CUDA events
 // on `s`, after one warm launch each, and returns the fastest in
@@ -208,7 +220,7 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
 // col_scale[0..NR] and col_scale[NR]).
 int launch_load_block(const void* psi_colmajor, void* slot, int64_t NH, int NR,
                       int precision, double* col_scale, bool uniform,
-                      cudaStream_t s, bool paired = false);
+                      cudaStream_t s, int layout = VEC_STD);
 
 // Whole kpm_1d recurrence in one cooperative launch (kpmgb_small.cu); sync[2]
 // must be zero.  small_partials_bytes: the partials it needs for NR columns.
@@ -254,6 +266,8 @@ struct ContractArgs {
   size_t scratch_bytes = 0;
   bool reuse_l = false;   // L (and scratch) unchanged since the previous call:
                           // the split form keeps its L digit planes
+  bool colpair = false;   // float-float R and L in the column-pair layout (the
+                          // split form contracts over memory order)
 };
 int launch_contract(const ContractArgs& a, int precision, int contraction,
                     cudaStream_t s);

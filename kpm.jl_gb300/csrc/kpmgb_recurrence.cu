@@ -254,6 +254,11 @@ size_t step_partials_bytes(const DeviceCSR& H, int64_t NH, int NR, int precision
   return worst;
 }
 
+bool colpair_step_applies(const DeviceCSR& H, int NR) {
+  return NR <= cols_per_launch() &&
+         select_kernel_ffcp(NR, H.is_real != 0, H.ell_w, H.max_row_nnz) != nullptr;
+}
+
 bool packed_step_applies(const DeviceCSR& H, int NR) {
   return NR <= cols_per_launch() &&
          select_kernel_ffpk(NR, H.is_real != 0, H.max_row_nnz, H.ell_w) != nullptr;
@@ -308,6 +313,16 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     // NR=16, kpm_2d 183 ms against 189 ms (exact-length last chunk); the
     // L2-resident 2D Anderson L=64, NR=12, 7.4 ms against 8.3 ms per call
     // (4 lanes x 3 columns against 16 x 1).
+    if (a.colpair) {
+      // the call keeps its vectors in the column-pair layout: only the
+      // column-pair kernel reads them
+      KernelFn fq = precision == KPMGB_PREC_FF && a.dot == DOT_NONE
+                        ? select_kernel_ffcp(p.ncols, H.is_real != 0, H.ell_w, H.max_row_nnz)
+                        : nullptr;
+      if (!fq) return fail(KPMGB_ERR_CUDA, "internal: column-pair layout without its kernel");
+      KPMGB_TRY(launch_step_kernel(fq, grid_for(fq, a.NH, p.ncols / 2), s, p));
+      continue;
+    }
     if (a.paired) {
       // the call keeps its vectors in the paired layout: only the packed
       // kernel reads them
@@ -454,7 +469,7 @@ template <bool FF>
 __global__ void __launch_bounds__(256) k_transpose_in(const double2* __restrict__ psi, void* out,
                                                       int64_t NH, int NR,
                                                       const double* __restrict__ col_scale,
-                                                      bool paired) {
+                                                      int layout) {
   __shared__ double2 tile[32][33];
   const int64_t r0 = (int64_t)blockIdx.x * 32;
   const int c0 = blockIdx.y * 32;
@@ -476,8 +491,18 @@ __global__ void __launch_bounds__(256) k_transpose_in(const double2* __restrict_
         const double f = 1.0 / col_scale[c];
         const float2 re = ff::split_double(v.x * f);
         const float2 im = ff::split_double(v.y * f);
-        static_cast<float4*>(out)[r * NR + c] = paired ? make_float4(re.x, im.x, re.y, im.y)
-                                                       : make_float4(re.x, re.y, im.x, im.y);
+        if (layout == VEC_COLPAIR) {
+          const int half = NR / 2, q = c % half, side = c / half;
+          float* f = static_cast<float*>(out) + (r * half + q) * 8 + side;
+          f[0] = re.x;
+          f[2] = re.y;
+          f[4] = im.x;
+          f[6] = im.y;
+        } else {
+          static_cast<float4*>(out)[r * NR + c] = layout == VEC_PAIRED
+                                                      ? make_float4(re.x, im.x, re.y, im.y)
+                                                      : make_float4(re.x, re.y, im.x, im.y);
+        }
       } else {
         static_cast<double2*>(out)[r * NR + c] = v;
       }
@@ -507,7 +532,9 @@ __global__ void k_copy2(const double2* src, double2* dst, int64_t n) {
 }  // namespace
 
 int launch_load_block(const void* psi, void* slot, int64_t NH, int NR, int precision,
-                      double* col_scale, bool uniform, cudaStream_t s, bool paired) {
+                      double* col_scale, bool uniform, cudaStream_t s, int layout) {
+  if (layout == VEC_COLPAIR && (NR % 2 != 0 || precision != KPMGB_PREC_FF))
+    return fail(KPMGB_ERR_CUDA, "internal: column-pair layout needs float-float and even NR");
   const bool ff = precision == KPMGB_PREC_FF;
   if (ff) {
     k_colnorm2<<<NR, 256, 0, s>>>(static_cast<const double2*>(psi), NH, col_scale);
@@ -520,10 +547,10 @@ int launch_load_block(const void* psi, void* slot, int64_t NH, int NR, int preci
   dim3 grid((unsigned)((NH + 31) / 32), (unsigned)((NR + 31) / 32));
   if (ff)
     k_transpose_in<true><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
-                                              col_scale, paired);
+                                              col_scale, layout);
   else
     k_transpose_in<false><<<grid, 256, 0, s>>>(static_cast<const double2*>(psi), slot, NH, NR,
-                                               nullptr, false);
+                                               nullptr, VEC_STD);
   KPMGB_LAUNCHED();
   return KPMGB_OK;
 }

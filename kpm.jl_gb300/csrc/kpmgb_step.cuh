@@ -756,6 +756,10 @@ struct PackedStep {
   int rows_per_block = 0;
 };
 PackedStep select_packed_step(int ncols, bool real, int max_row_nnz, int ell_w);
+// Complex operators on column pairs (kpmgb_step_ffpk.cu): steps without dots
+// of exactly 16 or 32 columns over padded rows of stride 8 or 12, vectors in
+// the column-pair layout; nullptr otherwise.  Lanes per row: ncols / 2.
+KernelFn select_kernel_ffcp(int ncols, bool real, int ell_w, int max_row_nnz);
 
 }  // namespace step
 }  // namespace kpmgb

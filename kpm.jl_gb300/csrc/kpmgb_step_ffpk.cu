@@ -23,6 +23,9 @@
 // issued before its arithmetic; 2 blocks per SM.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <type_traits>
+
 #include "kpmgb_step.cuh"
 
 namespace kpmgb {
@@ -264,6 +267,204 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
     d[1][c].x += join2(xS[c], xC[c]);
   }
   reduce_finalize<2, 32, CPL>(d, p);
+}
+
+// ---------------------------------------------------------------------------
+// Complex operators on column pairs (k_step_ffcp): kpm_2d's steps without
+// dots (chains and current applications) for 16 or 32 probe columns.  A
+// lane owns columns p and p + NR/2 of a row, and the call stores its vectors
+// in the column-pair layout: per row and p one 32-byte block
+// (re.hi, re.hi', re.lo, re.lo', im.hi, im.hi', im.lo, im.lo') for the two
+// columns, so two 16-byte loads give the {re.hi}, {re.lo}, {im.hi}, {im.lo}
+// pairs of both columns.  Both columns meet the same operator value, so
+// every anchored product of k_step_ffc runs once on the pair: per nonzero
+// 4 packed anchored products for two columns instead of 8 scalar ones.  Rows
+// of up to 8 live slots take one anchored chunk, each lane of a pair then
+// performing k_step_ffc's scalar sequence (y bitwise k_step_ffc's); longer
+// rows take two chunks merged by TwoSum (the gathers of one row and two
+// columns would not fit the registers of two blocks per SM).
+template <int LPH, int W, int WL>
+__global__ void __launch_bounds__(kThreads, 2) k_step_ffcp(KParams p) {
+  pdl_enter();
+  constexpr int RPW = 32 / LPH;            // rows per warp
+  constexpr int GROUPS = kThreads / LPH;   // rows per block tile
+  constexpr int kPieces = W / 4 + W;       // 16-byte pieces of one padded row
+  const int g = threadIdx.x / LPH, lg = threadIdx.x % LPH;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / LPH;              // row of this lane within the warp
+  const ulonglong2* __restrict__ x = static_cast<const ulonglong2*>(p.x);
+  const ulonglong2* z = static_cast<const ulonglong2*>(p.z);
+  ulonglong2* y = static_cast<ulonglong2*>(p.y);
+  const int* __restrict__ ecol = p.ell_col;
+  const float4* __restrict__ eval = static_cast<const float4*>(p.ell_val);
+  const f2 alpha2 = pk(p.alpha_f, p.alpha_f);
+  const int beta_mode = p.beta_mode;
+  const f2 zero2 = pk(0.f, 0.f);
+  // per warp, two buffers of RPW padded rows: W indices then W values each
+  __shared__ __align__(16) float4 sidx[kThreads / 32][2][RPW][kPieces];
+  const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+  auto stage = [&](int64_t t, int b) {
+    for (int q = lane; q < RPW * kPieces; q += 32) {
+      const int rr = q / kPieces, piece = q % kPieces;
+      const int64_t r = t * GROUPS + warp * RPW + rr;
+      if (t < ntiles && r < p.NH) {
+        const char* src = piece < W / 4
+                              ? reinterpret_cast<const char*>(ecol + r * W) + piece * 16
+                              : reinterpret_cast<const char*>(eval + r * W + (piece - W / 4));
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&sidx[warp][b][rr][piece]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int buf = 0;
+  stage(blockIdx.x, 0);
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    stage(t + gridDim.x, buf ^ 1);
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncwarp();
+    const int64_t r = t * GROUPS + g;
+    const bool row_ok = r < p.NH;
+    const int* jrow = reinterpret_cast<const int*>(&sidx[warp][buf][sub][0]);
+    const float4* hrow = &sidx[warp][buf][sub][W / 4];
+    // blocks of 32 bytes: [2 q] = {re.hi pair, re.lo pair}, [2 q + 1] = {im.hi, im.lo}
+    const int64_t base = (r * LPH + lg) * 2;
+    const ulonglong2 zero = make_ulonglong2(0ull, 0ull);
+    ulonglong2 z0 = zero, z1 = zero;
+    if (row_ok && beta_mode != 0) {
+      z0 = __ldcs(z + base);
+      z1 = __ldcs(z + base + 1);
+    }
+    // the row's slots in chunks of at most 8 (one anchor each, merged by
+    // TwoSum as in k_step_ff), so that the gathers of a chunk fit the
+    // registers of two blocks per SM
+    constexpr int CA = WL > 8 ? (WL + 1) / 2 : WL;
+    // row sums with the anchors removed: S (leading) + C (correction)
+    f2 Sr = zero2, Si = zero2, Cr = zero2, Ci = zero2;
+    auto chunk = [&](auto first_tag, int u0, auto n_tag) {
+      constexpr int N = decltype(n_tag)::value;
+      constexpr bool FIRST = decltype(first_tag)::value;
+      ulonglong2 g0[N], g1[N];
+      if (row_ok) {
+#pragma unroll
+        for (int u = 0; u < N; ++u) {
+          const int64_t e = ((int64_t)jrow[u0 + u] * LPH + lg) * 2;
+          g0[u] = __ldg(x + e);
+          g1[u] = __ldg(x + e + 1);
+        }
+      } else {
+#pragma unroll
+        for (int u = 0; u < N; ++u) g0[u] = g1[u] = zero;
+      }
+      float R = 0.f, M0 = 0.f, M1 = 0.f;
+#pragma unroll
+      for (int u = 0; u < N; ++u) {
+        const float4 h = hrow[u0 + u];
+        R = __fadd_rn(R, __fadd_rn(fabsf(h.x), fabsf(h.z)));
+        float a0, a1, b0, b1;
+        upk(g0[u].x, a0, a1);
+        upk(g1[u].x, b0, b1);
+        M0 = fmaxf(M0, fmaxf(fabsf(a0), fabsf(b0)));
+        M1 = fmaxf(M1, fmaxf(fabsf(a1), fabsf(b1)));
+      }
+      const float s0 =
+          __fmul_rn(6.0f, ff::pow2_floor(__fmul_rn(__fmul_rn(R, M0), 1.0f + 0x1p-14f)));
+      const float s1 =
+          __fmul_rn(6.0f, ff::pow2_floor(__fmul_rn(__fmul_rn(R, M1), 1.0f + 0x1p-14f)));
+      const f2 sg = pk(s0, s1);
+      f2 ar = sg, ai = sg, cr = zero2, ci = zero2;
+#pragma unroll
+      for (int u = 0; u < N; ++u) {
+        const float4 h = hrow[u0 + u];
+        const f2 hrh = pk(h.x, h.x), hrl = pk(h.y, h.y);
+        const f2 hih = pk(h.z, h.z), hil = pk(h.w, h.w);
+        const f2 nih = pk(-h.z, -h.z), nil = pk(-h.w, -h.w);
+        amac2(ar, cr, hrh, hrl, g0[u].x, g0[u].y);  // re += h.re x.re
+        amac2(ar, cr, nih, nil, g1[u].x, g1[u].y);  // re -= h.im x.im
+        amac2(ai, ci, hrh, hrl, g1[u].x, g1[u].y);  // im += h.re x.im
+        amac2(ai, ci, hih, hil, g0[u].x, g0[u].y);  // im += h.im x.re
+      }
+      // the anchor leaves exactly (Sterbenz: the accumulator stayed in the
+      // anchor's binade); later chunks merge by TwoSum as in k_step_ff
+      const f2 sr = sub2(ar, sg), si = sub2(ai, sg);
+      if constexpr (FIRST) {
+        Sr = sr;
+        Si = si;
+        Cr = cr;
+        Ci = ci;
+      } else {
+        f2 s, e;
+        two_sum2(Sr, sr, s, e);
+        Sr = s;
+        Cr = add2(Cr, add2(cr, e));
+        two_sum2(Si, si, s, e);
+        Si = s;
+        Ci = add2(Ci, add2(ci, e));
+      }
+    };
+    chunk(std::true_type{}, 0, std::integral_constant<int, CA>{});
+    if constexpr (WL > CA) chunk(std::false_type{}, CA, std::integral_constant<int, WL - CA>{});
+    __syncwarp();  // the buffer is restaged two tiles later
+    buf ^= 1;
+    if (row_ok) {
+      f2 out[4];
+#pragma unroll
+      for (int part = 0; part < 2; ++part) {
+        const f2 S = part == 0 ? Sr : Si;
+        const f2 C = part == 0 ? Cr : Ci;
+        const ulonglong2 zz = part == 0 ? z0 : z1;
+        const f2 u2 = mul2(alpha2, S);
+        const f2 c2 = mul2(alpha2, C);
+        f2 yh, yl;
+        if (beta_mode == 0) {
+          two_sum2(u2, c2, yh, yl);
+        } else {
+          f2 s2, e2;
+          if (beta_mode > 0) {
+            two_sum2(u2, zz.x, s2, e2);
+            two_sum2(s2, add2(e2, add2(c2, zz.y)), yh, yl);
+          } else {
+            s2 = sub2(u2, zz.x);
+            const f2 bb = sub2(s2, u2);
+            e2 = sub2(sub2(u2, sub2(s2, bb)), add2(zz.x, bb));
+            two_sum2(s2, add2(e2, sub2(c2, zz.y)), yh, yl);
+          }
+        }
+        out[2 * part] = yh;
+        out[2 * part + 1] = yl;
+      }
+      __stcs(y + base, make_ulonglong2(out[0], out[1]));
+      __stcs(y + base + 1, make_ulonglong2(out[2], out[3]));
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
+namespace {
+template <int LPH, int W>
+KernelFn ffcp_live(int live) {
+  switch (W - live) {
+    case 0: return k_step_ffcp<LPH, W, W>;
+    case 1: return k_step_ffcp<LPH, W, W - 1>;
+    case 2: return k_step_ffcp<LPH, W, W - 2>;
+    default: return k_step_ffcp<LPH, W, W - 3>;
+  }
+}
+template <int LPH>
+KernelFn ffcp_w(int ell_w, int max_row_nnz) {
+  switch (ell_w) {
+    case 8: return ffcp_live<LPH, 8>(std::max(max_row_nnz, 5));
+    case 12: return ffcp_live<LPH, 12>(std::max(max_row_nnz, 9));
+    default: return nullptr;
+  }
+}
+}  // namespace
+
+KernelFn select_kernel_ffcp(int ncols, bool real, int ell_w, int max_row_nnz) {
+  if (real || max_row_nnz < 1 || max_row_nnz > ell_w) return nullptr;
+  if (ncols == 16) return ffcp_w<8>(ell_w, max_row_nnz);
+  if (ncols == 32) return ffcp_w<16>(ell_w, max_row_nnz);
+  return nullptr;
 }
 
 KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {

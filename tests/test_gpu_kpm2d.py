@@ -164,3 +164,53 @@ def test_split_contraction_large_k():
     m64 = kg.kpm_2d(*ops, 64, 16, NH, psi_in=psi)
     msp = kg.kpm_2d(*ops, 64, 16, NH, psi_in=psi, contraction="split")
     assert relerr(msp, m64) < 1e-9
+
+
+@pytest.mark.parametrize("NR", [16, 32])
+@pytest.mark.parametrize("case", ["haldane", "peierls8"])
+@pytest.mark.parametrize("kw", [{}, {"arr_size": 6, "right_block": 4},
+                                {"moment_parity": "ODD"}, {"mn_sym": True}])
+def test_column_pair_path_matches_oracle(NR, case, kw):
+    """Float-float + split contraction with 16 or 32 probe columns on complex
+    operators of at most 12 nonzeros per row runs the column-pair layout
+    (k_step_ffcp: rows of up to 8 live slots in one anchored chunk, longer
+    rows in two); against the blocked oracle and the FP64 path, with small
+    blocks (left-chain wrap, right blocks recomputed), parity masks and
+    mn_sym."""
+    rng = np.random.default_rng(NR + len(case) + len(kw))
+    if case == "haldane":
+        H, Jx, Jy, _ = models.haldane(8, 8, t2=0.15, m=0.1)       # 10 nonzeros per row
+        Hn = (H / 3.6).tocsc()
+    else:
+        Hn = (_peierls(8, rng) / 4.3).tocsc()                     # 5 nonzeros per row
+        Jx = (1j * Hn).tocsc()
+        Jy = ((0.3 - 0.7j) * Hn.conj()).tocsc()
+    NH = Hn.shape[0]
+    NC = 24
+    pl = ko.random_phase_vectors(rng, NH, NR)
+    pr = ko.random_phase_vectors(rng, NH, NR)
+    ref = ko.kpm_2d(Hn, Jx, Jy, NC, pl, pr, NC, NC,
+                    moment_parity=kw.get("moment_parity", "NONE"), mn_sym=kw.get("mn_sym", False))
+    got = kg.kpm_2d(Hn, Jx, Jy, NC, NR, NH, psi_in_l=pl, psi_in_r=pr, precision="ff",
+                    contraction="split", **kw)
+    f64 = kg.kpm_2d(Hn, Jx, Jy, NC, NR, NH, psi_in_l=pl, psi_in_r=pr, **kw)
+    assert relerr(got, ref) < TOL["ff"]
+    assert relerr(got, f64) < TOL["ff"]
+
+
+def _peierls(L, rng):
+    """Square lattice with random U(1) phases on the bonds (complex, 5 per row)."""
+    n = L * L
+    rows, cols, vals = [], [], []
+    for i in range(L):
+        for j in range(L):
+            s = i * L + j
+            for t in (((i + 1) % L) * L + j, i * L + (j + 1) % L):
+                ph = np.exp(2j * np.pi * rng.random())
+                rows += [s, t]
+                cols += [t, s]
+                vals += [-ph, -np.conj(ph)]
+            rows.append(s)
+            cols.append(s)
+            vals.append(rng.uniform(-0.5, 0.5))
+    return sp.csc_matrix((vals, (rows, cols)), shape=(n, n))
