@@ -312,6 +312,85 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
   }
 }
 
+// The same slicing for blocks of 8 consecutive vectors (an 8-row core-matrix
+// group; nvec a multiple of 8) and 32 consecutive groups of 8 K' elements:
+// warp w reads vector v0 + w (each lane 64 contiguous bytes, the warp
+// 2 KB), the digit pieces meet in shared memory, and each store instruction
+// then writes whole 128-byte core-matrix rows (two 256-byte runs per warp)
+// instead of one 16-byte piece per row.
+template <bool FF, bool IS_B>
+__global__ void __launch_bounds__(256) k_slice8(const void* vecs, int64_t K, int nvec,
+                                                const int* exps, int64_t ktiles,
+                                                uint8_t* planes, bool colpair) {
+  constexpr int ROWS = IS_B ? TC_N : TC_M;
+  constexpr uint32_t TILE = IS_B ? B_TILE : A_TILE;
+  constexpr int NSET = IS_B ? 2 : 1;  // B: rows v and nvec + v
+  // [..][group][row]: the row index padded to 9 so that a warp's stores
+  // (one row, 32 groups) fall on distinct banks
+  __shared__ __align__(16) uint4 piece[NSET][TC_SLICES][32][9];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int v0 = blockIdx.y * 8;
+  const int64_t groups = ktiles * (TC_KT / 8);
+  const int64_t g0 = (int64_t)blockIdx.x * 32;
+  const int v = v0 + w;
+  const int64_t g = g0 + l;
+  if (g < groups) {
+    const int64_t kp0 = g * 8;  // first real K' element
+    const int e = exps[v];
+    float rh4[4], rl4[4], ih4[4], il4[4];
+    if (FF && colpair) {
+      load4_colpair(vecs, (int64_t)v * K + kp0 / 2, K - kp0 / 2, rh4, rl4, ih4, il4);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t kc = kp0 / 2 + j;
+        rh4[j] = rl4[j] = ih4[j] = il4[j] = 0.f;
+        if (kc < K) load_pair<FF>(vecs, (int64_t)v * K + kc, rh4[j], rl4[j], ih4[j], il4[j]);
+      }
+    }
+    float d[8][TC_SLICES];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      digits(rh4[j], rl4[j], e, d[2 * j]);
+      digits(ih4[j], il4[j], e, d[2 * j + 1]);
+    }
+#pragma unroll
+    for (int i = 0; i < TC_SLICES; ++i) {
+      __nv_bfloat16 h[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(ldexpf(d[q][i], -8 * i));
+      piece[0][i][l][w] = *reinterpret_cast<const uint4*>(h);
+      if constexpr (IS_B) {
+        // B' row: (-Im, Re) per complex element
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          h[2 * j] = __float2bfloat16_rn(ldexpf(-d[2 * j + 1][i], -8 * i));
+          h[2 * j + 1] = __float2bfloat16_rn(ldexpf(d[2 * j][i], -8 * i));
+        }
+        piece[NSET - 1][i][l][w] = *reinterpret_cast<const uint4*>(h);
+      }
+    }
+  }
+  __syncthreads();
+  // write phase: rows fastest, then groups (kin 0 and 8 are adjacent 128-byte
+  // rows of one 256-byte run), then planes
+#pragma unroll
+  for (int set = 0; set < NSET; ++set) {
+    const int row0 = set == 0 ? v0 : nvec + v0;
+    const int tile = row0 / ROWS, r0 = row0 % ROWS;
+    for (int q = threadIdx.x; q < TC_SLICES * 32 * 8; q += 256) {
+      const int rr = q & 7, gl = (q >> 3) & 31, i = q >> 8;
+      const int64_t gg = g0 + gl;
+      if (gg >= groups) continue;
+      const int64_t kt = gg / (TC_KT / 8);
+      const int kin = (int)(gg % (TC_KT / 8)) * 8;
+      uint8_t* tbase = planes + (size_t)(tile * ktiles + kt) * (TC_SLICES * TILE);
+      *reinterpret_cast<uint4*>(tbase + tile_off<TC_SLICES * ROWS>(i * ROWS + r0 + rr, kin)) =
+          piece[set][i][gl][rr];
+    }
+  }
+}
+
 // --------------------------------------------------------------- GEMM
 struct TcArgs {
   const uint8_t* A;      // planes [mtiles][ktiles][A_STAGE]
@@ -617,7 +696,13 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
       k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB, false);
     }
     KPMGB_LAUNCHED();
-    if (ff) {
+    if (a.nl % 8 == 0) {
+      const dim3 g8((unsigned)((pl.ktiles * (TC_KT / 8) + 31) / 32), (unsigned)(a.nl / 8));
+      if (ff)
+        k_slice8<true, true><<<g8, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, B, a.colpair);
+      else
+        k_slice8<false, true><<<g8, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, B, false);
+    } else if (ff) {
       k_slice<true, true><<<gB, 256, 0, s>>>(a.L, a.K, a.nl, expB, pl.ktiles, rowsB, B,
                                               a.colpair);
     } else {
@@ -632,7 +717,13 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
     k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA, false);
   }
   KPMGB_LAUNCHED();
-  if (ff) {
+  if (a.nr % 8 == 0) {
+    const dim3 g8((unsigned)((pl.ktiles * (TC_KT / 8) + 31) / 32), (unsigned)(a.nr / 8));
+    if (ff)
+      k_slice8<true, false><<<g8, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, A, a.colpair);
+    else
+      k_slice8<false, false><<<g8, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, A, false);
+  } else if (ff) {
     k_slice<true, false><<<gA, 256, 0, s>>>(a.R, a.K, a.nr, expA, pl.ktiles, rowsA, A,
                                              a.colpair);
   } else {
