@@ -452,7 +452,9 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
   KPMGB_TRY(ws.left.ensure(KLa * block));
   KPMGB_TRY(ws.right.ensure(KRa * block));
   KPMGB_TRY(ws.ring.ensure(4 * block));
-  KPMGB_TRY(ws.scales.ensure((size_t)(2 * NR + 8) * sizeof(double)));
+  // scales, then the per-vector maxima of the L and R blocks (column pairs)
+  const size_t scale_bytes = (size_t)(2 * NR + 8) * sizeof(double);
+  KPMGB_TRY(ws.scales.ensure(scale_bytes + (size_t)(KLa + KRa) * sizeof(unsigned)));
   KPMGB_TRY(ws.partials.ensure(step_partials_bytes(H->csr, NH, (int)NR, precision)));
   const size_t cs = contract_scratch_bytes(K, (int)KRa, (int)KLa, precision, opt.contraction);
   KPMGB_TRY(ws.gemm.ensure(cs));
@@ -488,8 +490,18 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
     KPMGB_LAUNCHED();
     dscale = sc + 2 * NR + 4;
   }
+  // column pairs: the kernels that write the L and R blocks also gather each
+  // vector's largest |high part| (the split contraction's exponents), so the
+  // contraction skips its own scan of the blocks
+  unsigned* maxL = colpair ? reinterpret_cast<unsigned*>(ws.scales.as<char>() + scale_bytes)
+                           : nullptr;
+  unsigned* maxR = colpair ? maxL + KLa : nullptr;
+  auto zero_max = [&](unsigned* m, int64_t n) -> int {
+    if (m && n > 0) KPMGB_CUDA(cudaMemsetAsync(m, 0, (size_t)n * sizeof(unsigned), s));
+    return KPMGB_OK;
+  };
   auto apply = [&](const DeviceCSR* op, const void* x, const void* z, void* y, double alpha,
-                   double beta) {
+                   double beta, unsigned* vmax = nullptr) {
     StepArgs a;
     a.H = op;
     a.NH = NH;
@@ -503,12 +515,17 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
     a.partials = ws.partials.ptr;
     a.partials_bytes = ws.partials.bytes;
     a.colpair = colpair;
+    a.vmax = vmax;
     return launch_step(a, precision, s);
   };
   // right seed Ja psi_r -> ring slot 3 (src/moment.jl:1021)
   KPMGB_TRY(apply(&Ja->csr, R(0), nullptr, RING(3), 1.0, 0.0));
   // left seed psi_l, H psi_l (src/moment.jl:1013-1018)
-  if (KLa >= 2) KPMGB_TRY(apply(&H->csr, L(0), nullptr, L(1), 1.0, 0.0));
+  if (colpair) KPMGB_TRY(launch_vec_absmax(L(0), K, 1, maxL, s));
+  if (KLa >= 2) {
+    KPMGB_TRY(zero_max(colpair ? maxL + 1 : nullptr, 1));
+    KPMGB_TRY(apply(&H->csr, L(0), nullptr, L(1), 1.0, 0.0, colpair ? maxL + 1 : nullptr));
+  }
 
   // right chain v_n = T_n(H) Ja psi_r (v_0 in ring slot 3, v_n in slot n%3),
   // right block entries Jb v_n (src/moment.jl:1034-1052)
@@ -529,9 +546,11 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
     return KPMGB_OK;
   };
   auto fill_right = [&](int64_t n1, int64_t n2) -> int {
+    KPMGB_TRY(zero_max(maxR, n2 - n1 + 1));
     for (int64_t n = n1; n <= n2; ++n) {
       KPMGB_TRY(advance_chain_to(n));
-      KPMGB_TRY(apply(&Jb->csr, right_vec(n), nullptr, R(n - n1), 1.0, 0.0));
+      KPMGB_TRY(apply(&Jb->csr, right_vec(n), nullptr, R(n - n1), 1.0, 0.0,
+                      colpair ? maxR + (n - n1) : nullptr));
     }
     return KPMGB_OK;
   };
@@ -545,8 +564,9 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
     const int64_t m1 = rep * KL;
     const int64_t m2 = std::min<int64_t>(m1 + KL, NC);  // exclusive
     const int64_t rep_size = m2 - m1;
+    KPMGB_TRY(zero_max(colpair ? maxL + 2 : nullptr, rep_size - 2));
     for (int64_t i = 2; i < rep_size; ++i)
-      KPMGB_TRY(apply(&H->csr, L(i - 1), L(i - 2), L(i), 2.0, -1.0));
+      KPMGB_TRY(apply(&H->csr, L(i - 1), L(i - 2), L(i), 2.0, -1.0, colpair ? maxL + i : nullptr));
     const int64_t nmax = opt.mn_sym ? m2 : NC;  // exclusive
     for (int64_t n1 = 0; n1 < nmax; n1 += KR) {
       const int64_t n2 = std::min<int64_t>(n1 + KR, nmax);  // exclusive
@@ -573,13 +593,16 @@ int run_kpm2d(Operator* H, Operator* Ja, Operator* Jb, int64_t NC, int64_t NR, i
       c.scratch_bytes = ws.gemm.bytes;
       c.reuse_l = n1 > 0;  // same left block as the previous contraction of this rep
       c.colpair = colpair;
+      c.maxR = colpair ? (right_resident ? maxR + n1 : maxR) : nullptr;
+      c.maxL = maxL;
       KPMGB_TRY(launch_contract(c, precision, opt.contraction, s));
     }
     if (rep < reps - 1) {
       // continue the left chain past the ring (chebyshev_iter_wrap,
       // src/utils/chebyshev_iteration.jl:31-34)
-      KPMGB_TRY(apply(&H->csr, L(KL - 1), L(KL - 2), L(0), 2.0, -1.0));
-      KPMGB_TRY(apply(&H->csr, L(0), L(KL - 1), L(1), 2.0, -1.0));
+      KPMGB_TRY(zero_max(maxL, 2));
+      KPMGB_TRY(apply(&H->csr, L(KL - 1), L(KL - 2), L(0), 2.0, -1.0, maxL));
+      KPMGB_TRY(apply(&H->csr, L(0), L(KL - 1), L(1), 2.0, -1.0, colpair ? maxL + 1 : nullptr));
     }
   }
   if (opt.mn_sym) KPMGB_TRY(launch_mn_sym(mu, (int)NC, s));

@@ -230,6 +230,37 @@ __global__ void __launch_bounds__(256) k_vec_exp(const void* vecs, int64_t K, in
   }
 }
 
+// Largest |high part| of column-pair vectors (float bits), and the exponent
+// of a gathered maximum (as k_vec_exp).
+__global__ void __launch_bounds__(256) k_vec_absmax(const void* vecs, int64_t K, int nvec,
+                                                    unsigned* out) {
+  const int v = blockIdx.x;
+  if (v >= nvec) return;
+  const float4* f = static_cast<const float4*>(vecs) + (int64_t)v * K;
+  float m = 0.f;
+  for (int64_t k = threadIdx.x; k < K; k += 256) {
+    const float4 q = __ldg(f + k);
+    m = fmaxf(m, fmaxf(fabsf(q.x), fabsf(q.y)));
+  }
+  __shared__ float red[256];
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[v] = __float_as_uint(red[0]);
+}
+
+__global__ void k_max_to_exp(const unsigned* mx, int n, int* exps) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float m = __uint_as_float(mx[i]);
+    int e = 0;
+    if (m > 0.f && isfinite(m)) frexpf(m, &e);
+    exps[i] = e;
+  }
+}
+
 // Five signed base-256 digits of the scaled value (vh + vl) * 2^(7-e).  The
 // value is first made an integer, N = round(vh 2^(39-e)) + round(vl 2^(39-e))
 // (|N| <= 2^39; within one unit, 2^-39 of the vector maximum), so no digit
@@ -654,6 +685,13 @@ size_t part_bound_bytes(const TcPlan& pl) {
 
 }  // namespace
 
+int launch_vec_absmax(const void* vecs, int64_t K, int nvec, unsigned* out, cudaStream_t s) {
+  if (nvec < 1) return KPMGB_OK;
+  k_vec_absmax<<<nvec, 256, 0, s>>>(vecs, K, nvec, out);
+  KPMGB_LAUNCHED();
+  return KPMGB_OK;
+}
+
 size_t contract_split_scratch_bytes(int64_t K, int nr, int nl) {
   // the largest plan over sub-blocks nr' <= nr, nl' <= nl is the full block's
   // (plane sizes grow with nr, nl; partials within part_bound_bytes)
@@ -690,7 +728,9 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
   // rows and columns that the epilogue discards, each output being its own
   // dot product.
   if (!a.reuse_l) {
-    if (ff) {
+    if (a.maxL) {
+      k_max_to_exp<<<(a.nl + 255) / 256, 256, 0, s>>>(a.maxL, a.nl, expB);
+    } else if (ff) {
       k_vec_exp<true><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB, a.colpair);
     } else {
       k_vec_exp<false><<<a.nl, 256, 0, s>>>(a.L, a.K, a.nl, expB, false);
@@ -711,7 +751,9 @@ int launch_contract_split(const ContractArgs& a, int precision, cudaStream_t s) 
     }
     KPMGB_LAUNCHED();
   }
-  if (ff) {
+  if (a.maxR) {
+    k_max_to_exp<<<(a.nr + 255) / 256, 256, 0, s>>>(a.maxR, a.nr, expA);
+  } else if (ff) {
     k_vec_exp<true><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA, a.colpair);
   } else {
     k_vec_exp<false><<<a.nr, 256, 0, s>>>(a.R, a.K, a.nr, expA, false);

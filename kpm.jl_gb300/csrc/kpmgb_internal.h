@@ -178,6 +178,8 @@ struct StepArgs {
   const double* mom_scale = nullptr;  // per-column factor applied to the dots
   double growth_limit = 0.0; // >0: flag if <x|x> > growth_limit * mu[0] (doubling)
   unsigned* sync = nullptr;  // ticket counter + status word
+  unsigned* vmax = nullptr;  // column-pair steps: the largest |y| high part
+                             // (float bits, atomicMax; zeroed by the caller)
   void* partials = nullptr;
   size_t partials_bytes = 0;  // 0: capacity not checked
   int variant = 0;           // 0 auto, 1 register-gather kernel, 9 padded-row kernel
@@ -268,7 +270,15 @@ struct ContractArgs {
                           // the split form keeps its L digit planes
   bool colpair = false;   // float-float R and L in the column-pair layout (the
                           // split form contracts over memory order)
+  // optional (column-pair layout): the largest |high part| of every R and L
+  // vector, gathered by the kernels that wrote them, in place of the
+  // contraction's own scan
+  const unsigned* maxR = nullptr;
+  const unsigned* maxL = nullptr;
 };
+// The largest |high part| of each of nvec float-float column-pair vectors of
+// K complex elements (float bits written to out).
+int launch_vec_absmax(const void* vecs, int64_t K, int nvec, unsigned* out, cudaStream_t s);
 int launch_contract(const ContractArgs& a, int precision, int contraction,
                     cudaStream_t s);
 size_t contract_scratch_bytes(int64_t K, int nr, int nl, int precision, int contraction);

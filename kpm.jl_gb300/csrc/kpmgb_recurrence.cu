@@ -298,6 +298,7 @@ int launch_step(const StepArgs& a, int precision, cudaStream_t s) {
     p.mom_scale = a.mom_scale;
     p.growth_limit = a.growth_limit;
     p.sync = a.sync;
+    p.vmax = a.vmax;
     p.partials = static_cast<double2*>(a.partials);
     p.partials_cap = (int64_t)(a.partials_bytes / sizeof(double2));
     p.ell_col = H.ell_col;

@@ -120,6 +120,9 @@ struct KParams {
   // the float-float kernels execute no FP64 instruction per row
   float alpha_f;
   int beta_mode;
+  // optional: the largest |high part| of y (float bits, atomicMax) for the
+  // split contraction's exponent (the column-pair kernel only)
+  unsigned* vmax;
 };
 
 template <int DOT>

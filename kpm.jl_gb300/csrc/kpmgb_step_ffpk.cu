@@ -318,6 +318,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffcp(KParams p) {
     asm volatile("cp.async.commit_group;" ::: "memory");
   };
   int buf = 0;
+  float ymax = 0.f;  // largest |high part| of this thread's outputs (p.vmax)
   stage(blockIdx.x, 0);
   for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     stage(t + gridDim.x, buf ^ 1);
@@ -435,9 +436,21 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffcp(KParams p) {
       }
       __stcs(y + base, make_ulonglong2(out[0], out[1]));
       __stcs(y + base + 1, make_ulonglong2(out[2], out[3]));
+      if (p.vmax) {
+        float a0, a1, b0, b1;
+        upk(out[0], a0, a1);
+        upk(out[2], b0, b1);
+        ymax = fmaxf(ymax, fmaxf(fmaxf(fabsf(a0), fabsf(a1)), fmaxf(fabsf(b0), fabsf(b1))));
+      }
     }
   }
   asm volatile("cp.async.wait_group 0;" ::: "memory");
+  if (p.vmax) {
+    // non-negative floats order as their bit patterns
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ymax = fmaxf(ymax, __shfl_xor_sync(0xffffffffu, ymax, off));
+    if (lane == 0) atomicMax(p.vmax, __float_as_uint(ymax));
+  }
 }
 
 namespace {
