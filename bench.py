@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-cond", action="store_true",
                    help="skip the kpm_2d (tensor-core contraction) summary of the headline line")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="skip the c1 / c4 / c5 summary of the headline line")
     p.add_argument("--workload", default="dos",
                    choices=["dos", "dos-small", "cond", "ensemble", "grad", "action", "dsigma",
                             "published"],
@@ -316,6 +318,65 @@ def _time_device(fn, stream, warmup, steps, sync):
     torch.cuda.synchronize()
     sync()
     return e0.elapsed_time(e1) / steps
+
+
+def secondary_summary(args):
+    """Compact numbers of the other benchmark configurations for the headline
+    line: c1 (2D Anderson L=64, NC=1024, NR=12, device-resident), c4 (256
+    ensemble members, NC=512, NR=8, device-resident) and c5 (gradient of a
+    DOS-window loss, graphene 128x128, NC=1024, NR=16, host API)."""
+    import torch
+    import kpm_gb300 as kg
+    from kpm_gb300 import models, rescale
+    out = {}
+    # c1
+    H = models.square_anderson(64, W=2.0, rng=np.random.default_rng(42))
+    h = rescale(H)
+    NH, NR, NC = 4096, 12, 1024
+    psi = kg.random_phase_vectors(np.random.default_rng(42), NH, NR)
+    op = kg.GB300Operator(h.H)
+    st = torch.cuda.Stream()
+    psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
+    mu_t = torch.zeros((NC, NR), dtype=torch.complex128, device="cuda")
+    c1 = {"workload": "kpm_1d, 2D square Anderson L=64 (NH=4096), NC=1024, NR=12"}
+    for prec in ("fp64", "ff"):
+        ms = _time_device(lambda: kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec, stream=st),
+                          st, 3, 10, lambda: kg.sync(op, st))
+        c1[prec] = {"ms_per_call": ms, "value": NR * NC / 2 / (ms / 1e3)}
+    out["c1"] = c1
+    # c4
+    rng = np.random.default_rng(42)
+    Hs, psis = [], []
+    for _ in range(256):
+        L = int(rng.integers(24, 97))
+        W = float(rng.uniform(1.0, 8.0))
+        Hs.append((models.square_anderson(L, W=W, rng=rng) / (4.0 + W / 2 + 0.1)).tocsc())
+        psis.append(kg.random_phase_vectors(rng, L * L, 8))
+    ens = kg.EnsembleOperator(Hs)
+    NC4, NR4 = 512, 8
+    epsi = torch.from_numpy(np.ascontiguousarray(np.vstack(psis).T)).cuda()
+    emu = torch.zeros((256, NC4, NR4), dtype=torch.complex128, device="cuda")
+    cur = torch.cuda.current_stream()
+    c4 = {"workload": "256 x kpm_1d, 2D Anderson L~U{24..96}, NC=512, NR=8 (device-resident)"}
+    for prec in ("fp64", "ff"):
+        ms = _time_device(lambda: kg.kpm_1d_ensemble_device(ens, NC4, epsi, emu, precision=prec),
+                          cur, 1, 3, lambda: kg.sync(ens.op))
+        c4[prec] = {"ms_per_call": ms, "value": 256 * NR4 * NC4 / 2 / (ms / 1e3)}
+    c4["ff_over_fp64"] = c4["fp64"]["ms_per_call"] / c4["ff"]["ms_per_call"]
+    out["c4"] = c4
+    # c5
+    rng = np.random.default_rng(42)
+    NH5 = 2 * 128 * 128
+    H5 = (models.graphene(128, 128, onsite=0.1 * rng.standard_normal(NH5)) / 3.4).tocsc()
+    NC5, NR5 = 1024, 16
+    psi5 = kg.random_phase_vectors(rng, NH5, NR5)
+    g5 = rng.standard_normal(NC5)
+    op5 = kg.GB300Operator(H5)
+    tf = _time_host(lambda: kg.kpm_1d(op5, NC5, NR5, psi_in=psi5), 1, 3)
+    tg = _time_host(lambda: kg.kpm_1d_grad(op5, NC5, psi5, g5), 1, 3)
+    out["c5"] = {"workload": "gradient of sum_m g_m mu_m, graphene 128x128, NC=1024, NR=16",
+                 "forward_ms": tf, "gradient_ms": tg, "gradient_over_forward": tg / tf}
+    return out
 
 
 def _time_host(fn, warmup, steps):
@@ -818,6 +879,10 @@ def main():
     if rank == 0 and world == 1 and not args.no_cond:
         cond = cond_summary(args)
 
+    secondary = None
+    if rank == 0 and world == 1 and not args.no_secondary:
+        secondary = secondary_summary(args)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -834,6 +899,7 @@ def main():
             "plain_fp64": plain,
             "cpu_baseline": cpu,
             "kpm2d_tensor_core": cond,
+            "other_configs": secondary,
             "version": kg.version(),
         }
         if world > 1:
