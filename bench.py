@@ -71,6 +71,7 @@ def parse():
                         "realisations), grad (adjoint gradient on graphene), action "
                         "(chebyshev_action)")
     p.add_argument("--haldane-L", type=int, default=256, help="cond: Haldane cells per side")
+    p.add_argument("--cond-NC", type=int, default=512, help="cond: Chebyshev moments per side")
     p.add_argument("--contraction", default="both", choices=["both", "split", "fp64"],
                    help="cond: which kpm_2d contraction(s) to time")
     return p.parse_args()
@@ -434,13 +435,13 @@ def workload_cond(args):
     Lh = args.haldane_L
     H, Jx, Jy, area = models.haldane(Lh, Lh, t=1.0, t2=0.1)
     h = rescale(H, center=True)
-    NH, NR, NC = H.shape[0], 16, 512
+    NH, NR, NC = H.shape[0], 16, args.cond_NC
     psi = kg.random_phase_vectors(np.random.default_rng(42), NH, NR)
     ops = [kg.GB300Operator(M) for M in (h.H, Jx, Jy)]
     s = torch.cuda.Stream()
     psi_t = torch.from_numpy(np.ascontiguousarray(psi.T)).cuda()
     F = 8.0 * NC * NC * NH * NR
-    out = {"workload": f"kpm_2d, Haldane {Lh}x{Lh}x2 (NH={NH}), t2=0.1i, NC=512, NR=16; "
+    out = {"workload": f"kpm_2d, Haldane {Lh}x{Lh}x2 (NH={NH}), t2=0.1i, NC={NC}, NR=16; "
                        "sigma_xy at 201 Ef",
            "flop_per_call_complex_fp64_equivalent": F}
     mus = {}

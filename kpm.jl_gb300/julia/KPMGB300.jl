@@ -22,7 +22,8 @@ using LinearAlgebra
 using SparseArrays
 import ChainRulesCore
 
-export GB300CSR, dos_moments_ad, cond_moments_ad, kubo_bastin_cond_ad
+export GB300CSR, dos_moments_ad, cond_moments_ad, kubo_bastin_cond_ad, kpm_1d_ensemble,
+       pinned_probes
 
 const libkpmgb = get(ENV, "KPMGB_LIB", joinpath(@__DIR__, "..", "kpm_gb300", "_lib", "libkpmgb.so"))
 
@@ -238,6 +239,39 @@ function kpm_1d_grad(H::SparseMatrixCSC, NC::Int64, psi_in::AbstractMatrix, g::A
                  op.handle, NC, NR, NH, Matrix{ComplexF64}(psi_in), Vector{Float64}(g),
                  checkpoint_every, out))
     return SparseMatrixCSC(size(Hc, 1), size(Hc, 2), copy(Hc.colptr), copy(Hc.rowval), out)
+end
+
+# Batched ensemble: the doubling moments of independent members in one call
+# (kpmgb_kpm1d_ensemble; it replaces a loop of kpm_1d! calls over disorder
+# realisations).  Hs: rescaled members; psis: their NH_i × NR probe blocks
+# (common NR).  Returns one NR × NC moment matrix per member.
+function kpm_1d_ensemble(Hs::AbstractVector{<:SparseMatrixCSC}, NC::Int64,
+                         psis::AbstractVector{<:AbstractMatrix}; precision::Symbol = :fp64)
+    @assert (mod(NC, 2) == 0) "Invalid NC: NC should be even."
+    @assert length(Hs) == length(psis) "one probe block per member"
+    NR = size(psis[1], 2)
+    seg = Int64[0; cumsum([size(H, 1) for H in Hs])]
+    op = GB300CSR(blockdiag((SparseMatrixCSC{ComplexF64,Int64}(H) for H in Hs)...))
+    psi = vcat((Matrix{ComplexF64}(p) for p in psis)...)
+    @assert size(psi) == (seg[end], NR) "every probe block must be (NH_i, NR) with a common NR"
+    out = Array{ComplexF64}(undef, NR, NC, length(Hs))
+    opts = Ref(Kpm1dOptions(_prec(precision), Int32(0), Int32(0), Int32(0)))
+    _check(ccall((:kpmgb_kpm1d_ensemble, libkpmgb), Cint,
+                 (Ptr{Cvoid}, Int32, Ptr{Int64}, Int64, Int64, Ptr{ComplexF64},
+                  Ptr{ComplexF64}, Ref{Kpm1dOptions}),
+                 op.handle, Int32(length(Hs)), seg, NC, NR, psi, out, opts))
+    return [out[:, :, i] for i in 1:length(Hs)]
+end
+
+# Page-locked host buffer for probe blocks (kpmgb_host_alloc): the library
+# reads pinned inputs of 1 MiB or more with a copy kernel over NVLink-C2C.
+function pinned_probes(NH::Integer, NR::Integer)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    _check(ccall((:kpmgb_host_alloc, libkpmgb), Cint, (Int64, Ref{Ptr{Cvoid}}),
+                 Int64(NH) * NR * sizeof(ComplexF64), out))
+    A = unsafe_wrap(Matrix{ComplexF64}, Ptr{ComplexF64}(out[]), (NH, NR); own = false)
+    finalizer(_ -> ccall((:kpmgb_host_free, libkpmgb), Cint, (Ptr{Cvoid},), out[]), A)
+    return A
 end
 
 # Directional derivative of the kpm_1d moments along H + t dH (forward mode):
