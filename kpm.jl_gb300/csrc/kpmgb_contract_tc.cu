@@ -40,6 +40,7 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <type_traits>
 
 #include "kpmgb_internal.h"
 
@@ -232,13 +233,15 @@ __global__ void __launch_bounds__(256) k_vec_exp(const void* vecs, int64_t K, in
 
 // Largest |high part| of column-pair vectors (float bits), and the exponent
 // of a gathered maximum (as k_vec_exp).
+// grid (chunks, nvec): each block folds its strided share of vector
+// blockIdx.y into out[v] (zeroed before) with one atomicMax
 __global__ void __launch_bounds__(256) k_vec_absmax(const void* vecs, int64_t K, int nvec,
                                                     unsigned* out) {
-  const int v = blockIdx.x;
+  const int v = blockIdx.y;
   if (v >= nvec) return;
   const float4* f = static_cast<const float4*>(vecs) + (int64_t)v * K;
   float m = 0.f;
-  for (int64_t k = threadIdx.x; k < K; k += 256) {
+  for (int64_t k = (int64_t)blockIdx.x * 256 + threadIdx.x; k < K; k += (int64_t)gridDim.x * 256) {
     const float4 q = __ldg(f + k);
     m = fmaxf(m, fmaxf(fabsf(q.x), fabsf(q.y)));
   }
@@ -249,7 +252,8 @@ __global__ void __launch_bounds__(256) k_vec_absmax(const void* vecs, int64_t K,
     if (threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) out[v] = __float_as_uint(red[0]);
+  // non-negative floats order as their bit patterns
+  if (threadIdx.x == 0) atomicMax(out + v, __float_as_uint(red[0]));
 }
 
 __global__ void k_max_to_exp(const unsigned* mx, int n, int* exps) {
@@ -267,16 +271,44 @@ __global__ void k_max_to_exp(const unsigned* mx, int n, int* exps) {
 // loses the low half's bits to an FP32 rounding; the digits then come off N
 // from the least significant end, balanced: d_i in [-128, 127] for i >= 1 and
 // |d_0| <= 128, with (vh + vl) 2^(7-e) = sum_i d_i 256^-i to that unit.
-__device__ __forceinline__ void digits(float vh, float vl, int e, float (&d)[TC_SLICES]) {
-  long long n = __float2ll_rn(ldexpf(vh, 39 - e)) + __float2ll_rn(ldexpf(vl, 39 - e));
+// `sc` is 2^(39-e) when that is a normal float (then v * sc is the exact
+// scaling), else 0 and the scaling goes through ldexpf.  After two digits the
+// rest of N (|N| < 2^40) fits 32 bits.
+__device__ __forceinline__ void digits(float vh, float vl, int e, float sc,
+                                       float (&d)[TC_SLICES]) {
+  const float xh = sc != 0.f ? __fmul_rn(vh, sc) : ldexpf(vh, 39 - e);
+  const float xl = sc != 0.f ? __fmul_rn(vl, sc) : ldexpf(vl, 39 - e);
+  long long n = __float2ll_rn(xh) + __float2ll_rn(xl);
+  // balanced digits from the least significant end: d = ((n + 128) mod 256)
+  // - 128 in [-128, 127], and n - d is a multiple of 256 (exact shift)
 #pragma unroll
-  for (int i = TC_SLICES - 1; i >= 1; --i) {
-    const int lo = (int)(n & 255);
-    const int di = lo >= 128 ? lo - 256 : lo;
+  for (int i = TC_SLICES - 1; i >= TC_SLICES - 2; --i) {
+    const int di = (((int)n + 128) & 255) - 128;
     d[i] = (float)di;
-    n = (n - di) / 256;  // exact: n - di is a multiple of 256
+    n = (n - di) >> 8;
   }
-  d[0] = (float)n;
+  int m = (int)n;
+#pragma unroll
+  for (int i = TC_SLICES - 3; i >= 1; --i) {
+    const int di = ((m + 128) & 255) - 128;
+    d[i] = (float)di;
+    m = (m - di) >> 8;
+  }
+  d[0] = (float)m;
+}
+
+// 2^(39-e) as a float when it is normal, else 0 (digits() then uses ldexpf).
+__device__ __forceinline__ float digit_scale(int e) {
+  const int k = 39 - e;
+  return (k >= -126 && k <= 127) ? __int_as_float((k + 127) << 23) : 0.f;
+}
+
+// The exact BF16 value of digit d of plane i: d * 2^(-8 i).
+template <int I>
+__device__ __forceinline__ __nv_bfloat16 plane_bf16(float d) {
+  constexpr float kScale = I == 0 ? 1.f : I == 1 ? 0x1p-8f : I == 2 ? 0x1p-16f : I == 3 ? 0x1p-24f
+                                                                                       : 0x1p-32f;
+  return __float2bfloat16_rn(__fmul_rn(d, kScale));
 }
 
 // Write the digit planes of A (R vectors) or B/B' (L vectors) in the
@@ -298,6 +330,7 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
     const int v = (int)(idx - g * nvec);
     const int64_t kp0 = g * 8;  // first real K' element
     const int e = exps[v];
+    const float sc = digit_scale(e);
     float d[8][TC_SLICES];
     float dq[8][TC_SLICES];  // B' digits (IS_B only)
     float rh4[4], rl4[4], ih4[4], il4[4];
@@ -314,8 +347,8 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const float rh = rh4[j], rl = rl4[j], ih = ih4[j], il = il4[j];
-      digits(rh, rl, e, d[2 * j]);
-      digits(ih, il, e, d[2 * j + 1]);
+      digits(rh, rl, e, sc, d[2 * j]);
+      digits(ih, il, e, sc, d[2 * j + 1]);
       if constexpr (IS_B) {
 #pragma unroll
         for (int i = 0; i < TC_SLICES; ++i) {
@@ -329,14 +362,19 @@ __global__ void __launch_bounds__(256) k_slice(const void* vecs, int64_t K, int 
     auto store = [&](int row, float (&dd)[8][TC_SLICES]) {
       const int tile = row / ROWS, r = row % ROWS;
       uint8_t* tbase = planes + (size_t)(tile * ktiles + kt) * (TC_SLICES * TILE);
-#pragma unroll
-      for (int i = 0; i < TC_SLICES; ++i) {
+      auto put = [&](auto plane) {
+        constexpr int i = decltype(plane)::value;
         __nv_bfloat16 h[8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(ldexpf(dd[q][i], -8 * i));
+        for (int q = 0; q < 8; ++q) h[q] = plane_bf16<i>(dd[q][i]);
         *reinterpret_cast<uint4*>(tbase + tile_off<TC_SLICES * ROWS>(i * ROWS + r, kin)) =
             *reinterpret_cast<const uint4*>(h);
-      }
+      };
+      put(std::integral_constant<int, 0>{});
+      put(std::integral_constant<int, 1>{});
+      put(std::integral_constant<int, 2>{});
+      put(std::integral_constant<int, 3>{});
+      put(std::integral_constant<int, 4>{});
     };
     store(v, d);
     if constexpr (IS_B) store(nvec + v, dq);
@@ -368,6 +406,7 @@ __global__ void __launch_bounds__(256) k_slice8(const void* vecs, int64_t K, int
   if (g < groups) {
     const int64_t kp0 = g * 8;  // first real K' element
     const int e = exps[v];
+    const float sc = digit_scale(e);
     float rh4[4], rl4[4], ih4[4], il4[4];
     if (FF && colpair) {
       load4_colpair(vecs, (int64_t)v * K + kp0 / 2, K - kp0 / 2, rh4, rl4, ih4, il4);
@@ -382,25 +421,30 @@ __global__ void __launch_bounds__(256) k_slice8(const void* vecs, int64_t K, int
     float d[8][TC_SLICES];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      digits(rh4[j], rl4[j], e, d[2 * j]);
-      digits(ih4[j], il4[j], e, d[2 * j + 1]);
+      digits(rh4[j], rl4[j], e, sc, d[2 * j]);
+      digits(ih4[j], il4[j], e, sc, d[2 * j + 1]);
     }
-#pragma unroll
-    for (int i = 0; i < TC_SLICES; ++i) {
+    auto put = [&](auto plane) {
+      constexpr int i = decltype(plane)::value;
       __nv_bfloat16 h[8];
 #pragma unroll
-      for (int q = 0; q < 8; ++q) h[q] = __float2bfloat16_rn(ldexpf(d[q][i], -8 * i));
+      for (int q = 0; q < 8; ++q) h[q] = plane_bf16<i>(d[q][i]);
       piece[0][i][l][w] = *reinterpret_cast<const uint4*>(h);
       if constexpr (IS_B) {
         // B' row: (-Im, Re) per complex element
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          h[2 * j] = __float2bfloat16_rn(ldexpf(-d[2 * j + 1][i], -8 * i));
-          h[2 * j + 1] = __float2bfloat16_rn(ldexpf(d[2 * j][i], -8 * i));
+          h[2 * j] = plane_bf16<i>(-d[2 * j + 1][i]);
+          h[2 * j + 1] = plane_bf16<i>(d[2 * j][i]);
         }
         piece[NSET - 1][i][l][w] = *reinterpret_cast<const uint4*>(h);
       }
-    }
+    };
+    put(std::integral_constant<int, 0>{});
+    put(std::integral_constant<int, 1>{});
+    put(std::integral_constant<int, 2>{});
+    put(std::integral_constant<int, 3>{});
+    put(std::integral_constant<int, 4>{});
   }
   __syncthreads();
   // write phase: rows fastest, then groups (kin 0 and 8 are adjacent 128-byte
@@ -687,7 +731,9 @@ size_t part_bound_bytes(const TcPlan& pl) {
 
 int launch_vec_absmax(const void* vecs, int64_t K, int nvec, unsigned* out, cudaStream_t s) {
   if (nvec < 1) return KPMGB_OK;
-  k_vec_absmax<<<nvec, 256, 0, s>>>(vecs, K, nvec, out);
+  KPMGB_CUDA(cudaMemsetAsync(out, 0, (size_t)nvec * sizeof(unsigned), s));
+  const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>((K + 4095) / 4096, 512));
+  k_vec_absmax<<<dim3((unsigned)chunks, (unsigned)nvec), 256, 0, s>>>(vecs, K, nvec, out);
   KPMGB_LAUNCHED();
   return KPMGB_OK;
 }
