@@ -93,10 +93,10 @@ typedef struct kpmgb_kpm1d_options {
                               in distributed shared memory (one launch per
                               call; NH up to ~100k rows); 11: row-streaming
                               padded-row kernels (float-float; real operators
-                              with 33..64 columns and rows of 5..8 nonzeros,
-                              on packed FP32 pairs for exactly 64 columns in
-                              the doubling path; complex operators with 9..32
-                              columns).  Other values fail with
+                              with rows of 5..8 nonzeros: 33..64 columns, and
+                              in the doubling path on packed FP32 pairs 9..32
+                              or exactly 64 columns; complex operators with
+                              9..32 columns).  Other values fail with
                               KPMGB_ERR_ARGUMENT.
                               Automatic selection (0) is the cluster kernel
                               (10) for small operators (float-float:

@@ -270,6 +270,137 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
 }
 
 // ---------------------------------------------------------------------------
+// One column per lane (k_step_ffpk1): the packed row-streaming step for 9..32
+// columns, LPR lanes per row (RPW = 32 / LPR rows per warp), with half the
+// loads per lane of k_step_ffpk and so three blocks per SM.
+template <int LPR, int W>
+__global__ void __launch_bounds__(kThreads, 3) k_step_ffpk1(KParams p) {
+  pdl_enter();
+  constexpr int RPW = 32 / LPR;           // rows per warp
+  constexpr int GROUPS = kThreads / LPR;  // rows per block tile
+  constexpr int kStride = 8;              // padded row stride (ints / float2 values)
+  const int g = threadIdx.x / LPR, lg = threadIdx.x % LPR;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / LPR;             // row of this lane within the warp
+  const bool live = lg < p.ncols;
+  const ulonglong2* __restrict__ x = static_cast<const ulonglong2*>(p.x);
+  const ulonglong2* z = static_cast<const ulonglong2*>(p.z);
+  ulonglong2* y = static_cast<ulonglong2*>(p.y);
+  const int* __restrict__ ecol = p.ell_col;
+  const float2* __restrict__ eval = static_cast<const float2*>(p.ell_val);
+  const f2 alpha2 = pk(p.alpha_f, p.alpha_f);
+  const int beta_mode = p.beta_mode;
+  const int ld = p.ld;
+  const f2 zero2 = pk(0.f, 0.f);
+  __shared__ double2 sacc[kThreads][2];
+  // per warp, two buffers of RPW padded rows: 8 column indices, 8 values
+  __shared__ __align__(16) int sidx[kThreads / 32][2][RPW][3 * kStride];
+  f2 nS = zero2, nC = zero2, xS = zero2, xC = zero2;
+  sacc[threadIdx.x][0] = sacc[threadIdx.x][1] = make_double2(0.0, 0.0);
+  int rows_since_flush = 0;
+  const int64_t ntiles = (p.NH + GROUPS - 1) / GROUPS;
+  // the warp's lanes copy the RPW rows of tile t (6 pieces of 16 bytes each)
+  auto stage = [&](int64_t t, int b) {
+    for (int q = lane; q < RPW * 6; q += 32) {
+      const int rr = q / 6, piece = q % 6;
+      const int64_t r = t * GROUPS + warp * RPW + rr;
+      if (t < ntiles && r < p.NH) {
+        const char* src = piece < 2
+                              ? reinterpret_cast<const char*>(ecol + r * kStride) + piece * 16
+                              : reinterpret_cast<const char*>(eval + r * kStride) + (piece - 2) * 16;
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(&sidx[warp][b][rr][piece * 4]);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  int buf = 0;
+  stage(blockIdx.x, 0);
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    stage(t + gridDim.x, buf ^ 1);
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
+    __syncwarp();
+    const int64_t r = t * GROUPS + g;
+    const bool ok = r < p.NH && live;
+    const int* jrow = &sidx[warp][buf][sub][0];
+    const float4* hrow = reinterpret_cast<const float4*>(&sidx[warp][buf][sub][kStride]);
+    const int64_t e = r * ld + p.c0 + lg;
+    const ulonglong2 zero = make_ulonglong2(0ull, 0ull);
+    ulonglong2 zv = zero, xo = zero, xv[W];
+    if (ok) {
+      if (beta_mode != 0) zv = __ldcs(z + e);
+      xo = __ldg(x + e);
+#pragma unroll
+      for (int u = 0; u < W; ++u) xv[u] = __ldg(x + (int64_t)jrow[u] * ld + p.c0 + lg);
+    } else {
+#pragma unroll
+      for (int u = 0; u < W; ++u) xv[u] = zero;
+    }
+    float hh[8], hl[8];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const float4 v = hrow[q];
+      hh[2 * q] = v.x;
+      hl[2 * q] = v.y;
+      hh[2 * q + 1] = v.z;
+      hl[2 * q + 1] = v.w;
+    }
+    __syncwarp();  // the buffer is restaged two tiles later
+    buf ^= 1;
+    float R = 0.f, M = 0.f;
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      R = __fadd_rn(R, fabsf(hh[u]));
+      float re, im;
+      upk(xv[u].x, re, im);
+      M = fmaxf(M, fmaxf(fabsf(re), fabsf(im)));
+    }
+    const float sig = __fmul_rn(6.0f, ff::pow2_floor(__fmul_rn(__fmul_rn(R, M), 1.0f + 0x1p-14f)));
+    const f2 sig2 = pk(sig, sig);
+    f2 A = sig2, C = zero2;
+#pragma unroll
+    for (int u = 0; u < W; ++u) amac2(A, C, pk(hh[u], hh[u]), pk(hl[u], hl[u]), xv[u].x, xv[u].y);
+    if (ok) {
+      const f2 S = sub2(A, sig2);
+      const f2 u2 = mul2(alpha2, S);
+      const f2 c2 = mul2(alpha2, C);
+      f2 yh, yl;
+      if (beta_mode == 0) {
+        two_sum2(u2, c2, yh, yl);
+      } else {
+        f2 s2, e2;
+        if (beta_mode > 0) {
+          two_sum2(u2, zv.x, s2, e2);
+          two_sum2(s2, add2(e2, add2(c2, zv.y)), yh, yl);
+        } else {
+          s2 = sub2(u2, zv.x);
+          const f2 bb = sub2(s2, u2);
+          e2 = sub2(sub2(u2, sub2(s2, bb)), add2(zv.x, bb));
+          two_sum2(s2, add2(e2, sub2(c2, zv.y)), yh, yl);
+        }
+      }
+      __stcs(y + e, make_ulonglong2(yh, yl));
+      const f2 nxh = sub2(zero2, xo.x);
+      dacc2(nS, nC, xo.x, nxh, xo.y, xo.x, xo.y);
+      dacc2(xS, xC, xo.x, nxh, xo.y, yh, yl);
+    }
+    if (++rows_since_flush == kFlushRows) {
+      rows_since_flush = 0;
+      sacc[threadIdx.x][0].x += join2(nS, nC);
+      sacc[threadIdx.x][1].x += join2(xS, xC);
+      nS = nC = xS = xC = zero2;
+    }
+  }
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  double2 d[2][1];
+  d[0][0] = sacc[threadIdx.x][0];
+  d[0][0].x += join2(nS, nC);
+  d[1][0] = sacc[threadIdx.x][1];
+  d[1][0].x += join2(xS, xC);
+  reduce_finalize<2, LPR, 1>(d, p);
+}
+
+// ---------------------------------------------------------------------------
 // Complex operators on column pairs (k_step_ffcp): kpm_2d's steps without
 // dots (chains and current applications) for 16 or 32 probe columns.  A
 // lane owns columns p and p + NR/2 of a row, and the call stores its vectors
@@ -480,8 +611,24 @@ KernelFn select_kernel_ffcp(int ncols, bool real, int ell_w, int max_row_nnz) {
   return nullptr;
 }
 
+namespace {
+template <int LPR>
+KernelFn ffpk1_w(int max_row_nnz) {
+  switch (max_row_nnz) {
+    case 5: return k_step_ffpk1<LPR, 5>;
+    case 6: return k_step_ffpk1<LPR, 6>;
+    case 7: return k_step_ffpk1<LPR, 7>;
+    case 8: return k_step_ffpk1<LPR, 8>;
+    default: return nullptr;
+  }
+}
+}  // namespace
+
 KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {
-  if (!real || ell_w != 8 || ncols != 64 || max_row_nnz > 8) return nullptr;
+  if (!real || ell_w != 8 || max_row_nnz > 8) return nullptr;
+  if (ncols >= 9 && ncols <= 16) return ffpk1_w<16>(max_row_nnz);
+  if (ncols >= 17 && ncols <= 32) return ffpk1_w<32>(max_row_nnz);
+  if (ncols != 64) return nullptr;
   switch (max_row_nnz) {
     case 5: return k_step_ffpk<5>;
     case 6: return k_step_ffpk<6>;
@@ -491,11 +638,13 @@ KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {
   }
 }
 
+int ffpk_lanes(int ncols) { return ncols <= 16 ? 16 : 32; }
+
 PackedStep select_packed_step(int ncols, bool real, int max_row_nnz, int ell_w) {
   PackedStep ps;
   ps.fn = select_kernel_ffpk(ncols, real, max_row_nnz, ell_w);
   ps.threads = kThreads;
-  ps.rows_per_block = kThreads / 32;
+  ps.rows_per_block = ncols == 64 ? kThreads / 32 : kThreads / ffpk_lanes(ncols);
   ps.smem = 0;
   return ps;
 }

@@ -435,8 +435,11 @@ def test_streaming_kernel_limits():
     rng = np.random.default_rng(4)
     H = (models.cubic_anderson(5, W=1.0, rng=rng) / 7.0).tocsc()
     psi = ko.random_phase_vectors(rng, 125, 40)
-    with pytest.raises(kg.KPMArgumentError):   # 32 columns
-        kg.kpm_1d(H, 16, 32, psi_in=psi[:, :32], precision="ff", kernel="streaming")
+    with pytest.raises(kg.KPMArgumentError):   # 8 columns
+        kg.kpm_1d(H, 16, 8, psi_in=psi[:, :8], precision="ff", kernel="streaming")
+    with pytest.raises(kg.KPMArgumentError):   # bra/ket path with 32 columns
+        kg.kpm_1d(H, 16, 32, psi_in_l=psi[:, :32], psi_in_r=psi[:, 8:], precision="ff",
+                  kernel="streaming")
     with pytest.raises(kg.KPMArgumentError):   # FP64
         kg.kpm_1d(H, 16, 40, psi_in=psi, precision="fp64", kernel="streaming")
     Hc = _peierls_square(8, rng)               # complex operator, 40 columns
@@ -594,3 +597,26 @@ def test_pinned_host_probes_match_pageable(lr):
     else:
         kg.kpm_1d_bang(op, NC, NR, NH, c, own)
     assert np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("NR", [9, 12, 16, 17, 24, 32])
+@pytest.mark.parametrize("W", [5, 7, 8])
+def test_packed_one_column_kernel_matches_oracle(NR, W):
+    """Float-float doubling steps of real operators with 9..32 columns run on
+    packed FP32 pairs, one column per lane (k_step_ffpk1, paired vector
+    layout): against the oracle and the register-gather kernel; the doubling
+    moments' imaginary parts are exactly 0."""
+    rng = np.random.default_rng(100 + NR + 7 * W)
+    if W == 7:
+        H = (models.cubic_anderson(7, W=4.0, rng=rng) / 8.2).tocsc()
+    else:
+        H = _ragged_herm(rng, 300, W, False)
+        while np.diff(H.tocsr().indptr).max() != W:
+            H = _ragged_herm(rng, 300, W, False)
+    NH = H.shape[0]
+    psi = ko.random_phase_vectors(rng, NH, NR)
+    got = kg.kpm_1d(H, 96, NR, psi_in=psi, avg_output=False, precision="ff", kernel="streaming")
+    gat = kg.kpm_1d(H, 96, NR, psi_in=psi, avg_output=False, precision="ff", kernel="gather")
+    assert relerr(got, ko.kpm_1d_doubling(H, 96, psi)) < TOL["ff"]
+    assert relerr(got, gat) < 1e-12
+    assert np.all(got.imag == 0.0)
