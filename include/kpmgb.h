@@ -94,9 +94,9 @@ typedef struct kpmgb_kpm1d_options {
                               call; NH up to ~100k rows); 11: row-streaming
                               padded-row kernels (float-float; real operators
                               with rows of 5..8 nonzeros: 33..64 columns, and
-                              in the doubling path on packed FP32 pairs 9..32
-                              or exactly 64 columns; complex operators with
-                              9..32 columns).  Other values fail with
+                              in the doubling path on packed FP32 pairs
+                              9..64 columns; complex operators with 9..32
+                              columns).  Other values fail with
                               KPMGB_ERR_ARGUMENT.
                               Automatic selection (0) is the cluster kernel
                               (10) for small operators (float-float:

@@ -204,10 +204,10 @@ int run_kpm1d(Operator* op, int64_t NC, int64_t NR, int64_t NH, const void* psi_
       (precision == KPMGB_PREC_FF
            ? NH <= 16384 && NH * NR <= 131072
            : (NH <= 16384 && NH * NR <= 524288) || (NH <= 32768 && NR <= 4));
-  // Float-float doubling calls with 64 columns on real operators of at most
-  // 8 nonzeros per row keep their vectors in the paired element layout and
-  // run every step on packed FP32 pairs (k_step_ffpk; KPMGB_PAIRED=0 keeps
-  // the standard layout and k_step_ffr).
+  // Float-float doubling calls with 9..64 columns on real operators of at
+  // most 8 nonzeros per row keep their vectors in the paired element layout
+  // and run every step on packed FP32 pairs (k_step_ffpk / k_step_ffpk1;
+  // KPMGB_PAIRED=0 keeps the standard layout and k_step_ffr).
   static const bool paired_on = [] {
     const char* e = std::getenv("KPMGB_PAIRED");
     return !(e && std::atoi(e) == 0);

@@ -746,7 +746,7 @@ KernelFn select_kernel_ffr(int ncols, int dot, bool real, int max_row_nnz, int e
 KernelFn select_kernel_ffc(int ncols, int dot, bool real, int ell_w, int max_row_nnz);
 int ffc_lanes(int ncols);
 // Row-streaming float-float kernel on packed FP32 pairs (kpmgb_step_ffpk.cu):
-// real operators, exactly 64 columns, doubling dots, rows of 5..8 nonzeros,
+// real operators, 9..64 columns, doubling dots, rows of 5..8 nonzeros,
 // vectors in the paired element layout (re.hi, im.hi, re.lo, im.lo);
 // nullptr otherwise.  Rows per block tile: 8.
 KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w);

@@ -1,5 +1,6 @@
 // Row-streaming float-float step on packed FP32 pairs (k_step_ffpk): real
-// operators, 64 columns, doubling dots.
+// operators, 33..64 columns (two per lane), doubling dots; k_step_ffpk1 below
+// serves 9..32 columns (one per lane).
 //
 // Blackwell executes `fma/add/sub/mul.rn.f32x2` on a 64-bit register pair:
 // one instruction for two correctly rounded FP32 operations.  For real H the
@@ -105,11 +106,16 @@ __device__ __forceinline__ double join2(f2 S, f2 C) {
 
 }  // namespace
 
-template <int W>
+template <int W, bool FULL>
 __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
   pdl_enter();
   constexpr int GROUPS = kThreads / 32;  // rows per block tile
   constexpr int CPL = 2;
+  // 33..63 columns: the second column slot of the lanes past the last column
+  // is dead (no loads, stores or dots)
+  bool live[CPL];
+#pragma unroll
+  for (int c = 0; c < CPL; ++c) live[c] = FULL || (threadIdx.x & 31) + 32 * c < p.ncols;
   constexpr int kStride = 8;  // padded row stride (ints / float2 values)
   const int g = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const ulonglong2* __restrict__ x = static_cast<const ulonglong2*>(p.x);
@@ -171,11 +177,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
     const int64_t base = r * ld + p.c0;
     // every load of the row, before any arithmetic
     ulonglong2 zv[CPL], xo[CPL], xv[CPL][W];
+    const ulonglong2 zero4 = make_ulonglong2(0ull, 0ull);
 #pragma unroll
     for (int c = 0; c < CPL; ++c) {
       const int64_t e = base + lane + 32 * c;
-      zv[c] = beta_mode != 0 ? __ldcs(z + e) : make_ulonglong2(0ull, 0ull);
-      xo[c] = __ldg(x + e);
+      zv[c] = live[c] && beta_mode != 0 ? __ldcs(z + e) : zero4;
+      xo[c] = live[c] ? __ldg(x + e) : zero4;
     }
     {
       const int4 j0 = reinterpret_cast<const int4*>(jrow)[0];
@@ -184,7 +191,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
 #pragma unroll
       for (int c = 0; c < CPL; ++c)
 #pragma unroll
-        for (int u = 0; u < W; ++u) xv[c][u] = __ldg(x + (int64_t)jj[u] * ld + p.c0 + lane + 32 * c);
+        for (int u = 0; u < W; ++u)
+          xv[c][u] = live[c] ? __ldg(x + (int64_t)jj[u] * ld + p.c0 + lane + 32 * c) : zero4;
     }
     float hh[8], hl[8];
 #pragma unroll
@@ -242,10 +250,12 @@ __global__ void __launch_bounds__(kThreads, 2) k_step_ffpk(KParams p) {
           two_sum2(s, add2(e, sub2(c2, zv[c].y)), yh, yl);
         }
       }
-      __stcs(y + base + lane + 32 * c, make_ulonglong2(yh, yl));
-      const f2 nxh = sub2(zero2, xo[c].x);  // exact negation
-      dacc2(nS[c], nC[c], xo[c].x, nxh, xo[c].y, xo[c].x, xo[c].y);
-      dacc2(xS[c], xC[c], xo[c].x, nxh, xo[c].y, yh, yl);
+      if (live[c]) {
+        __stcs(y + base + lane + 32 * c, make_ulonglong2(yh, yl));
+        const f2 nxh = sub2(zero2, xo[c].x);  // exact negation
+        dacc2(nS[c], nC[c], xo[c].x, nxh, xo[c].y, xo[c].x, xo[c].y);
+        dacc2(xS[c], xC[c], xo[c].x, nxh, xo[c].y, yh, yl);
+      }
     }
     if (++rows_since_flush == kFlushRows) {
       rows_since_flush = 0;
@@ -628,12 +638,13 @@ KernelFn select_kernel_ffpk(int ncols, bool real, int max_row_nnz, int ell_w) {
   if (!real || ell_w != 8 || max_row_nnz > 8) return nullptr;
   if (ncols >= 9 && ncols <= 16) return ffpk1_w<16>(max_row_nnz);
   if (ncols >= 17 && ncols <= 32) return ffpk1_w<32>(max_row_nnz);
-  if (ncols != 64) return nullptr;
+  if (ncols < 33 || ncols > 64) return nullptr;
+  const bool full = ncols == 64;
   switch (max_row_nnz) {
-    case 5: return k_step_ffpk<5>;
-    case 6: return k_step_ffpk<6>;
-    case 7: return k_step_ffpk<7>;
-    case 8: return k_step_ffpk<8>;
+    case 5: return full ? k_step_ffpk<5, true> : k_step_ffpk<5, false>;
+    case 6: return full ? k_step_ffpk<6, true> : k_step_ffpk<6, false>;
+    case 7: return full ? k_step_ffpk<7, true> : k_step_ffpk<7, false>;
+    case 8: return full ? k_step_ffpk<8, true> : k_step_ffpk<8, false>;
     default: return nullptr;
   }
 }
@@ -644,7 +655,7 @@ PackedStep select_packed_step(int ncols, bool real, int max_row_nnz, int ell_w) 
   PackedStep ps;
   ps.fn = select_kernel_ffpk(ncols, real, max_row_nnz, ell_w);
   ps.threads = kThreads;
-  ps.rows_per_block = ncols == 64 ? kThreads / 32 : kThreads / ffpk_lanes(ncols);
+  ps.rows_per_block = ncols > 32 ? kThreads / 32 : kThreads / ffpk_lanes(ncols);
   ps.smem = 0;
   return ps;
 }

@@ -112,7 +112,7 @@ def kpm_1d(H, NC: int, NR: int, NH: int | None = None, *, psi_in=None, psi_in_l=
     ``kernel`` picks the recurrence kernel (``include/kpmgb.h``,
     ``kernel_variant``): ``"auto"`` (one thread-block-cluster launch per call
     for small operators, else per-step launches of the row-streaming kernels
-    -- on packed FP32 pairs for real operators with 9..32 or 64 columns,
+    -- on packed FP32 pairs for real operators with 9..64 columns,
     float-float doubling -- where they apply, else of the register-gather
     kernel), ``"gather"``,
     ``"padded"``, ``"streaming"``, ``"cluster"``, ``"single"``, ``"tune"``.

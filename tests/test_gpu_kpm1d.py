@@ -599,13 +599,14 @@ def test_pinned_host_probes_match_pageable(lr):
     assert np.array_equal(a, c)
 
 
-@pytest.mark.parametrize("NR", [9, 12, 16, 17, 24, 32])
+@pytest.mark.parametrize("NR", [9, 12, 16, 17, 24, 32, 33, 40, 48, 63, 64])
 @pytest.mark.parametrize("W", [5, 7, 8])
-def test_packed_one_column_kernel_matches_oracle(NR, W):
-    """Float-float doubling steps of real operators with 9..32 columns run on
-    packed FP32 pairs, one column per lane (k_step_ffpk1, paired vector
-    layout): against the oracle and the register-gather kernel; the doubling
-    moments' imaginary parts are exactly 0."""
+def test_packed_kernels_match_oracle(NR, W):
+    """Float-float doubling steps of real operators with 9..64 columns run on
+    packed FP32 pairs in the paired vector layout: one column per lane for
+    9..32 columns (k_step_ffpk1), two per lane for 33..64 (k_step_ffpk, idle
+    lanes masked below 64).  Against the oracle and the register-gather
+    kernel; the doubling moments' imaginary parts are exactly 0."""
     rng = np.random.default_rng(100 + NR + 7 * W)
     if W == 7:
         H = (models.cubic_anderson(7, W=4.0, rng=rng) / 8.2).tocsc()
