@@ -91,12 +91,16 @@ void tune_cache_put(const std::string& key, const std::string& value) {
   m[key] = value;
   make_dirs(path);
   const std::string tmp = path + ".tmp" + std::to_string((long)getpid());
+  bool ok = false;
   {
     std::ofstream f(tmp, std::ios::trunc);
     if (!f) return;
     for (const auto& kv : m) f << kv.first << ' ' << kv.second << '\n';
+    f.flush();
+    ok = f.good();
   }
-  std::rename(tmp.c_str(), path.c_str());
+  // a short write (full disk) must not replace a good cache
+  if (!ok || std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
 }
 
 }  // namespace kpmgb

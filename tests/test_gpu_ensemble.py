@@ -203,3 +203,41 @@ def test_ensemble_device_entry_matches_host_entry(built_lib, prec):
         assert np.array_equal(got[i].T, m)
     with pytest.raises(kg.KPMArgumentError):
         kg.kpm_1d_ensemble_device(ens, NC, psi_t, mu_t[:, :64], precision=prec)
+
+
+def _ragged_member(rng, n, max_row, complex_h):
+    """Hermitian member with row lengths spread over 0..max_row, scaled into
+    the Chebyshev domain."""
+    rows, cols = [], []
+    for i in range(n):
+        for j in rng.choice(n, size=int(rng.integers(0, max_row // 2 + 1)), replace=False):
+            rows.append(i)
+            cols.append(int(j))
+    vals = rng.standard_normal(len(rows)) + (1j * rng.standard_normal(len(rows)) if complex_h else 0)
+    A = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    A = (A + A.conj().T).tocsr()
+    A.sum_duplicates()
+    keep = (np.diff(A.indptr) <= max_row).astype(float)
+    A = sp.csc_matrix(sp.diags(keep) @ A @ sp.diags(keep))
+    A.eliminate_zeros()
+    return A / (1.05 * max(np.abs(np.linalg.eigvalsh(A.toarray())).max(), 1e-3))
+
+
+@pytest.mark.parametrize("NR", [1, 3, 8, 13, 32])
+@pytest.mark.parametrize("complex_h", [False, True])
+def test_ensemble_padded_rows_widths_match_oracle(built_lib, NR, complex_h):
+    """Float-float padded-row steps of real and complex members for 1..32
+    probe columns and ragged rows of up to 8 nonzeros (empty rows included):
+    every member against the oracle, and the padded and CSR-row kernels
+    against each other (their float-float sums are anchored per padded row
+    and per 8-nonzero chunk of a CSR row: agreement to ~1e-12)."""
+    rng = np.random.default_rng(300 + NR + 7 * complex_h)
+    Hs = [_ragged_member(rng, n, 8, complex_h) for n in (150, 700, 33, 520)]
+    psis = [ko.random_phase_vectors(rng, H.shape[0], NR) for H in Hs]
+    got = kg.kpm_1d_ensemble(Hs, 96, psis, precision="ff", avg_output=False, kernel="padded")
+    auto = kg.kpm_1d_ensemble(Hs, 96, psis, precision="ff", avg_output=False)
+    csr = kg.kpm_1d_ensemble(Hs, 96, psis, precision="ff", avg_output=False, kernel="gather")
+    for H, psi, m, a, c in zip(Hs, psis, got, auto, csr):
+        assert relerr(m, ko.kpm_1d_doubling(H, 96, psi)) < TOL["ff"]
+        assert np.array_equal(m, a)
+        assert relerr(m, c) < 1e-11
