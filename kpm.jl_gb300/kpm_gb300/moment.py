@@ -548,10 +548,13 @@ def kpm_1d_ensemble(Hs, NC: int, psis, *, precision: str = "fp64", avg_output: b
     rc = lib.kpmgb_kpm1d_ensemble(op.handle, len(sizes), seg.ctypes.data, NC, NR, psi.ctypes.data,
                                   out.ctypes.data, C.byref(opts))
     _native.check(rc)
-    res = [np.ascontiguousarray(out[i].T) for i in range(len(sizes))]
     if avg_output:
-        return [m.sum(axis=0).real / NR for m in res]
-    return res
+        # column by column in order: the same sums as kpm_1d's averaging
+        acc = out[:, :, 0].copy()
+        for r in range(1, NR):
+            acc += out[:, :, r]
+        return list(acc.real / NR)
+    return [np.ascontiguousarray(out[i].T) for i in range(len(sizes))]
 
 
 def kpm_1d_ensemble_device(ens: "EnsembleOperator", NC: int, psi_t, mu_t, *,
