@@ -120,9 +120,14 @@ int grid_m(int64_t M);
 
 int launch_rowmajor_to_colmajor(const double2* in, double2* out, int64_t NH, int NR, int K,
                                 cudaStream_t s) {
-  const dim3 tg((unsigned)((NH + 31) / 32), (unsigned)((NR + 31) / 32), (unsigned)K);
-  k_rowmajor_to_colmajor<<<tg, 256, 0, s>>>(in, out, NH, NR);
-  KPMGB_LAUNCHED();
+  // at most 65535 blocks per launch (the grid's z limit)
+  for (int k0 = 0; k0 < K; k0 += 65535) {
+    const int nk = std::min(K - k0, 65535);
+    const size_t ofs = (size_t)k0 * NH * NR;
+    const dim3 tg((unsigned)((NH + 31) / 32), (unsigned)((NR + 31) / 32), (unsigned)nk);
+    k_rowmajor_to_colmajor<<<tg, 256, 0, s>>>(in + ofs, out + ofs, NH, NR);
+    KPMGB_LAUNCHED();
+  }
   return KPMGB_OK;
 }
 

@@ -733,8 +733,13 @@ int launch_vec_absmax(const void* vecs, int64_t K, int nvec, unsigned* out, cuda
   if (nvec < 1) return KPMGB_OK;
   KPMGB_CUDA(cudaMemsetAsync(out, 0, (size_t)nvec * sizeof(unsigned), s));
   const int chunks = (int)std::max<int64_t>(1, std::min<int64_t>((K + 4095) / 4096, 512));
-  k_vec_absmax<<<dim3((unsigned)chunks, (unsigned)nvec), 256, 0, s>>>(vecs, K, nvec, out);
-  KPMGB_LAUNCHED();
+  // at most 65535 vectors per launch (the grid's y limit)
+  for (int v0 = 0; v0 < nvec; v0 += 65535) {
+    const int nv = std::min(nvec - v0, 65535);
+    k_vec_absmax<<<dim3((unsigned)chunks, (unsigned)nv), 256, 0, s>>>(
+        static_cast<const float4*>(vecs) + (int64_t)v0 * K, K, nv, out + v0);
+    KPMGB_LAUNCHED();
+  }
   return KPMGB_OK;
 }
 
