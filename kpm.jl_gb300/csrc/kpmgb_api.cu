@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "kpmgb_csr_host.h"
 #include "kpmgb_ffmath.cuh"
 #include "kpmgb_internal.h"
 
@@ -79,14 +80,7 @@ Operator::~Operator() {
   DevBuf* bufs[] = {&ws.slots, &ws.bra,  &ws.partials, &ws.sync,  &ws.scales, &ws.mu,
                     &ws.psi_in, &ws.left, &ws.right,   &ws.ring,  &ws.gemm,   &ws.split};
   for (DevBuf* b : bufs) b->release();
-  cudaFree(csr.rowptr);
-  cudaFree(csr.col);
-  cudaFree(csr.perm);
-  cudaFree(csr.val);
-  cudaFree(csr.val_real);
-  cudaFree(csr.val_ff);
-  cudaFree(csr.ell_col);
-  cudaFree(csr.ell_val);
+  cudaFree(csr.block);  // every array of the operator
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -649,40 +643,36 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
   if (!colptr || (nnz > 0 && (!rowval || !nzval))) return fail(KPMGB_ERR_ARGUMENT, "null array");
   if (colptr[0] != index_base || colptr[n] - index_base != nnz)
     return fail(KPMGB_ERR_ARGUMENT, "colptr is inconsistent with nnz");
-  // CSC -> CSR (a true transpose; rows come out sorted by column)
-  std::vector<int> rowptr(n + 1, 0);
-  for (int64_t j = 0; j < n; ++j) {
-    const int64_t a = colptr[j] - index_base, b = colptr[j + 1] - index_base;
-    if (b < a || a < 0 || b > nnz) return fail(KPMGB_ERR_ARGUMENT, "colptr is not monotone");
-    for (int64_t k = a; k < b; ++k) {
-      const int64_t i = rowval[k] - index_base;
-      if (i < 0 || i >= n) return fail(KPMGB_ERR_ARGUMENT, "row index out of range");
-      rowptr[i + 1]++;
+  // CSC -> CSR (a true transpose; rows come out sorted by column).  Up to
+  // kCachedStaging bytes the conversion goes into one page-locked buffer kept
+  // across calls (no page faults, and the upload runs at the copy kernel's
+  // rate); larger operators use a buffer of their own.
+  constexpr size_t kCachedStaging = size_t(64) << 20;
+  static std::mutex staging_mtx;
+  static HostCSR staging_csr;
+  static unsigned char* staging = nullptr;
+  static size_t staging_cap = 0;
+  const size_t need = csr_host_bytes(n, nnz);
+  std::unique_lock<std::mutex> staging_lk(staging_mtx, std::defer_lock);
+  HostCSR local;
+  HostCSR* hcp = &local;
+  unsigned char* dst = nullptr;
+  if (need <= kCachedStaging) {
+    staging_lk.lock();
+    if (staging_cap < need) {
+      if (staging) cudaFreeHost(staging);
+      staging = nullptr;
+      staging_cap = 0;
+      const size_t cap = std::max(need, size_t(4) << 20);
+      if (cudaHostAlloc(&staging, cap, cudaHostAllocPortable) == cudaSuccess) staging_cap = cap;
+      else cudaGetLastError();  // fall back to a pageable buffer
     }
+    hcp = &staging_csr;
+    dst = staging_cap >= need ? staging : nullptr;
   }
-  int max_nnz = 0;
-  for (int64_t i = 0; i < n; ++i) {
-    max_nnz = std::max(max_nnz, rowptr[i + 1]);
-    rowptr[i + 1] += rowptr[i];
-  }
-  std::vector<int> col(nnz);
-  std::vector<int> perm(nnz);
-  std::vector<double> val(2 * nnz);
-  std::vector<int> fillp(rowptr.begin(), rowptr.end() - 1);
-  int is_real = 1;
-  std::vector<double> rowsum(n, 0.0);
-  for (int64_t j = 0; j < n; ++j) {
-    for (int64_t k = colptr[j] - index_base; k < colptr[j + 1] - index_base; ++k) {
-      const int64_t i = rowval[k] - index_base;
-      const int dst = fillp[i]++;
-      col[dst] = (int)j;
-      perm[dst] = (int)k;
-      val[2 * dst] = nzval[2 * k];
-      val[2 * dst + 1] = nzval[2 * k + 1];
-      if (nzval[2 * k + 1] != 0.0) is_real = 0;
-      rowsum[i] += std::fabs(nzval[2 * k]) + std::fabs(nzval[2 * k + 1]);
-    }
-  }
+  HostCSR& hc = *hcp;
+  const std::string err = csc_to_csr(n, nnz, colptr, rowval, nzval, index_base, 0, hc, dst);
+  if (!err.empty()) return fail(KPMGB_ERR_ARGUMENT, "%s", err.c_str());
   Operator* op = new Operator();
   cudaGetDevice(&op->device);
   auto cleanup = [&](int rc) {
@@ -692,10 +682,19 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
   DeviceCSR& c = op->csr;
   c.n = n;
   c.nnz = nnz;
-  c.is_real = is_real;
-  c.max_row_nnz = max_nnz;
-  for (int64_t i = 0; i < n; ++i) c.rmax = std::max(c.rmax, rowsum[i]);
+  c.is_real = hc.is_real;
+  c.max_row_nnz = hc.max_row_nnz;
+  c.rmax = hc.rmax;
+  const int is_real = hc.is_real;
   const size_t nz = (size_t)std::max<int64_t>(nnz, 1);
+  // one device block: the converted arrays (laid out as the host buffer, so
+  // one copy uploads them), then the arrays built on the device
+  const int W = nnz > 0 ? step::ell_width(hc.max_row_nnz) : 0;
+  const size_t off_real = csr_align256(hc.off_val + nz * sizeof(double2));
+  const size_t off_ff = off_real + (is_real ? csr_align256(nz * sizeof(double)) : 0);
+  const size_t off_ecol = off_ff + csr_align256(nz * (is_real ? sizeof(float2) : sizeof(float4)));
+  const size_t off_eval = off_ecol + csr_align256((size_t)n * W * sizeof(int));
+  const size_t total = off_eval + (size_t)n * W * (is_real ? sizeof(float2) : sizeof(float4));
 #define CREATE_CUDA(call)                                                                   \
   do {                                                                                      \
     cudaError_t e_ = (call);                                                                \
@@ -704,34 +703,33 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
                           "%s failed: %s", #call, cudaGetErrorString(e_)));                 \
   } while (0)
   CREATE_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
-  CREATE_CUDA(cudaMalloc(&c.rowptr, (n + 1) * sizeof(int)));
-  CREATE_CUDA(cudaMalloc(&c.col, nz * sizeof(int)));
-  CREATE_CUDA(cudaMalloc(&c.perm, nz * sizeof(int)));
-  CREATE_CUDA(cudaMalloc(&c.val, nz * sizeof(double2)));
-  if (is_real) CREATE_CUDA(cudaMalloc(&c.val_real, nz * sizeof(double)));
-  CREATE_CUDA(cudaMalloc(&c.val_ff, nz * (is_real ? sizeof(float2) : sizeof(float4))));
-  CREATE_CUDA(cudaMemcpy(c.rowptr, rowptr.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CREATE_CUDA(cudaMalloc(&c.block, total));
+  char* base = static_cast<char*>(c.block);
+  c.rowptr = reinterpret_cast<int*>(base);
+  c.col = reinterpret_cast<int*>(base + hc.off_col);
+  c.perm = reinterpret_cast<int*>(base + hc.off_perm);
+  c.val = reinterpret_cast<double2*>(base + hc.off_val);
+  c.val_real = is_real ? reinterpret_cast<double*>(base + off_real) : nullptr;
+  c.val_ff = base + off_ff;
+  if (copy_to_device(base, hc.buf, hc.bytes, op->stream) != KPMGB_OK) return cleanup(KPMGB_ERR_CUDA);
   if (nnz > 0) {
-    CREATE_CUDA(cudaMemcpy(c.col, col.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
-    CREATE_CUDA(cudaMemcpy(c.perm, perm.data(), nnz * sizeof(int), cudaMemcpyHostToDevice));
-    CREATE_CUDA(cudaMemcpy(c.val, val.data(), nnz * sizeof(double2), cudaMemcpyHostToDevice));
     const int blocks = (int)std::min<int64_t>((nnz + 255) / 256, 4096);
     k_split_values<<<blocks, 256, 0, op->stream>>>(c.val, nnz, is_real, c.val_ff, c.val_real);
     g_launches.fetch_add(1);
     CREATE_CUDA(cudaGetLastError());
     // fixed-width padded rows for the padded-row step kernel (rows <= 16)
-    const int W = step::ell_width(max_nnz);
     if (W > 0) {
-      CREATE_CUDA(cudaMalloc(&c.ell_col, (size_t)n * W * sizeof(int)));
-      CREATE_CUDA(cudaMalloc(&c.ell_val, (size_t)n * W * (is_real ? sizeof(float2) : sizeof(float4))));
+      c.ell_col = reinterpret_cast<int*>(base + off_ecol);
+      c.ell_val = base + off_eval;
       if (step::launch_build_ell(c.rowptr, c.col, c.val_ff, is_real != 0, n, W, c.ell_col,
                                  c.ell_val, op->stream) != 0)
         CREATE_CUDA(cudaGetLastError());
       g_launches.fetch_add(1);
       c.ell_w = W;
     }
-    CREATE_CUDA(cudaStreamSynchronize(op->stream));
   }
+  // the host buffer is released on return: the copy must have completed
+  CREATE_CUDA(cudaStreamSynchronize(op->stream));
 #undef CREATE_CUDA
   *out = reinterpret_cast<kpmgb_operator>(op);
   return KPMGB_OK;

@@ -99,6 +99,7 @@ struct DeviceCSR {
   void* ell_val = nullptr;
   int ell_w = 0;
   int* perm = nullptr;  // CSR position -> position in the caller's CSC arrays
+  void* block = nullptr;  // the one device allocation that holds the arrays above
 };
 
 // Device status words written by kernels (read back by the host at sync).
