@@ -563,7 +563,9 @@ def workload_published(args):
     256x256 (NC=1024, NR=8, K=2).  Timed end to end through the host API from
     host arrays: `per_call_operator` builds the device operator inside every
     call (as the reference converts and uploads H per call), `resident` reuses
-    it.  Default (FP64) precision, as the reference."""
+    it.  Default (FP64) precision, as the reference; `resident_ff` and
+    `resident_ff_split` add the chosen forms (float-float recurrences, split
+    tensor-core contraction)."""
     import kpm_gb300 as kg
     rng = np.random.default_rng(42)
     steps = max(args.steps, 3)
@@ -592,11 +594,18 @@ def workload_published(args):
     psi = kg.random_phase_vectors(rng, NH, 4)
     ops = [kg.GB300Operator(M) for M in (Hn, Jx, Jy)]
     for tag, kw in (("default", {}), ("arr64", {"arr_size": 64})):
+        split = dict(kw, precision="ff", contraction="split")
+        ref = kg.kpm_2d(*ops, 64, 4, NH, psi_in=psi, **kw)
+        got = kg.kpm_2d(*ops, 64, 4, NH, psi_in=psi, **split)
         out[f"kpm_2d_NH16384_NC64_NR4_{tag}"] = {
             "per_call_operator_s": _time_host(lambda: kg.kpm_2d(Hn, Jx, Jy, 64, 4, NH, psi_in=psi,
                                                                 **kw), 1, steps) / 1e3,
             "resident_s": _time_host(lambda: kg.kpm_2d(*ops, 64, 4, NH, psi_in=psi, **kw), 1,
-                                     steps) / 1e3}
+                                     steps) / 1e3,
+            # the chosen form: float-float recurrences, split tensor-core contraction
+            "resident_ff_split_s": _time_host(lambda: kg.kpm_2d(*ops, 64, 4, NH, psi_in=psi,
+                                                                **split), 1, steps) / 1e3,
+            "ff_split_vs_fp64_rel_err": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}
     H, _, _ = _square_lattice(256)
     a, Hn = kg.normalizeH(H)
     V = kg.random_phase_vectors(rng, 65536, 8)

@@ -47,21 +47,11 @@ void clear_error() { t_last_error.clear(); }
 int DevBuf::ensure(size_t need) {
   if (need <= bytes && ptr) return KPMGB_OK;
   release();
-  if (need == 0) return KPMGB_OK;
-  cudaError_t e = cudaMalloc(&ptr, need);
-  if (e != cudaSuccess) {
-    ptr = nullptr;
-    bytes = 0;
-    cudaGetLastError();
-    return fail(KPMGB_ERR_ALLOC, "cudaMalloc of %zu bytes failed: %s", need,
-                cudaGetErrorString(e));
-  }
-  bytes = need;
-  return KPMGB_OK;
+  return dev_alloc(need, &ptr, &bytes);
 }
 
-void DevBuf::release() {
-  if (ptr) cudaFree(ptr);
+void DevBuf::release(bool device_idle) {
+  dev_release(ptr, bytes, device_idle);
   ptr = nullptr;
   bytes = 0;
 }
@@ -75,12 +65,15 @@ void GraphCache::release() {
 
 Operator::~Operator() {
   cudaSetDevice(device);
-  if (stream) cudaStreamSynchronize(stream);
+  // every kernel that may use the operator's memory has finished (its own
+  // stream and callers' streams of the device entry points) before the
+  // blocks go back to the cache
+  cudaDeviceSynchronize();
   graph.release();
   DevBuf* bufs[] = {&ws.slots, &ws.bra,  &ws.partials, &ws.sync,  &ws.scales, &ws.mu,
                     &ws.psi_in, &ws.left, &ws.right,   &ws.ring,  &ws.gemm,   &ws.split};
-  for (DevBuf* b : bufs) b->release();
-  cudaFree(csr.block);  // every array of the operator
+  for (DevBuf* b : bufs) b->release(true);
+  dev_release(csr.block, csr.block_bytes, true);  // every array of the operator
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -703,7 +696,7 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
                           "%s failed: %s", #call, cudaGetErrorString(e_)));                 \
   } while (0)
   CREATE_CUDA(cudaStreamCreateWithFlags(&op->stream, cudaStreamNonBlocking));
-  CREATE_CUDA(cudaMalloc(&c.block, total));
+  if (dev_alloc(total, &c.block, &c.block_bytes) != KPMGB_OK) return cleanup(KPMGB_ERR_ALLOC);
   char* base = static_cast<char*>(c.block);
   c.rowptr = reinterpret_cast<int*>(base);
   c.col = reinterpret_cast<int*>(base + hc.off_col);

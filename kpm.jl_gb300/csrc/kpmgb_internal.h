@@ -66,12 +66,19 @@ bool tune_cache_get(const std::string& key, std::string* value);
 void tune_cache_put(const std::string& key, const std::string& value);
 
 // ------------------------------------------------------------- resources
+// Device blocks from the library's cache of released blocks (kpmgb_alloc.cu):
+// dev_alloc returns a block of at least `need` bytes and its capacity;
+// dev_release caches it (after a device synchronize unless the caller has
+// just synchronized: device_idle) or frees it when the cache is full.
+int dev_alloc(size_t need, void** out, size_t* capacity);
+void dev_release(void* p, size_t capacity, bool device_idle);
+
 // Grow-only device buffer owned by an operator handle.
 struct DevBuf {
   void* ptr = nullptr;
-  size_t bytes = 0;
+  size_t bytes = 0;  // capacity
   int ensure(size_t need);
-  void release();
+  void release(bool device_idle = false);
   template <typename T>
   T* as() const { return static_cast<T*>(ptr); }
 };
@@ -100,6 +107,7 @@ struct DeviceCSR {
   int ell_w = 0;
   int* perm = nullptr;  // CSR position -> position in the caller's CSC arrays
   void* block = nullptr;  // the one device allocation that holds the arrays above
+  size_t block_bytes = 0;  // its capacity
 };
 
 // Device status words written by kernels (read back by the host at sync).

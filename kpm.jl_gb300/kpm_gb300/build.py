@@ -37,6 +37,7 @@ SOURCES = [
     "kpmgb_action.cu",
     "kpmgb_timing.cu",
     "kpmgb_tune.cu",
+    "kpmgb_alloc.cu",
     "kpmgb_hostio.cu",
     "kpmgb_step_ffpk.cu",
 ]
