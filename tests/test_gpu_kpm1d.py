@@ -621,3 +621,24 @@ def test_packed_kernels_match_oracle(NR, W):
     assert relerr(got, ko.kpm_1d_doubling(H, 96, psi)) < TOL["ff"]
     assert relerr(got, gat) < 1e-12
     assert np.all(got.imag == 0.0)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "ff"])
+def test_operators_rebuilt_on_cached_blocks(prec):
+    """Operators and workspaces built and destroyed in a loop reuse released
+    device blocks (the library's block cache): every rebuilt operator gives
+    its first build's moments bitwise, and the oracle's."""
+    rng = np.random.default_rng(91)
+    Hs = [(models.square_anderson(L, W=2.0, rng=rng) / 5.1).tocsc() for L in (40, 23, 40, 57)]
+    psis = [ko.random_phase_vectors(rng, H.shape[0], 12) for H in Hs]
+    first = {}
+    for rep in range(3):
+        for i, (H, psi) in enumerate(zip(Hs, psis)):
+            op = kg.GB300Operator(H)
+            mu = kg.kpm_1d(op, 128, 12, psi_in=psi, avg_output=False, precision=prec)
+            del op
+            if rep == 0:
+                first[i] = mu
+                assert relerr(mu, ko.kpm_1d_doubling(H, 128, psi)) < TOL[prec]
+            else:
+                assert np.array_equal(mu, first[i])
