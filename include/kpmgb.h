@@ -128,9 +128,10 @@ const char* kpmgb_last_error(void);
 /* Upload a square sparse operator given in CSC form and keep it resident on
  * the current CUDA device until kpmgb_operator_destroy.  The library builds
  * the row-major CSR (a true transpose, the operator need not be Hermitian;
- * up to 8 host threads for large operators).  Replaces the per-call
- * `maybe_to_device(H)` conversion of src/moment.jl:432,1002-1004 /
- * ext/KPMCUDAExt.jl:26-27.  Blocking call. */
+ * up to 8 host threads for large operators; conversions of up to 64 MiB go
+ * through one page-locked host buffer that the library keeps between calls).
+ * Replaces the per-call `maybe_to_device(H)` conversion of
+ * src/moment.jl:432,1002-1004 / ext/KPMCUDAExt.jl:26-27.  Blocking call. */
 int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr,
                           const int64_t* rowval, const double* nzval,
                           int32_t index_base, kpmgb_operator* out);

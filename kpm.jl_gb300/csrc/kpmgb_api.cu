@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -664,7 +665,13 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
     dst = staging_cap >= need ? staging : nullptr;
   }
   HostCSR& hc = *hcp;
-  const std::string err = csc_to_csr(n, nnz, colptr, rowval, nzval, index_base, 0, hc, dst);
+  std::string err;
+  try {
+    err = csc_to_csr(n, nnz, colptr, rowval, nzval, index_base, 0, hc, dst);
+  } catch (const std::bad_alloc&) {
+    return fail(KPMGB_ERR_ALLOC, "host memory for the CSR conversion of %lld entries",
+                (long long)nnz);
+  }
   if (!err.empty()) return fail(KPMGB_ERR_ARGUMENT, "%s", err.c_str());
   Operator* op = new Operator();
   cudaGetDevice(&op->device);

@@ -71,6 +71,7 @@ inline size_t csr_host_bytes(int64_t n, int64_t nnz) {
 }
 
 // Converts; returns "" on success, else the argument error's message.
+// Throws std::bad_alloc when the host buffers cannot be allocated.
 // threads <= 0 picks csr_threads(nnz).  dst: a caller buffer of at least
 // csr_host_bytes(n, nnz) bytes, or null to use (and keep) out's own.
 inline std::string csc_to_csr(int64_t n, int64_t nnz, const int64_t* colptr,
@@ -141,7 +142,12 @@ inline std::string csc_to_csr(int64_t n, int64_t nnz, const int64_t* colptr,
     }
     std::vector<std::thread> pool;
     pool.reserve((size_t)T - 1);
-    for (int t = 1; t < T; ++t) pool.emplace_back(fn, t);
+    int t = 1;
+    try {
+      for (; t < T; ++t) pool.emplace_back(fn, t);
+    } catch (...) {  // no more threads: run the remaining row ranges here
+      for (; t < T; ++t) fn(t);
+    }
     fn(0);
     for (auto& th : pool) th.join();
   };
