@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <new>
 #include <string>
 #include <vector>
@@ -44,6 +45,18 @@ int fail(int code, const char* fmt, ...) {
 }
 
 void clear_error() { t_last_error.clear(); }
+
+int exception_status() noexcept {
+  try {
+    throw;
+  } catch (const std::bad_alloc&) {
+    return fail(KPMGB_ERR_ALLOC, "host memory allocation failed");
+  } catch (const std::exception& e) {
+    return fail(KPMGB_ERR_CUDA, "internal error: %s", e.what());
+  } catch (...) {
+    return fail(KPMGB_ERR_CUDA, "internal error");
+  }
+}
 
 int DevBuf::ensure(size_t need) {
   if (need <= bytes && ptr) return KPMGB_OK;
@@ -612,22 +625,22 @@ const char* kpmgb_last_error(void) { return t_last_error.c_str(); }
 
 int64_t kpmgb_kernel_launch_count(void) { return g_launches.load(); }
 
-int kpmgb_host_alloc(int64_t bytes, void** out) {
+int kpmgb_host_alloc(int64_t bytes, void** out) try {
   clear_error();
   if (!out || bytes < 1) return fail(KPMGB_ERR_ARGUMENT, "invalid host allocation");
   *out = nullptr;
   KPMGB_CUDA(cudaMallocHost(out, (size_t)bytes));
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
-int kpmgb_host_free(void* ptr) {
+int kpmgb_host_free(void* ptr) try {
   clear_error();
   if (ptr) KPMGB_CUDA(cudaFreeHost(ptr));
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
 int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const int64_t* rowval,
-                          const double* nzval, int32_t index_base, kpmgb_operator* out) {
+                          const double* nzval, int32_t index_base, kpmgb_operator* out) try {
   clear_error();
   if (!out) return fail(KPMGB_ERR_ARGUMENT, "out is null");
   *out = nullptr;
@@ -733,18 +746,18 @@ int kpmgb_operator_create(int64_t n, int64_t nnz, const int64_t* colptr, const i
 #undef CREATE_CUDA
   *out = reinterpret_cast<kpmgb_operator>(op);
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
-int kpmgb_operator_destroy(kpmgb_operator h) {
+int kpmgb_operator_destroy(kpmgb_operator h) try {
   clear_error();
   if (!h) return KPMGB_OK;
   Operator* op = as_op(h);
   { std::lock_guard<std::mutex> lk(op->mtx); }
   delete op;
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
-int kpmgb_operator_info(kpmgb_operator h, int64_t* n, int64_t* nnz, int32_t* is_real) {
+int kpmgb_operator_info(kpmgb_operator h, int64_t* n, int64_t* nnz, int32_t* is_real) try {
   clear_error();
   if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   Operator* op = as_op(h);
@@ -752,9 +765,9 @@ int kpmgb_operator_info(kpmgb_operator h, int64_t* n, int64_t* nnz, int32_t* is_
   if (nnz) *nnz = op->csr.nnz;
   if (is_real) *is_real = op->csr.is_real;
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
-int kpmgb_operator_sync(kpmgb_operator h, void* stream) {
+int kpmgb_operator_sync(kpmgb_operator h, void* stream) try {
   clear_error();
   if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   Operator* op = as_op(h);
@@ -764,21 +777,21 @@ int kpmgb_operator_sync(kpmgb_operator h, void* stream) {
     return KPMGB_OK;
   }
   return check_status(op, pick_stream(op, stream));
-}
+} KPMGB_ENTRY_CATCH
 
 int kpmgb_kpm1d_device(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const void* psi,
-                       void* mu_all, const kpmgb_kpm1d_options* opts, void* stream) {
+                       void* mu_all, const kpmgb_kpm1d_options* opts, void* stream) try {
   clear_error();
   if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   Operator* op = as_op(h);
   Guard g(op);
   return run_kpm1d(op, NC, NR, NH, nullptr, psi, static_cast<double2*>(mu_all), opts,
                    pick_stream(op, stream), false);
-}
+} KPMGB_ENTRY_CATCH
 
 int kpmgb_kpm1d_lr_device(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH,
                           const void* psi_l, const void* psi_r, void* mu_all,
-                          const kpmgb_kpm1d_options* opts, void* stream) {
+                          const kpmgb_kpm1d_options* opts, void* stream) try {
   clear_error();
   if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   if (!psi_l || !psi_r) return fail(KPMGB_ERR_ARGUMENT, "must set both `psi_in_l` and `psi_in_r`");
@@ -786,7 +799,7 @@ int kpmgb_kpm1d_lr_device(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH,
   Guard g(op);
   return run_kpm1d(op, NC, NR, NH, psi_l, psi_r, static_cast<double2*>(mu_all), opts,
                    pick_stream(op, stream), true);
-}
+} KPMGB_ENTRY_CATCH
 
 static int host_kpm1d(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const double* psi_l,
                       const double* psi_r, double* mu_all, const kpmgb_kpm1d_options* opts,
@@ -811,33 +824,33 @@ static int host_kpm1d(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, cons
 }
 
 int kpmgb_kpm1d(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const double* psi,
-                double* mu_all, const kpmgb_kpm1d_options* opts) {
+                double* mu_all, const kpmgb_kpm1d_options* opts) try {
   return host_kpm1d(h, NC, NR, NH, nullptr, psi, mu_all, opts, false);
-}
+} KPMGB_ENTRY_CATCH
 
 int kpmgb_kpm1d_lr(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH, const double* psi_l,
-                   const double* psi_r, double* mu_all, const kpmgb_kpm1d_options* opts) {
+                   const double* psi_r, double* mu_all, const kpmgb_kpm1d_options* opts) try {
   if (!psi_l || !psi_r) {
     clear_error();
     return fail(KPMGB_ERR_ARGUMENT, "must set both `psi_in_l` and `psi_in_r` or neither.");
   }
   return host_kpm1d(h, NC, NR, NH, psi_l, psi_r, mu_all, opts, true);
-}
+} KPMGB_ENTRY_CATCH
 
 int kpmgb_kpm2d_device(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t NC,
                        int64_t NR, int64_t NH, const void* psi_l, const void* psi_r, void* mu,
-                       const kpmgb_kpm2d_options* opts, void* stream) {
+                       const kpmgb_kpm2d_options* opts, void* stream) try {
   clear_error();
   if (!H || !Ja || !Jb) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   Operator* op = as_op(H);
   Guard g(op);
   return run_kpm2d(op, as_op(Ja), as_op(Jb), NC, NR, NH, psi_l, psi_r, static_cast<double2*>(mu),
                    opts, pick_stream(op, stream));
-}
+} KPMGB_ENTRY_CATCH
 
 int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t NC, int64_t NR,
                 int64_t NH, const double* psi_l, const double* psi_r, double* mu,
-                const kpmgb_kpm2d_options* opts) {
+                const kpmgb_kpm2d_options* opts) try {
   clear_error();
   if (!H || !Ja || !Jb) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   if (!psi_l || !psi_r || !mu) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
@@ -856,7 +869,7 @@ int kpmgb_kpm2d(kpmgb_operator H, kpmgb_operator Ja, kpmgb_operator Jb, int64_t 
                       opts, s));
   KPMGB_CUDA(cudaMemcpyAsync(mu, op->ws.mu.ptr, (size_t)NC * NC * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
-}
+} KPMGB_ENTRY_CATCH
 
 }  // extern "C"
 
@@ -1044,16 +1057,16 @@ static int run_ensemble(kpmgb_operator h, int32_t nseg, const int64_t* seg, int6
 
 extern "C" int kpmgb_kpm1d_ensemble(kpmgb_operator h, int32_t nseg, const int64_t* seg,
                                     int64_t NC, int64_t NR, const double* psi, double* mu_all,
-                                    const kpmgb_kpm1d_options* opts) {
+                                    const kpmgb_kpm1d_options* opts) try {
   return run_ensemble(h, nseg, seg, NC, NR, psi, mu_all, opts, nullptr, false);
-}
+} KPMGB_ENTRY_CATCH
 
 extern "C" int kpmgb_kpm1d_ensemble_device(kpmgb_operator h, int32_t nseg, const int64_t* seg,
                                            int64_t NC, int64_t NR, const void* psi, void* mu_all,
-                                           const kpmgb_kpm1d_options* opts, void* stream) {
+                                           const kpmgb_kpm1d_options* opts, void* stream) try {
   return run_ensemble(h, nseg, seg, NC, NR, static_cast<const double*>(psi),
                       static_cast<double*>(mu_all), opts, stream, true);
-}
+} KPMGB_ENTRY_CATCH
 
 // ------------------------------------------------------------ adjoint
 namespace kpmgb {
@@ -1065,7 +1078,7 @@ int run_kpm1d_grad(const DeviceCSR& H, const int* d_perm, int64_t NC, int NR, in
 
 extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_t NH,
                                 const double* psi, const double* g, int64_t checkpoint_every,
-                                double* grad) {
+                                double* grad) try {
   clear_error();
   if (!h || !psi || !g || !grad) return fail(KPMGB_ERR_ARGUMENT, "null argument");
   if (NC < 4 || NC % 2 != 0) return fail(KPMGB_ERR_ARGUMENT, "Invalid NC: NC should be even and >= 4.");
@@ -1100,7 +1113,7 @@ extern "C" int kpmgb_kpm1d_grad(kpmgb_operator h, int64_t NC, int64_t NR, int64_
   }
   KPMGB_CUDA(cudaMemcpyAsync(grad, gcsc, (size_t)op->csr.nnz * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
-}
+} KPMGB_ENTRY_CATCH
 
 // ------------------------------------------------------- kpm_2d gradient
 namespace kpmgb {
@@ -1127,7 +1140,7 @@ extern "C" int kpmgb_kpm2d_grad(kpmgb_operator h, kpmgb_operator ja, kpmgb_opera
                                 kpmgb_operator jbh, int64_t NC, int64_t NR, int64_t NH,
                                 const double* psi_l, const double* psi_r, const double* G,
                                 int32_t moment_parity, double* grad_H, double* grad_Ja,
-                                double* grad_Jb) {
+                                double* grad_Jb) try {
   clear_error();
   if (!h || !ja || !jb || !jbh) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   if (!psi_l || !psi_r || !G || !grad_H || !grad_Ja || !grad_Jb)
@@ -1214,7 +1227,7 @@ extern "C" int kpmgb_kpm2d_grad(kpmgb_operator h, kpmgb_operator ja, kpmgb_opera
   }
   KPMGB_CUDA(cudaStreamSynchronize(s));
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
 // ------------------------------------------------------- chebyshev_action
 namespace kpmgb {
@@ -1225,7 +1238,7 @@ int run_chebyshev_action(Operator* op, int64_t NH, int64_t NR, const double2* V_
 
 extern "C" int kpmgb_chebyshev_action(kpmgb_operator h, int64_t NH, int64_t NR, const double* V,
                                       int64_t NC, int64_t K, const double* C,
-                                      int64_t check_every, double* out) {
+                                      int64_t check_every, double* out) try {
   clear_error();
   if (!h || !V || !C || !out) return fail(KPMGB_ERR_ARGUMENT, "null argument");
   if (NC < 1) return fail(KPMGB_ERR_ARGUMENT, "C must have at least one coefficient row");
@@ -1261,12 +1274,12 @@ extern "C" int kpmgb_chebyshev_action(kpmgb_operator h, int64_t NH, int64_t NR, 
                                  ws.gemm.as<double2>(), check_every, ws.right.as<double2>(), s));
   KPMGB_CUDA(cudaMemcpyAsync(out, ws.right.ptr, (size_t)K * blk, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
-}
+} KPMGB_ENTRY_CATCH
 
 // --------------------------------------------------------- kpm_1d_current
 extern "C" int kpmgb_kpm1d_current(kpmgb_operator h, kpmgb_operator jadj, int64_t NC, int64_t NR,
                                    int64_t NH, const double* psi, double* mu_all,
-                                   const kpmgb_kpm1d_options* opts) {
+                                   const kpmgb_kpm1d_options* opts) try {
   clear_error();
   if (!h || !jadj) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   if (!psi || !mu_all) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
@@ -1302,7 +1315,7 @@ extern "C" int kpmgb_kpm1d_current(kpmgb_operator h, kpmgb_operator jadj, int64_
   KPMGB_TRY(run_kpm1d(op, NC, NR, NH, in + blk, in, ws.mu.as<double2>(), opts, s, true));
   KPMGB_CUDA(cudaMemcpyAsync(mu_all, ws.mu.ptr, (size_t)NR * NC * 16, cudaMemcpyDeviceToHost, s));
   return check_status(op, s);
-}
+} KPMGB_ENTRY_CATCH
 
 // ------------------------------------------------------------------ kpm_3d
 // kpm_3d!(H, Ja, Jb, Jc, NC, NR, NH, mu, psi_in_l, psi_in_r)
@@ -1312,7 +1325,7 @@ extern "C" int kpmgb_kpm1d_current(kpmgb_operator h, kpmgb_operator jadj, int64_
 extern "C" int kpmgb_kpm3d(kpmgb_operator h, kpmgb_operator ja, kpmgb_operator jb,
                            kpmgb_operator jc, int64_t NC, int64_t NR, int64_t NH,
                            const double* psi_l, const double* psi_r, double* mu,
-                           const kpmgb_kpm2d_options* opts) {
+                           const kpmgb_kpm2d_options* opts) try {
   clear_error();
   if (!h || !ja || !jb || !jc) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   if (!psi_l || !psi_r || !mu) return fail(KPMGB_ERR_ARGUMENT, "null buffer");
@@ -1370,7 +1383,7 @@ extern "C" int kpmgb_kpm3d(kpmgb_operator h, kpmgb_operator ja, kpmgb_operator j
     KPMGB_TRY(check_status(op, s));
   }
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
 // ------------------------------------------------------------- self-test
 // Drives the bounded-wait error path of the single-launch kernel: a grid
@@ -1378,7 +1391,7 @@ extern "C" int kpmgb_kpm3d(kpmgb_operator h, kpmgb_operator ja, kpmgb_operator j
 // sets) gives up after a short spin, every block records TIMEOUT and leaves,
 // and the host maps the status to KPMGB_ERR_TIMEOUT.  The context stays
 // usable.  Returns KPMGB_ERR_TIMEOUT when the path works.
-extern "C" int kpmgb_selftest_wait_expiry(kpmgb_operator h) {
+extern "C" int kpmgb_selftest_wait_expiry(kpmgb_operator h) try {
   clear_error();
   if (!h) return fail(KPMGB_ERR_ARGUMENT, "null operator");
   Operator* op = as_op(h);
@@ -1398,4 +1411,4 @@ extern "C" int kpmgb_selftest_wait_expiry(kpmgb_operator h) {
                                ws.mu.as<double2>(), nullptr, 0.0, ws.partials.ptr,
                                ws.partials.bytes, ws.sync.as<unsigned>(), s, 1u, 4096));
   return check_status(op, s);
-}
+} KPMGB_ENTRY_CATCH

@@ -29,6 +29,15 @@ extern std::atomic<int64_t> g_launches;
                            cudaGetErrorString(e_), __FILE__, __LINE__);        \
   } while (0)
 
+// Every int-returning entry point is a function-try-block ending in
+// KPMGB_ENTRY_CATCH, so no C++ exception (a failed host allocation) crosses
+// the C ABI: it becomes KPMGB_ERR_ALLOC or KPMGB_ERR_CUDA with a message.
+int exception_status() noexcept;
+#define KPMGB_ENTRY_CATCH \
+  catch (...) {           \
+    return ::kpmgb::exception_status(); \
+  }
+
 #define KPMGB_TRY(expr)        \
   do {                         \
     int rc_ = (expr);          \

@@ -107,7 +107,7 @@ using namespace kpmgb;
 
 extern "C" int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int32_t* col,
                                    const double* val, int64_t NC, int64_t NR, const double* psi,
-                                   double* mu_all, void* stream) {
+                                   double* mu_all, void* stream) try {
   clear_error();
   if (NH < 1 || NH >= (int64_t(1) << 31)) return fail(KPMGB_ERR_ARGUMENT, "invalid NH=%lld", (long long)NH);
   if (NR < 1 || NR > (1 << 20)) return fail(KPMGB_ERR_ARGUMENT, "invalid NR=%lld", (long long)NR);
@@ -182,4 +182,4 @@ extern "C" int kpmgb_kpm1d_noalloc(int64_t NH, const int32_t* rowptr, const int3
   if (status != 0)
     return fail(KPMGB_ERR_CUDA, "unexpected kernel status 0x%x", status);
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH

@@ -361,7 +361,7 @@ using namespace kpmgb;
 extern "C" int kpmgb_kubo_bastin(const double* mu2d, int64_t ld, int64_t NC, double a, double b,
                                  const double* Ef, int64_t nE, int64_t NH, double area,
                                  double beta, const double* damping, int64_t quad_N,
-                                 double edge_cutoff, double* sigma) {
+                                 double edge_cutoff, double* sigma) try {
   clear_error();
   if (!mu2d || !Ef || !sigma) return fail(KPMGB_ERR_ARGUMENT, "null argument");
   if (!(a > 0)) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: a must be positive.");
@@ -433,11 +433,11 @@ extern "C" int kpmgb_kubo_bastin(const double* mu2d, int64_t ld, int64_t NC, dou
   KPMGB_CUDA(cudaMemcpyAsync(sigma, d_sig, nE * sizeof(double), cudaMemcpyDeviceToHost, cs.s));
   KPMGB_CUDA(cudaStreamSynchronize(cs.s));
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
 extern "C" int kpmgb_kubo_bastin_weights(int64_t NC, double a, double b, double Ef, int64_t NH,
                                          double area, double beta, const double* damping,
-                                         int64_t quad_N, double edge_cutoff, double* W) {
+                                         int64_t quad_N, double edge_cutoff, double* W) try {
   clear_error();
   if (!W) return fail(KPMGB_ERR_ARGUMENT, "null argument");
   if (!(a > 0)) return fail(KPMGB_ERR_ARGUMENT, "kubo_bastin_cond: a must be positive.");
@@ -502,20 +502,20 @@ extern "C" int kpmgb_kubo_bastin_weights(int64_t NC, double a, double b, double 
                              cs.s));
   KPMGB_CUDA(cudaStreamSynchronize(cs.s));
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
 extern "C" int kpmgb_dos_derivative(const double* mu, int64_t NC, double a, double b,
                                     const double* damping, const double* E, int64_t nE,
                                     int32_t dE_order, double* rho);
 
 extern "C" int kpmgb_dos(const double* mu, int64_t NC, double a, double b, const double* damping,
-                         const double* E, int64_t nE, double* rho) {
+                         const double* E, int64_t nE, double* rho) try {
   return kpmgb_dos_derivative(mu, NC, a, b, damping, E, nE, 0, rho);
-}
+} KPMGB_ENTRY_CATCH
 
 extern "C" int kpmgb_dos_derivative(const double* mu, int64_t NC, double a, double b,
                                     const double* damping, const double* E, int64_t nE,
-                                    int32_t dE_order, double* rho) {
+                                    int32_t dE_order, double* rho) try {
   clear_error();
   if (dE_order < 0 || dE_order > kMaxDosOrder)
     return fail(KPMGB_ERR_ARGUMENT, "dos: dE_order must be in 0..%d (got %d)", kMaxDosOrder,
@@ -551,4 +551,4 @@ extern "C" int kpmgb_dos_derivative(const double* mu, int64_t NC, double a, doub
   KPMGB_CUDA(cudaMemcpyAsync(rho, d_rho, nE * sizeof(double), cudaMemcpyDeviceToHost, cs.s));
   KPMGB_CUDA(cudaStreamSynchronize(cs.s));
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH

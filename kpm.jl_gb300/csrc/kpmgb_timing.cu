@@ -66,13 +66,13 @@ void timing_add(int kernel, cudaEvent_t e0, cudaEvent_t e1) {
 
 using namespace kpmgb;
 
-extern "C" int kpmgb_timing_enable(int32_t on) {
+extern "C" int kpmgb_timing_enable(int32_t on) try {
   clear_error();
   g_timing.store(on != 0);
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
 
-extern "C" int kpmgb_timing_read(int32_t kernel, double* total_ms, int64_t* launches) {
+extern "C" int kpmgb_timing_read(int32_t kernel, double* total_ms, int64_t* launches) try {
   clear_error();
   if (kernel < 0 || kernel >= TIMED_COUNT) return fail(KPMGB_ERR_ARGUMENT, "unknown timed kernel %d", kernel);
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
@@ -95,9 +95,9 @@ extern "C" int kpmgb_timing_read(int32_t kernel, double* total_ms, int64_t* laun
   if (total_ms) *total_ms = sum;
   if (launches) *launches = (int64_t)ev.size();
   return rc;
-}
+} KPMGB_ENTRY_CATCH
 
-extern "C" int kpmgb_measure_fp64_peak(double* tflops) {
+extern "C" int kpmgb_measure_fp64_peak(double* tflops) try {
   clear_error();
   if (!tflops) return fail(KPMGB_ERR_ARGUMENT, "null output");
   int dev = 0, sms = 0;
@@ -135,4 +135,4 @@ extern "C" int kpmgb_measure_fp64_peak(double* tflops) {
   const double fma = (double)blocks * 256 * iters * 8;
   *tflops = 2.0 * fma / (best * 1e-3) / 1e12;
   return KPMGB_OK;
-}
+} KPMGB_ENTRY_CATCH
