@@ -344,6 +344,15 @@ def secondary_summary(args):
         ms = _time_device(lambda: kg.kpm_1d_device(op, NC, psi_t, mu_t, precision=prec, stream=st),
                           st, 3, 10, lambda: kg.sync(op, st))
         c1[prec] = {"ms_per_call": ms, "value": NR * NC / 2 / (ms / 1e3)}
+    # the reference's own CPU configuration: the C port of its CPU path, the
+    # whole call on the host cores
+    from oracle import cpu_port
+    nt = cpu_port.max_threads()
+    t0 = time.perf_counter()
+    cpu_port.kpm1d_cpu(h.H, NC, psi, nthreads=nt)
+    dt = time.perf_counter() - t0
+    c1["cpu_baseline"] = {"ms_per_call": dt * 1e3, "value": NR * NC / 2 / dt, "cores": nt,
+                          "kind": "port", "sample": "the whole call (512 steps)"}
     out["c1"] = c1
     # c4
     rng = np.random.default_rng(42)
