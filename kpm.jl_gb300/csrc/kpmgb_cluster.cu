@@ -172,6 +172,10 @@ __global__ void __launch_bounds__(kCT, 1) k_kpm1d_cluster(ClusterParams p) {
     const bool first = n == 1;
     const int dot = p.lr ? (first ? DOT_LR2 : DOT_LR1) : DOT_DOUBLING;
     double2 dd[2] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    // float-float: the dot terms of the thread's rows stay float-float
+    // (leading S, correction Cc; [dot][re/im]) through the warp's sum, so the
+    // step does no FP64 work but one join per warp
+    float fS[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, fC[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
     const uint32_t xbase = slot_base + (uint32_t)(xs * p.rows) * (uint32_t)sizeof(V);
     for (int i = tid; i < own; i += kCT) {
       const int64_t r = r0 + i;
@@ -275,37 +279,51 @@ __global__ void __launch_bounds__(kCT, 1) k_kpm1d_cluster(ClusterParams p) {
           }
         }
       } else {
-        float S[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, Cc[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
         if (dot == DOT_DOUBLING) {
-          ffnorm2(S[0], Cc[0], xr);
-          ffdot(S[1], Cc[1], xr, y);
+          ffnorm2(fS[0], fC[0], xr);
+          ffdot(fS[1], fC[1], xr, y);
         } else {
           const float4 b = __ldg(bra + r * p.NR + c);
           if (dot == DOT_LR2) {
-            ffdot(S[0], Cc[0], b, xr);
-            ffdot(S[1], Cc[1], b, y);
+            ffdot(fS[0], fC[0], b, xr);
+            ffdot(fS[1], fC[1], b, y);
           } else {
-            ffdot(S[0], Cc[0], b, y);
+            ffdot(fS[0], fC[0], b, y);
           }
-        }
-#pragma unroll
-        for (int k = 0; k < 2; ++k) {
-          dd[k].x += ff::join(S[k][0], Cc[k][0]);
-          dd[k].y += ff::join(S[k][1], Cc[k][1]);
         }
       }
       // y overwrites z (this row only; other CTAs read the x slot this step)
       slot[ys * p.rows + i] = y;
     }
     // fixed-order block reduction of the dot terms: a shuffle tree in every
-    // warp, then warp 0 adds the warp sums in warp order
+    // warp (float-float: merged by TwoSum, then joined once), then warp 0
+    // adds the warp sums in warp order
+    if constexpr (FF) {
 #pragma unroll
-    for (int k = 0; k < 2; ++k)
+      for (int off = 16; off > 0; off >>= 1)
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        dd[k].x += __shfl_down_sync(0xffffffffu, dd[k].x, off);
-        dd[k].y += __shfl_down_sync(0xffffffffu, dd[k].y, off);
-      }
+        for (int k = 0; k < 2; ++k)
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            const float s2 = __shfl_down_sync(0xffffffffu, fS[k][q], off);
+            const float c2 = __shfl_down_sync(0xffffffffu, fC[k][q], off);
+            float sum, err;
+            ff::two_sum(fS[k][q], s2, sum, err);
+            fS[k][q] = sum;
+            fC[k][q] = __fadd_rn(fC[k][q], __fadd_rn(c2, err));
+          }
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+        dd[k] = make_double2(ff::join(fS[k][0], fC[k][0]), ff::join(fS[k][1], fC[k][1]));
+    } else {
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          dd[k].x += __shfl_down_sync(0xffffffffu, dd[k].x, off);
+          dd[k].y += __shfl_down_sync(0xffffffffu, dd[k].y, off);
+        }
+    }
     const int warp = tid >> 5, lane = tid & 31;
     if (lane == 0) {
       red[warp] = dd[0];
