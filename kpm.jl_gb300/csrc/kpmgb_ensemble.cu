@@ -190,6 +190,22 @@ __device__ __forceinline__ void ffdacc(float& S, float& C, float ah, float al, f
   ff::dacc(S, C, ah, al, bh, bl);
 }
 
+// Sum of the float-float pair (S, C) over the lanes that share a column (lane
+// offsets LPR, 2 LPR, ... 16), merged by TwoSum: the same result in every
+// lane of the column, with no FP64 work.
+template <int LPR>
+__device__ __forceinline__ void ff_lane_sum(float& S, float& C) {
+#pragma unroll
+  for (int off = LPR; off < 32; off <<= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, S, off);
+    const float c2 = __shfl_xor_sync(0xffffffffu, C, off);
+    float sum, err;
+    ff::two_sum(S, s2, sum, err);
+    S = sum;
+    C = __fadd_rn(C, __fadd_rn(c2, err));
+  }
+}
+
 // Persistent ensemble kernel: LPR lanes per row, one column per lane (NR <= 32).
 template <bool FF, bool REALH, int LPR>
 __global__ void __launch_bounds__(kEnsThreads) k_ensemble(EnsParams p) {
@@ -564,6 +580,9 @@ __global__ void __launch_bounds__(kEnsStepThreads) k_ensemble_step(EnsParams p, 
         ffdacc(S1, C1, xo.z, xo.w, yo.z, yo.w);
       }
     }
+    // the column sums stay float-float until the lanes of a column agree
+    ff_lane_sum<LPR>(S0, C0);
+    ff_lane_sum<LPR>(S1, C1);
     d0.x = ff::join(S0, C0);
     d1.x = ff::join(S1, C1);
   } else if (cc < p.NR) {
@@ -595,11 +614,13 @@ __global__ void __launch_bounds__(kEnsStepThreads) k_ensemble_step(EnsParams p, 
       d1.y = ff::join(S[2], C[2]);
     }
   }
+  if constexpr (!(FF && W > 0)) {  // the padded float-float rows summed their lanes above
 #pragma unroll
-  for (int off = LPR; off < 32; off <<= 1) {
-    d0.x += __shfl_xor_sync(0xffffffffu, d0.x, off);
-    d1.x += __shfl_xor_sync(0xffffffffu, d1.x, off);
-    d1.y += __shfl_xor_sync(0xffffffffu, d1.y, off);
+    for (int off = LPR; off < 32; off <<= 1) {
+      d0.x += __shfl_xor_sync(0xffffffffu, d0.x, off);
+      d1.x += __shfl_xor_sync(0xffffffffu, d1.x, off);
+      d1.y += __shfl_xor_sync(0xffffffffu, d1.y, off);
+    }
   }
   if (lane < LPR) {
     red[warp][0][lane] = d0;
